@@ -1,0 +1,220 @@
+/*
+ * pach_gpu.h -- C ABI of the GB300 (sm_103a) stochastic split ray tracer.
+ *
+ * Drop-in boundary for Pachyderm's SplitRayTracer path.  A host (the C# Simulation_Type shim
+ * through P/Invoke, the C++ mirror in split_ray_tracer.hpp, or Python through ctypes) passes plain
+ * arrays; the library owns every device allocation and handle.  Plain C types only.
+ *
+ * Reference interfaces replaced (paths relative to Pachyderm_Acoustic_Universal/; "TaskAll" is
+ * "Classes_Complete_Trace - TaskAll.cs"):
+ *   pach_scene_create        Polygon_Scene ctor + Construct + partition
+ *                            (Classes_Scenes.cs:70-105, 447-630, 727-755)
+ *   pach_trace_begin         SplitRayTracer ctor + Begin (TaskAll:68-177, 209-240)
+ *   pach_trace_poll          ThreadState / ProgressMsg (TaskAll:246-250, 742-763)
+ *   pach_trace_cancel        Conclude_Simulation / cancellation token (TaskAll:252-255, 276-280)
+ *   pach_trace_wait          the host's poll-until-stopped loop
+ *   pach_trace_get_histograms Combine_ThreadLocal_Results + Receiver_Bank histogram getters
+ *                            (TaskAll:768-774; Classes_Receivers.cs:676-679, 924-927, 1088-1102, 1774-1786)
+ *   pach_trace_get_stats     PercentLost, _currentRay, _rayTotal, _ts (TaskAll:40-47, 776-782)
+ *   pach_medium_properties   Uniform_Medium ctor (Classes_Medium_Props.cs:286-299)
+ *   pach_math_*              AcousticalMath (Classes_Math.cs:272-586, 934-1005)
+ *
+ * Error behaviour: every entry point returns a pach_status; the message of the last failure on
+ * the calling thread is available from pach_last_error.  No callbacks cross the ABI.
+ */
+#ifndef PACH_GPU_H
+#define PACH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PACH_ABI_VERSION 1
+#define PACH_BANDS 8
+
+typedef enum {
+    PACH_OK = 0,
+    PACH_ERR_INVALID_ARGUMENT = 1,
+    PACH_ERR_OUT_OF_MEMORY = 2,
+    PACH_ERR_CUDA = 3,
+    PACH_ERR_TIMEOUT = 4,          /* pach_trace_wait ran out of time; the run continues */
+    PACH_ERR_CANCELLED = 5,
+    PACH_ERR_BOUNDS = 6,           /* a device queue or stack bound was exceeded */
+    PACH_ERR_NOT_READY = 7,
+    PACH_ERR_NO_DEVICE = 8,
+    PACH_ERR_GAVE_UP = 9           /* a bounded device wait or work cap ran out */
+} pach_status;
+
+typedef enum { PACH_RUN_RUNNING = 0, PACH_RUN_STOPPED = 1, PACH_RUN_FAILED = 2, PACH_RUN_CANCELLED = 3 } pach_run_state;
+
+typedef enum {
+    PACH_SOURCE_GEODESIC = 0,      /* GeodesicSource: order-1 icosphere face (ray mod 80) + random point */
+    PACH_SOURCE_RANDOM = 1,        /* RandomSource: theta, phi ~ U[0, 2pi) */
+    PACH_SOURCE_UNIFORM = 2        /* uniform on the sphere */
+} pach_source_kind;
+
+/* Scene: polygons over a shared vertex list (any vertex count; fan-triangulated, polygon id kept),
+ * 8-band absorption / scattering / transmission per polygon, and the air state of the Scene ctor. */
+typedef struct {
+    int32_t n_vertices;
+    const double *vertices;        /* [3*n_vertices] metres */
+    int32_t n_polys;
+    const int32_t *poly_offsets;   /* [n_polys+1] into poly_indices */
+    const int32_t *poly_indices;
+    const double *absorption;      /* [n_polys*8] */
+    const double *scattering;      /* [n_polys*8] */
+    const double *transmission;    /* [n_polys*8] or NULL */
+    double temp_c;                 /* degC */
+    double rel_humidity;           /* percent */
+    double pressure_hpa;           /* hPa, as the Scene ctor (1013.25 = 101.325 kPa) */
+    int32_t air_choice;            /* 0 ISO 9613-1, 1 Evans-Bazley, 2 tables */
+    int32_t edge_correction;
+    int32_t grid_cells_per_tri;    /* uniform-grid density (cells per triangle); 0 = default */
+    int32_t reserved;
+} pach_scene_desc;
+
+typedef struct {
+    double origin[3];
+    double power_db[PACH_BANDS];   /* dB re 1e-12 W per octave band */
+    int32_t kind;                  /* pach_source_kind */
+    int32_t reserved;
+} pach_source_desc;
+
+typedef struct {
+    double origin[3];
+    double radius;                 /* Spherical_Receiver.Radius (the reference ctor fixes 1 m) */
+} pach_receiver_desc;
+
+typedef struct {
+    uint64_t seed;                 /* Philox key; a run is reproducible for a fixed seed */
+    int64_t ray_count;             /* primary rays (SplitRayTracer rayCount > 0) */
+    int64_t ray_begin;             /* index of the first primary: a shard [ray_begin, ray_begin+ray_count)
+                                      draws the same random streams as in an unsharded run */
+    double cutoff_length_m;        /* SplitRayTracer "cutoffTime" argument: a LENGTH, COTime = L / c */
+    int32_t oct_lo, oct_hi;        /* octave range, inclusive, 0 = 62.5 Hz .. 7 = 8 kHz */
+    int32_t is_order;              /* image-source order already covered; -1: rays also record the direct path */
+    int32_t sample_rate;           /* histogram rate Hz (Receiver_Bank SampleRate, 1000 for 1 ms bins) */
+    double hist_cotime_ms;         /* histogram length ms (Receiver_Bank COTime_in) */
+    int32_t pure_specular;         /* 1: all scattering and transmission forced to 0 */
+    int32_t max_broadband_bounces; /* 0 = derived bound from the scene's least lossy surface */
+    int64_t max_segments_per_ray;  /* safety cap on one octave ray (0 = 1<<22) */
+    int64_t queue_budget_items;    /* device queue budget per chunk (0 = default) */
+    int32_t block_threads;         /* 0 = autotuned / default */
+    int32_t blocks_per_sm;         /* 0 = autotuned / default */
+    const double *prim_dirs;       /* optional [ray_count][3] emission directions (importance sampling) */
+    const double *prim_weights;    /* optional [ray_count] emission weights (1/q) */
+} pach_trace_params;
+
+typedef struct {
+    int32_t state;                 /* pach_run_state */
+    int32_t last_status;           /* pach_status of a failed run */
+    int64_t rays_done;             /* _currentRay */
+    int64_t rays_total;
+    int64_t end_traces;            /* _rayTotal ("sub-rays") */
+    int64_t segments;
+} pach_progress;
+
+typedef struct {
+    int64_t primaries;
+    int64_t segments;              /* shoot calls, broadband + octave, hit or miss */
+    int64_t segments_broadband;
+    int64_t segments_phase_b;
+    int64_t segments_phase_c;
+    int64_t octave_rays;
+    int64_t end_traces;
+    int64_t detections;
+    int64_t capped;
+    int64_t fp64_retests;          /* FP32 hits re-tested in FP64 (near edge / grazing) */
+    int64_t queue_overflows;
+    int64_t stack_spills;
+    double lost_energy;            /* W (sum over rays, unscaled) */
+    double initial_energy;
+    double percent_lost;           /* 100 lost / initial (PercentLost) */
+    int32_t h_oct;
+    int32_t bins;
+    double cotime_s;
+    double sound_speed;
+    double rho_c;
+    double air_atten_db_per_m[PACH_BANDS];
+    double device_ms;              /* CUDA-event time of all kernels of the run */
+    double octave_kernel_ms;       /* CUDA-event time of the octave-ray kernel launches */
+    int64_t octave_kernel_launches;
+    int64_t kernel_launches;
+    double wall_ms;
+    int32_t grid_dims[3];
+    int32_t chunks;
+} pach_stats;
+
+typedef struct pach_scene pach_scene;
+typedef struct pach_run pach_run;
+
+const char *pach_version(void);
+/* Copies the last error message of the calling thread; returns its length. */
+int pach_last_error(char *buf, size_t cap);
+/* Number of visible CUDA devices (0 on a machine without a GPU); never fails. */
+int pach_device_count(void);
+
+pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out);
+void pach_scene_destroy(pach_scene *scene);
+/* Scene facts the SplitRayTracer ctor derives (Scene.SurfaceArea, Sound_speed, Rho_C, Attenuation). */
+pach_status pach_scene_info(const pach_scene *scene, int32_t *n_polys, int32_t *n_triangles,
+                            double *sound_speed, double *rho_c, double air_atten_db_per_m[PACH_BANDS],
+                            double *poly_area /* [n_polys] or NULL */);
+
+pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
+                             const pach_receiver_desc *receivers, int32_t n_receivers,
+                             const pach_trace_params *params, pach_run **out);
+pach_status pach_trace_poll(pach_run *run, pach_progress *progress);
+pach_status pach_trace_cancel(pach_run *run);
+/* Blocks until the run stops or timeout_ms passes (timeout_ms < 0: no limit). */
+pach_status pach_trace_wait(pach_run *run, int64_t timeout_ms);
+/* Histograms, layouts energy/pressure [R][8][T], dir_pos/dir_neg [R][3][8][T] (+x,+y,+z arrival
+ * components), analysis [R][3][8][T] (0 specular, 1 diffuse, 2 specular-after-scatter).
+ * scaled = 0: raw sums; 1: Combine_ThreadLocal_Results scaling (energy, dir and analysis / N,
+ * pressure / sqrt(N), then x n_sources, pressure x sqrt(n_sources)).  Any pointer may be NULL.
+ * cap_bins = capacity of each of energy/pressure in doubles (R*8*T). */
+pach_status pach_trace_get_histograms(pach_run *run, int32_t scaled, double *energy, double *pressure,
+                                      double *dir_pos, double *dir_neg, double *analysis, size_t cap_bins);
+pach_status pach_trace_get_stats(pach_run *run, pach_stats *stats);
+void pach_run_destroy(pach_run *run);
+
+/* Synchronous convenience: begin + wait + histograms + stats. */
+pach_status pach_trace_run(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
+                           const pach_receiver_desc *receivers, int32_t n_receivers,
+                           const pach_trace_params *params, int32_t scaled, double *energy, double *pressure,
+                           double *dir_pos, double *dir_neg, double *analysis, size_t cap_bins, pach_stats *stats);
+
+/* Pure-specular paths (oracle (a)): per bounce the hit polygon (-1 = miss), leg length and hit
+ * point, traced by the same device traversal as the tracer. */
+pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double *origins, const double *dirs,
+                                      int32_t max_bounces, int32_t *poly_out, double *t_out, double *pts_out);
+
+/* Emission directions of primaries [ray_begin, ray_begin+n) as the tracer draws them. */
+pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, int32_t n_sources,
+                                 int32_t kind, double *dirs_out);
+
+/* Air: attenuation (dB/m at the 8 octave centres), sound speed (m/s), density (kg/m^3). */
+pach_status pach_medium_properties(double temp_c, double rel_humidity, double pressure_hpa, int32_t air_choice,
+                                   int32_t edge_correction, double atten_db_per_m[PACH_BANDS],
+                                   double *sound_speed, double *rho);
+
+/* AcousticalMath (Classes_Math.cs). */
+pach_status pach_math_schroeder(const double *etc, int32_t n, double *out);              /* 282-299 */
+double pach_math_t_x(const double *schroeder, int32_t n, int32_t decay_depth, int32_t sample_f); /* 511-526 */
+double pach_math_edt(const double *schroeder, int32_t n, int32_t sample_f);              /* 534-549 */
+double pach_math_clarity(const double *etc, int32_t n, double sample_f, double seconds, double start_time,
+                         int32_t pressure);                                               /* 559-586 */
+double pach_math_definition(const double *etc, int32_t n, double sample_f, double seconds, double start_time,
+                            int32_t pressure);                                            /* 934-962 */
+double pach_math_center_time(const double *etc, int32_t n, int32_t sample_f, double direct_time,
+                             int32_t pressure);                                           /* 971-986 */
+double pach_math_strength(const double *etc, int32_t n, double swl, int32_t pressure);   /* 993-1005 */
+double pach_math_sound_speed(double temp_c);                                               /* 272-275 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PACH_GPU_H */

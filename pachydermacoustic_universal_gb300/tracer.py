@@ -1,0 +1,189 @@
+"""Array-level Python API over the C ABI: device scenes, runs, histograms and stats."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import check, dptr, iptr
+
+
+class DeviceScene:
+    """A scene resident on the GPU (pach_scene_create)."""
+
+    def __init__(self, scene, grid_cells_per_tri: int = 0):
+        L = _capi.lib()
+        self._v = np.ascontiguousarray(scene.vertices, dtype=np.float64).reshape(-1)
+        self._o = np.ascontiguousarray(scene.poly_offsets, dtype=np.int32)
+        self._i = np.ascontiguousarray(scene.poly_indices, dtype=np.int32)
+        self._a = np.ascontiguousarray(scene.absorption, dtype=np.float64).reshape(-1)
+        self._s = np.ascontiguousarray(scene.scattering, dtype=np.float64).reshape(-1)
+        tr = getattr(scene, "transmission", None)
+        self._t = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1) if tr is not None else None
+        desc = _capi.SceneDesc(self._v.size // 3, dptr(self._v), self._o.size - 1, iptr(self._o), iptr(self._i),
+                               dptr(self._a), dptr(self._s), dptr(self._t), scene.temp_c, scene.rel_humidity,
+                               scene.pressure_hpa, scene.air_choice, scene.edge_correction, grid_cells_per_tri, 0)
+        h = C.c_void_p()
+        check(L.pach_scene_create(C.byref(desc), C.byref(h)))
+        self.handle = h
+        self.n_polys = self._o.size - 1
+
+    def info(self):
+        L = _capi.lib()
+        npoly, ntri = C.c_int32(), C.c_int32()
+        c, rc = C.c_double(), C.c_double()
+        att = np.zeros(8)
+        area = np.zeros(self.n_polys)
+        check(L.pach_scene_info(self.handle, C.byref(npoly), C.byref(ntri), C.byref(c), C.byref(rc), dptr(att), dptr(area)))
+        return {"n_polys": npoly.value, "n_triangles": ntri.value, "sound_speed": c.value, "rho_c": rc.value,
+                "air_atten_db_per_m": att, "poly_area": area}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.lib().pach_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def source_array(sources):
+    arr = (_capi.SourceDesc * len(sources))()
+    for i, s in enumerate(sources):
+        arr[i].origin[:] = [float(x) for x in s.origin]
+        arr[i].power_db[:] = [float(x) for x in s.power_db]
+        arr[i].kind = int(s.kind)
+    return arr
+
+
+def receiver_array(receivers):
+    arr = (_capi.ReceiverDesc * max(1, len(receivers)))()
+    for i, r in enumerate(receivers):
+        arr[i].origin[:] = [float(x) for x in r.origin]
+        arr[i].radius = float(r.radius)
+    return arr
+
+
+def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 7), is_order=-1, sample_rate=1000,
+                pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, queue_budget_items=0,
+                block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0):
+    p = _capi.TraceParams()
+    p.seed = seed
+    p.ray_count = int(rays)
+    p.ray_begin = int(ray_begin)
+    p.cutoff_length_m = float(cutoff_length_m)
+    p.oct_lo, p.oct_hi = int(oct_range[0]), int(oct_range[1])
+    p.is_order = int(is_order)
+    p.sample_rate = int(sample_rate)
+    p.hist_cotime_ms = float(hist_cotime_ms)
+    p.pure_specular = int(bool(pure_specular))
+    p.max_broadband_bounces = int(max_broadband_bounces)
+    p.max_segments_per_ray = int(max_segments_per_ray)
+    p.queue_budget_items = int(queue_budget_items)
+    p.block_threads = int(block_threads)
+    p.blocks_per_sm = int(blocks_per_sm)
+    p.prim_dirs = dptr(prim_dirs)
+    p.prim_weights = dptr(prim_weights)
+    return p
+
+
+class Run:
+    """An asynchronous tracing run (pach_trace_begin ... pach_run_destroy)."""
+
+    def __init__(self, dscene: DeviceScene, sources, receivers, params, keep=()):
+        L = _capi.lib()
+        self._src = source_array(sources)
+        self._rec = receiver_array(receivers)
+        self._keep = keep
+        self.R = len(receivers)
+        self.params = params
+        self.T = int(params.sample_rate * params.hist_cotime_ms / 1000.0)
+        h = C.c_void_p()
+        check(L.pach_trace_begin(dscene.handle, self._src, len(sources), self._rec, len(receivers), C.byref(params),
+                                 C.byref(h)))
+        self.handle = h
+
+    def poll(self):
+        pr = _capi.Progress()
+        check(_capi.lib().pach_trace_poll(self.handle, C.byref(pr)))
+        return {k: getattr(pr, k) for k, _ in pr._fields_}
+
+    def cancel(self):
+        check(_capi.lib().pach_trace_cancel(self.handle))
+
+    def wait(self, timeout_ms=-1):
+        check(_capi.lib().pach_trace_wait(self.handle, timeout_ms))
+
+    def histograms(self, scaled=False):
+        R, T = self.R, self.T
+        E = np.zeros((R, 8, T))
+        P = np.zeros((R, 8, T))
+        Dp = np.zeros((R, 3, 8, T))
+        Dn = np.zeros((R, 3, 8, T))
+        An = np.zeros((R, 3, 8, T))
+        check(_capi.lib().pach_trace_get_histograms(self.handle, int(bool(scaled)), dptr(E), dptr(P), dptr(Dp),
+                                                    dptr(Dn), dptr(An), E.size))
+        return {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}
+
+    def stats(self):
+        s = _capi.Stats()
+        check(_capi.lib().pach_trace_get_stats(self.handle, C.byref(s)))
+        return s.to_dict()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.lib().pach_run_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, **kw):
+    """Trace a rooms.Workload on the GPU; returns (histograms, stats)."""
+    ds = dscene or DeviceScene(workload.scene)
+    n = workload.rays if rays is None else rays
+    pd = kw.pop("prim_dirs", None)
+    pw = kw.pop("prim_weights", None)
+    pd = np.ascontiguousarray(pd, dtype=np.float64) if pd is not None else None
+    pw = np.ascontiguousarray(pw, dtype=np.float64) if pw is not None else None
+    params = make_params(rays=n, cutoff_length_m=workload.cutoff_length_m, hist_cotime_ms=workload.cutoff_s * 1000.0,
+                         seed=seed, sample_rate=workload.sample_rate, prim_dirs=pd, prim_weights=pw, **kw)
+    run = Run(ds, workload.sources, workload.receivers, params, keep=(pd, pw))
+    try:
+        run.wait()
+        return run.histograms(scaled=scaled), run.stats()
+    finally:
+        run.close()
+
+
+def specular_paths(dscene: DeviceScene, origins, dirs, max_bounces):
+    o = np.ascontiguousarray(origins, dtype=np.float64)
+    d = np.ascontiguousarray(dirs, dtype=np.float64)
+    n = o.shape[0]
+    poly = np.zeros((n, max_bounces), dtype=np.int32)
+    t = np.zeros((n, max_bounces))
+    pts = np.zeros((n, max_bounces, 3))
+    check(_capi.lib().pach_trace_specular_paths(dscene.handle, n, dptr(o), dptr(d), max_bounces, iptr(poly), dptr(t),
+                                                dptr(pts)))
+    return poly, t, pts
+
+
+def emit_directions(seed, ray_begin, n, n_sources, kind):
+    out = np.zeros((n, 3))
+    check(_capi.lib().pach_emit_directions(seed, ray_begin, n, n_sources, kind, dptr(out)))
+    return out
+
+
+def medium_properties(temp_c=20.0, hr=50.0, pa_hpa=1013.25, air_choice=0, edge=0):
+    att = np.zeros(8)
+    c, rho = C.c_double(), C.c_double()
+    check(_capi.lib().pach_medium_properties(temp_c, hr, pa_hpa, air_choice, edge, dptr(att), C.byref(c), C.byref(rho)))
+    return att, c.value, rho.value

@@ -1,0 +1,222 @@
+"""CPU checks: the oracle against the committed known answers, and the engine's host-side parts
+(C ABI exports, air model, parameter functions, argument validation) against the oracle.
+None of these launch a kernel."""
+import json
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pachydermacoustic_universal_gb300 import rooms, _capi, tracer
+from pachydermacoustic_universal_gb300.simulation import AcousticalMath
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def load(name):
+    with open(os.path.join(GOLD, name)) as f:
+        return json.load(f)
+
+
+# ---------------------------------------------------------------- RNG
+def test_philox_known_answers():
+    for v in load("philox_kat.json"):
+        assert O.philox(*v["ctr"], *v["key"]) == v["out"]
+
+
+# ---------------------------------------------------------------- air (Classes_Medium_Props.cs)
+@pytest.mark.parametrize("case", load("iso9613.json"))
+def test_air_model_oracle_and_engine_match_fixture(case):
+    att_o, c_o, rho_o = O.medium(case["temp_c"], case["hr"], case["pa_hpa"])
+    att_e, c_e, rho_e = tracer.medium_properties(case["temp_c"], case["hr"], case["pa_hpa"])
+    ref = np.array(case["atten_db_per_m"])
+    np.testing.assert_allclose(att_o, ref, rtol=1e-12)
+    np.testing.assert_allclose(att_e, ref, rtol=1e-12)
+    assert c_o == pytest.approx(case["c"], rel=1e-15) and c_e == pytest.approx(case["c"], rel=1e-15)
+    assert rho_o == pytest.approx(case["rho"], rel=1e-13) and rho_e == pytest.approx(case["rho"], rel=1e-13)
+
+
+def test_air_model_iso_table_values_at_20c_50pct():
+    # ISO 9613-1 Table 1 (20 degC, 50 % RH, 101.325 kPa): 4.66 dB/km at 1 kHz, 9.86 at 2 kHz, 29.7 at 4 kHz
+    att, c, _ = tracer.medium_properties(20.0, 50.0, 1013.25)
+    assert att[4] * 1000 == pytest.approx(4.66, abs=0.01)
+    assert att[5] * 1000 == pytest.approx(9.86, abs=0.05)
+    assert att[6] * 1000 == pytest.approx(29.7, abs=0.1)
+    assert c == 343.0
+
+
+@pytest.mark.parametrize("choice", [1, 2])
+def test_air_alternatives_match_oracle(choice):
+    for hr in (40.0, 60.0, 80.0):
+        a_o, _, _ = O.medium(22.0, hr, 1013.25, choice, 1)
+        a_e, _, _ = tracer.medium_properties(22.0, hr, 1013.25, choice, 1)
+        np.testing.assert_allclose(a_e, a_o, rtol=1e-14)
+
+
+# ---------------------------------------------------------------- geometry
+def _shoebox(L):
+    b = rooms._Builder()
+    rooms._box_faces(b, (0, 0, 0), L)
+    v, offs, idx = b.arrays()
+    P = offs.size - 1
+    return rooms.SceneArrays(v, offs, idx, np.full((P, 8), 0.1), np.zeros((P, 8)), np.zeros((P, 8)))
+
+
+# face index in rooms._box_faces order -> (axis, side)
+FACE_AXIS_SIDE = {0: (2, 0), 1: (2, 1), 2: (1, 0), 3: (1, 1), 4: (0, 1), 5: (0, 0)}
+
+
+@pytest.mark.parametrize("brute", [False, True])
+def test_oracle_specular_paths_match_image_lattice(brute):
+    g = load("shoebox_paths.json")
+    sc = _shoebox(tuple(g["size"]))
+    o = np.array([r["origin"] for r in g["rays"]])
+    d = np.array([r["dir"] for r in g["rays"]])
+    nb = len(g["rays"][0]["legs"])
+    poly, t, pts = O.specular_paths(sc, o, d, nb, brute_force=brute)
+    for i, r in enumerate(g["rays"]):
+        for b in range(nb):
+            assert FACE_AXIS_SIDE[poly[i, b] // 2] == tuple(r["walls"][b]), (i, b)
+        np.testing.assert_allclose(t[i], r["legs"], rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(pts[i], r["points"], atol=1e-8)
+
+
+def test_oracle_grid_equals_brute_force_in_irregular_hall():
+    w = rooms.irregular_hall_c2(target_tris=3000)
+    rng = np.random.default_rng(5)
+    lo, hi = w.scene.bounds()
+    for dom in (7, 23):
+        for _ in range(200):
+            o = rng.uniform(lo + 3, hi - 3)
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            pg, tg, _ = O.shoot(w.scene, o, d, grid_domain=dom)
+            pb, tb, _ = O.shoot(w.scene, o, d, brute_force=True)
+            assert pg == pb and tg == pytest.approx(tb, rel=1e-12)
+
+
+def test_oracle_trace_grid_and_brute_force_agree():
+    w = rooms.shoebox_c1()
+    h1, s1 = O.trace(w, rays=64, threads=4)
+    h2, s2 = O.trace(w, rays=64, threads=4, brute_force=True)
+    assert s1["segments"] == s2["segments"]
+    np.testing.assert_allclose(h1["energy"], h2["energy"], rtol=1e-9, atol=0)
+
+
+def test_oracle_threads_do_not_change_results():
+    w = rooms.shoebox_c1()
+    h1, s1 = O.trace(w, rays=48, threads=1)
+    h2, s2 = O.trace(w, rays=48, threads=6)
+    assert s1["segments"] == s2["segments"] and s1["detections"] == s2["detections"]
+    np.testing.assert_allclose(h1["energy"], h2["energy"], rtol=1e-12, atol=1e-300)
+
+
+def test_oracle_energy_bookkeeping_pure_specular_lossless_air():
+    """Pure specular, one band path: every primary's energy is either absorbed, lost, or still in
+    flight at the cutoff.  With 100 % absorbing walls a broadband ray ends at its first wall."""
+    w = rooms.shoebox_c1()
+    w.scene.absorption[:] = 1.0
+    h, st = O.trace(w, rays=200, threads=2, pure_specular=True)
+    # phase A: 1 bounce (E drops to 0 <= TP1); Scatter_Early skips bands whose energy is 0
+    # (Classes_Materials.cs:4508), so only the 8 final-split rays remain, each 1 bounce in B and C
+    assert st["segments_broadband"] == 200
+    assert st["octave_rays"] == 200 * 8
+    assert st["segments_phase_b"] == 200 * 8 and st["segments_phase_c"] == 200 * 8
+    assert st["lost_energy"] == 0.0
+
+
+# ---------------------------------------------------------------- room-acoustic parameters
+@pytest.mark.parametrize("case", load("decay_params.json"))
+def test_parameters_on_ideal_exponential_decay(case):
+    fs, n, k = case["fs"], case["n"], case["rate"]
+    etc = np.exp(-k * np.arange(n) / fs)
+    sch_o = O.schroeder(etc)
+    sch_e = AcousticalMath.Schroeder_Integral(etc)
+    np.testing.assert_allclose(sch_e, sch_o, rtol=1e-14, atol=1e-16)
+    for f_o, f_e in ((O.t_x(sch_o, 30, fs), AcousticalMath.T_X(sch_e, 30, fs)),
+                     (O.edt(sch_o, fs), AcousticalMath.EarlyDecayTime(sch_e, fs))):
+        assert f_o == pytest.approx(case["T"], rel=2e-3)
+        assert f_e == pytest.approx(f_o, rel=1e-12)
+    assert O.clarity(etc, fs, 0.08, 0.0) == pytest.approx(case["C80"], abs=1e-9)
+    assert AcousticalMath.Clarity(etc, fs, 0.08, 0.0, False) == pytest.approx(case["C80"], abs=1e-9)
+    assert O.definition(etc, fs, 0.05, 0.0) == pytest.approx(case["D50"], rel=1e-9)
+    assert AcousticalMath.Definition(etc, fs, 0.05, 0.0, False) == pytest.approx(case["D50"], rel=1e-9)
+
+
+def test_parameter_functions_engine_equals_oracle_on_noisy_curves():
+    rng = np.random.default_rng(3)
+    for trial in range(20):
+        n = int(rng.integers(500, 4000))
+        etc = rng.exponential(size=n) * np.exp(-rng.uniform(3, 30) * np.arange(n) / 1000.0)
+        etc[: int(rng.integers(0, 40))] = 0.0
+        start = float(rng.uniform(0, 0.03))
+        sch = O.schroeder(etc)
+        assert AcousticalMath.T_X(sch, 30, 1000) == pytest.approx(O.t_x(sch, 30, 1000), rel=1e-12, nan_ok=True)
+        assert AcousticalMath.T_X(sch, 20, 1000) == pytest.approx(O.t_x(sch, 20, 1000), rel=1e-12, nan_ok=True)
+        assert AcousticalMath.EarlyDecayTime(sch, 1000) == pytest.approx(O.edt(sch, 1000), rel=1e-12, nan_ok=True)
+        assert AcousticalMath.Clarity(etc, 1000, 0.08, start, False) == pytest.approx(O.clarity(etc, 1000, 0.08, start), rel=1e-12)
+        assert AcousticalMath.Definition(etc, 1000, 0.05, start, False) == pytest.approx(O.definition(etc, 1000, 0.05, start), rel=1e-12)
+        assert AcousticalMath.Center_Time(etc, 1000, start, False) == pytest.approx(O.center_time(etc, 1000, start), rel=1e-12)
+        assert AcousticalMath.Strength(etc, 120.0, False) == pytest.approx(O.strength(etc, 120.0), rel=1e-12)
+
+
+# ---------------------------------------------------------------- the C ABI
+def test_library_exports_every_declared_symbol():
+    header = open(os.path.join(ROOT, "include", "pach_gpu.h")).read()
+    declared = set(re.findall(r"\b(pach_[a-z0-9_]+)\s*\(", header))
+    assert declared == set(_capi.EXPORTS)
+    L = _capi.lib()
+    for name in declared:
+        assert hasattr(L, name), name
+
+
+def test_no_cpu_fallback_without_device():
+    if _capi.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    w = rooms.shoebox_c1()
+    with pytest.raises(_capi.PachError) as ei:
+        tracer.DeviceScene(w.scene)
+    assert ei.value.status == 8  # PACH_ERR_NO_DEVICE
+
+
+def test_scene_validation_errors():
+    w = rooms.shoebox_c1()
+    bad = rooms.SceneArrays(w.scene.vertices.copy(), w.scene.poly_offsets, w.scene.poly_indices,
+                            w.scene.absorption, w.scene.scattering, w.scene.transmission)
+    bad.vertices[0, 0] = np.nan
+    with pytest.raises(_capi.PachError) as ei:
+        tracer.DeviceScene(bad)
+    assert ei.value.status == 1
+    bad2 = rooms.SceneArrays(w.scene.vertices, w.scene.poly_offsets, w.scene.poly_indices,
+                             w.scene.absorption * 5, w.scene.scattering, w.scene.transmission)
+    with pytest.raises(_capi.PachError) as ei:
+        tracer.DeviceScene(bad2)
+    assert ei.value.status == 1 and "[0, 1]" in str(ei.value)
+    offs = w.scene.poly_offsets.copy()
+    idx = w.scene.poly_indices.copy()
+    idx[3] = 10_000
+    with pytest.raises(_capi.PachError):
+        tracer.DeviceScene(rooms.SceneArrays(w.scene.vertices, offs, idx, w.scene.absorption, w.scene.scattering,
+                                             w.scene.transmission))
+
+
+def test_medium_argument_errors():
+    with pytest.raises(_capi.PachError):
+        tracer.medium_properties(20.0, -1.0, 1013.25)
+    with pytest.raises(_capi.PachError):
+        tracer.medium_properties(20.0, 50.0, 1013.25, air_choice=7)
+
+
+# ---------------------------------------------------------------- workloads
+def test_workload_generators_have_the_named_shapes():
+    c1 = rooms.shoebox_c1()
+    assert c1.scene.n_triangles == 12 and len(c1.receivers) == 3 and c1.rays == 100_000
+    assert np.all((c1.scene.absorption >= 0.05) & (c1.scene.absorption <= 0.35))
+    c2 = rooms.irregular_hall_c2()
+    assert 19_000 <= c2.scene.n_triangles <= 21_000 and len(c2.sources) == 2 and len(c2.receivers) == 16
+    lo, hi = c2.scene.bounds()
+    assert np.all(hi - lo > np.array([39, 24, 14]))
