@@ -72,8 +72,8 @@ typedef struct {
     double pressure_hpa;           /* hPa, as the Scene ctor (1013.25 = 101.325 kPa) */
     int32_t air_choice;            /* 0 ISO 9613-1, 1 Evans-Bazley, 2 tables */
     int32_t edge_correction;
-    int32_t grid_cells_per_tri;    /* uniform-grid density (cells per triangle); 0 = default */
-    int32_t reserved;
+    int32_t reserved0;
+    int32_t reserved1;
 } pach_scene_desc;
 
 typedef struct {
@@ -101,9 +101,13 @@ typedef struct {
     int32_t pure_specular;         /* 1: all scattering and transmission forced to 0 */
     int32_t max_broadband_bounces; /* 0 = derived bound from the scene's least lossy surface */
     int64_t max_segments_per_ray;  /* safety cap on one octave ray (0 = 1<<22) */
-    int64_t queue_budget_items;    /* device queue budget per chunk (0 = default) */
-    int32_t block_threads;         /* 0 = autotuned / default */
-    int32_t blocks_per_sm;         /* 0 = autotuned / default */
+    int64_t feed_batch;            /* primaries handed to the device per phase-A launch (0 = default) */
+    int32_t block_threads;         /* threads per block of the trace and shade kernels; 0 = default */
+    int32_t blocks_per_sm;         /* resident blocks per SM to launch; 0 = occupancy maximum */
+    int32_t wave_kilo_items;       /* octave rays per wave, in units of 1024; 0 = default */
+    int32_t ring_log2;             /* ring queue capacity 2^ring_log2 octave rays; 0 = default */
+    int32_t kernel_timing;         /* 1: CUDA events around every kernel (per-kernel times in pach_stats) */
+    int32_t reserved;
     const double *prim_dirs;       /* optional [ray_count][3] emission directions (importance sampling) */
     const double *prim_weights;    /* optional [ray_count] emission weights (1/q) */
 } pach_trace_params;
@@ -140,12 +144,17 @@ typedef struct {
     double rho_c;
     double air_atten_db_per_m[PACH_BANDS];
     double device_ms;              /* CUDA-event time of all kernels of the run */
-    double octave_kernel_ms;       /* CUDA-event time of the octave-ray kernel launches */
-    int64_t octave_kernel_launches;
+    double trace_ms;               /* per-kernel CUDA-event times (kernel_timing = 1, else 0) */
+    double shade_ms;
+    double broadband_ms;
+    int64_t waves;                 /* wavefront iterations that traced octave rays */
     int64_t kernel_launches;
+    int64_t peak_live_rays;        /* most octave rays held in the ring at once */
+    int64_t bvh_nodes_visited;     /* octave-ray traversal work: inner BVH nodes visited */
+    int64_t tri_tests;             /* octave-ray traversal work: triangles tested */
     double wall_ms;
-    int32_t grid_dims[3];
-    int32_t chunks;
+    int32_t accel[3];              /* BVH inner nodes, leaves, depth */
+    int32_t reserved;
 } pach_stats;
 
 typedef struct pach_scene pach_scene;
@@ -191,6 +200,12 @@ pach_status pach_trace_run(pach_scene *scene, const pach_source_desc *sources, i
  * point, traced by the same device traversal as the tracer. */
 pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double *origins, const double *dirs,
                                       int32_t max_bounces, int32_t *poly_out, double *t_out, double *pts_out);
+
+/* Builds the scene's BVH on the host and walks it for each ray (FP32 boxes as on the device, FP64
+ * triangle tests, t > 1e-10): checks the acceleration structure the kernels use without a GPU.
+ * poly_out = -1 on a miss. */
+pach_status pach_scene_shoot_host(const pach_scene_desc *desc, int32_t n, const double *origins, const double *dirs,
+                                  int32_t *poly_out, double *t_out);
 
 /* Emission directions of primaries [ray_begin, ray_begin+n) as the tracer draws them. */
 pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, int32_t n_sources,

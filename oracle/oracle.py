@@ -46,7 +46,7 @@ class OrcStats(C.Structure):
     _fields_ = [("primaries", C.c_int64), ("segments", C.c_int64), ("segments_broadband", C.c_int64),
                 ("segments_phase_b", C.c_int64), ("segments_phase_c", C.c_int64), ("octave_rays", C.c_int64),
                 ("end_traces", C.c_int64), ("detections", C.c_int64), ("capped", C.c_int64),
-                ("lost_energy", C.c_double), ("initial_energy", C.c_double), ("h_oct", C.c_int32),
+                ("cells_visited", C.c_int64), ("tri_tests", C.c_int64), ("lost_energy", C.c_double), ("initial_energy", C.c_double), ("h_oct", C.c_int32),
                 ("bins", C.c_int32), ("cotime_s", C.c_double), ("sound_speed", C.c_double), ("rho_c", C.c_double),
                 ("air_atten_db_per_m", C.c_double * 8)]
 

@@ -283,12 +283,14 @@ struct Tracer {
     const Scene &S;
     std::vector<uint32_t> mail;
     uint32_t stamp = 0;
+    int64_t cells_visited = 0, tri_tests = 0;   /* algorithm-defined work of the reference traversal */
     explicit Tracer(const Scene &s) : S(s), mail(s.tris.size(), 0) {}
 
     bool shoot(V3 o, V3 d, Hit &h) {
         const double EPS = 0.0000000001;
         if (S.brute) {
             double best = 1e300; int bi = -1;
+            tri_tests += (int64_t)S.tris.size();
             for (int i = 0; i < (int)S.tris.size(); ++i) {
                 double t;
                 if (hit_tri(S.tris[i], o, d, t) && t > EPS && t < best) { best = t; bi = i; }
@@ -322,9 +324,11 @@ struct Tracer {
         double tDZ = d.z != 0 ? std::fabs(S.cell.z / d.z) : 1e300;
         double best = 1e300; int bi = -1;
         for (int guard = 0; guard < 3 * S.D + 3; ++guard) {
+            ++cells_visited;
             for (int i : S.cells[((size_t)X * S.D + Y) * S.D + Z]) {
                 if (mail[i] == stamp) continue;
                 mail[i] = stamp;
+                ++tri_tests;
                 double t;
                 if (hit_tri(S.tris[i], o, d, t) && t > EPS && t < best) { best = t; bi = i; }
             }
@@ -835,6 +839,7 @@ int orc_trace_ex(const orc_scene_desc *scene, int32_t n_src, const orc_source *s
         out.segments_broadband += w.st.segments_broadband; out.segments_phase_b += w.st.segments_phase_b;
         out.segments_phase_c += w.st.segments_phase_c; out.octave_rays += w.st.octave_rays;
         out.end_traces += w.st.end_traces; out.detections += w.st.detections; out.capped += w.st.capped;
+        out.cells_visited += w.tr.cells_visited; out.tri_tests += w.tr.tri_tests;
         out.lost_energy += w.st.lost_energy; out.initial_energy += w.st.initial_energy;
         delete W[t];
     }

@@ -78,6 +78,8 @@ typedef struct {
     int64_t end_traces;            /* _rayTotal: octave rays entering End_Trace */
     int64_t detections;
     int64_t capped;                /* rays stopped by a safety cap */
+    int64_t cells_visited;         /* voxel cells stepped by the reference traversal (all segments) */
+    int64_t tri_tests;             /* polygon tests after mailboxing (all segments) */
     double lost_energy;
     double initial_energy;
     int32_t h_oct;

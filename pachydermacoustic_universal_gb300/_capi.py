@@ -28,8 +28,8 @@ class SceneDesc(C.Structure):
     _fields_ = [("n_vertices", C.c_int32), ("vertices", _dp), ("n_polys", C.c_int32), ("poly_offsets", _ip),
                 ("poly_indices", _ip), ("absorption", _dp), ("scattering", _dp), ("transmission", _dp),
                 ("temp_c", C.c_double), ("rel_humidity", C.c_double), ("pressure_hpa", C.c_double),
-                ("air_choice", C.c_int32), ("edge_correction", C.c_int32), ("grid_cells_per_tri", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("air_choice", C.c_int32), ("edge_correction", C.c_int32), ("reserved0", C.c_int32),
+                ("reserved1", C.c_int32)]
 
 
 class SourceDesc(C.Structure):
@@ -44,8 +44,10 @@ class TraceParams(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("ray_count", C.c_int64), ("ray_begin", C.c_int64), ("cutoff_length_m", C.c_double),
                 ("oct_lo", C.c_int32), ("oct_hi", C.c_int32), ("is_order", C.c_int32), ("sample_rate", C.c_int32),
                 ("hist_cotime_ms", C.c_double), ("pure_specular", C.c_int32), ("max_broadband_bounces", C.c_int32),
-                ("max_segments_per_ray", C.c_int64), ("queue_budget_items", C.c_int64),
+                ("max_segments_per_ray", C.c_int64), ("feed_batch", C.c_int64),
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("wave_kilo_items", C.c_int32), ("ring_log2", C.c_int32),
+                ("kernel_timing", C.c_int32), ("reserved", C.c_int32),
                 ("prim_dirs", _dp), ("prim_weights", _dp)]
 
 
@@ -62,9 +64,10 @@ class Stats(C.Structure):
                 ("lost_energy", C.c_double), ("initial_energy", C.c_double), ("percent_lost", C.c_double),
                 ("h_oct", C.c_int32), ("bins", C.c_int32), ("cotime_s", C.c_double), ("sound_speed", C.c_double),
                 ("rho_c", C.c_double), ("air_atten_db_per_m", C.c_double * 8), ("device_ms", C.c_double),
-                ("octave_kernel_ms", C.c_double), ("octave_kernel_launches", C.c_int64),
-                ("kernel_launches", C.c_int64), ("wall_ms", C.c_double), ("grid_dims", C.c_int32 * 3),
-                ("chunks", C.c_int32)]
+                ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("broadband_ms", C.c_double),
+                ("waves", C.c_int64), ("kernel_launches", C.c_int64), ("peak_live_rays", C.c_int64),
+                ("bvh_nodes_visited", C.c_int64), ("tri_tests", C.c_int64),
+                ("wall_ms", C.c_double), ("accel", C.c_int32 * 3), ("reserved", C.c_int32)]
 
     def to_dict(self):
         out = {}
@@ -78,7 +81,7 @@ class Stats(C.Structure):
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
            "pach_scene_info", "pach_trace_begin", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
-           "pach_trace_specular_paths", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
+           "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
            "pach_math_strength", "pach_math_sound_speed"]
 
@@ -110,6 +113,7 @@ def _declare(L):
                                      C.POINTER(TraceParams), C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_size_t,
                                      C.POINTER(Stats)]),
         "pach_trace_specular_paths": (C.c_int, [vp, C.c_int32, _dp, _dp, C.c_int32, _ip, _dp, _dp]),
+        "pach_scene_shoot_host": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, _dp, _dp, _ip, _dp]),
         "pach_emit_directions": (C.c_int, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _dp]),
         "pach_medium_properties": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _dp, _dp, _dp]),
         "pach_math_schroeder": (C.c_int, [_dp, C.c_int32, _dp]),

@@ -55,11 +55,11 @@ struct pach_scene {
     int device = 0;
     HostScene hs;
     DevScene dev{};
-    DevMem tri, tri64, norm, mat, trans, cs, ct;
+    DevMem tri, tri64, norm, mat, trans, bvh;
     std::mutex mu;
     ~pach_scene() {
         cudaSetDevice(device);
-        for (DevMem *m : {&tri, &tri64, &norm, &mat, &trans, &cs, &ct}) m->release();
+        for (DevMem *m : {&tri, &tri64, &norm, &mat, &trans, &bvh}) m->release();
     }
 };
 
@@ -104,7 +104,9 @@ cudaError_t upload(DevMem &m, const void *src, size_t bytes) {
     return bytes ? cudaMemcpy(m.p, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
 }
 
-// The run worker: chunks of primaries -> k_broadband -> k_octave (+ spill drains).
+// The run worker: uploads the run's inputs, then drives the wavefront loop on one stream --
+// iterations of feed -> broadband -> wave -> trace -> shade, launched in batches between which the
+// host reads the device schedule (done flag, progress) once.
 void run_worker(pach_run *run) {
     auto finish = [&](pach_status s, const std::string &msg, int st) {
         std::lock_guard<std::mutex> lk(run->mu);
@@ -119,49 +121,44 @@ void run_worker(pach_run *run) {
     cudaError_t e = cudaSetDevice(sc->device);
     if (e != cudaSuccess) return finish(PACH_ERR_CUDA, cuda_msg(e, "cudaSetDevice"), PACH_RUN_FAILED);
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, eo0 = nullptr, eo1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> kev;  // per-kernel timing events (kernel_timing = 1)
     std::string where;
     pach_status status = PACH_OK;
     std::string msg;
     int final_state = PACH_RUN_STOPPED;
+    WaveCtl *h_ctl = nullptr;
+    DevCounters *h_cnt = nullptr;
     do {
-#define TRY(x)                                      \
-    do {                                            \
-        e = (x);                                    \
-        if (e != cudaSuccess) { where = #x; break; } \
-    } while (0)
+#define TRY(x)                                        \
+    {                                                 \
+        e = (x);                                      \
+        if (e != cudaSuccess) { where = #x; break; }  \
+    }
         TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        if (e) break;
         TRY(cudaEventCreate(&ev0));
-        if (e) break;
         TRY(cudaEventCreate(&ev1));
-        if (e) break;
-        TRY(cudaEventCreate(&eo0));
-        if (e) break;
-        TRY(cudaEventCreate(&eo1));
-        if (e) break;
+        TRY(cudaMallocHost(&h_ctl, sizeof(WaveCtl)));
+        TRY(cudaMallocHost(&h_cnt, sizeof(DevCounters)));
         const HostScene &hs = sc->hs;
         const int R = run->R, T = run->T;
         const size_t nE = (size_t)R * kBands * T, nD = (size_t)R * 3 * kBands * T;
-        TRY(run->hE.alloc(std::max<size_t>(nE, 1) * 8)); if (e) break;
-        TRY(run->hP.alloc(std::max<size_t>(nE, 1) * 8)); if (e) break;
-        TRY(run->hDp.alloc(std::max<size_t>(nD, 1) * 8)); if (e) break;
-        TRY(run->hDn.alloc(std::max<size_t>(nD, 1) * 8)); if (e) break;
-        TRY(run->hAn.alloc(std::max<size_t>(nD, 1) * 8)); if (e) break;
-        TRY(run->cnt.alloc(sizeof(DevCounters))); if (e) break;
-        TRY(run->qctl.alloc(8 * sizeof(unsigned long long))); if (e) break;
-        TRY(cudaMemsetAsync(run->hE.p, 0, run->hE.bytes, stream)); if (e) break;
-        TRY(cudaMemsetAsync(run->hP.p, 0, run->hP.bytes, stream)); if (e) break;
-        TRY(cudaMemsetAsync(run->hDp.p, 0, run->hDp.bytes, stream)); if (e) break;
-        TRY(cudaMemsetAsync(run->hDn.p, 0, run->hDn.bytes, stream)); if (e) break;
-        TRY(cudaMemsetAsync(run->hAn.p, 0, run->hAn.bytes, stream)); if (e) break;
-        TRY(cudaMemsetAsync(run->cnt.p, 0, sizeof(DevCounters), stream)); if (e) break;
+        TRY(run->hE.alloc(std::max<size_t>(nE, 1) * 8));
+        TRY(run->hP.alloc(std::max<size_t>(nE, 1) * 8));
+        TRY(run->hDp.alloc(std::max<size_t>(nD, 1) * 8));
+        TRY(run->hDn.alloc(std::max<size_t>(nD, 1) * 8));
+        TRY(run->hAn.alloc(std::max<size_t>(nD, 1) * 8));
+        TRY(run->cnt.alloc(sizeof(DevCounters)));
+        TRY(run->qctl.alloc(sizeof(WaveCtl)));
+        for (DevMem *m : {&run->hE, &run->hP, &run->hDp, &run->hDn, &run->hAn, &run->cnt, &run->qctl})
+            TRY(cudaMemsetAsync(m->p, 0, m->bytes, stream));
+        if (e) break;
         // receivers, sources, powers, geodesic faces
         std::vector<float4> rec(std::max(R, 1));
         for (int i = 0; i < R; ++i)
             rec[i] = make_float4((float)run->rec[i].origin[0], (float)run->rec[i].origin[1], (float)run->rec[i].origin[2],
                                  (float)(run->rec[i].radius * run->rec[i].radius));
-        TRY(upload(run->drec, rec.data(), rec.size() * sizeof(float4))); if (e) break;
+        TRY(upload(run->drec, rec.data(), rec.size() * sizeof(float4)));
         std::vector<float4> src(run->nsrc);
         std::vector<float> e0((size_t)run->nsrc * kBands);
         for (int s = 0; s < run->nsrc; ++s) {
@@ -169,40 +166,42 @@ void run_worker(pach_run *run) {
                                  (float)run->src[s].kind);
             for (int o = 0; o < kBands; ++o) e0[s * kBands + o] = (float)(1e-12 * std::pow(10.0, .1 * run->src[s].power_db[o]));
         }
-        TRY(upload(run->dsrc, src.data(), src.size() * sizeof(float4))); if (e) break;
-        TRY(upload(run->de0, e0.data(), e0.size() * sizeof(float))); if (e) break;
+        TRY(upload(run->dsrc, src.data(), src.size() * sizeof(float4)));
+        TRY(upload(run->de0, e0.data(), e0.size() * sizeof(float)));
         std::vector<double> gf;
         geodesic_faces(gf);
         std::vector<float4> geo(kGeoFaces * 3);
         for (int i = 0; i < kGeoFaces * 3; ++i) geo[i] = make_float4((float)gf[3 * i], (float)gf[3 * i + 1], (float)gf[3 * i + 2], 0.f);
-        TRY(upload(run->dgeo, geo.data(), geo.size() * sizeof(float4))); if (e) break;
+        TRY(upload(run->dgeo, geo.data(), geo.size() * sizeof(float4)));
+        if (!run->prim_dirs.empty()) TRY(upload(run->ddirs, run->prim_dirs.data(), run->prim_dirs.size() * sizeof(double)));
+        if (!run->prim_weights.empty()) TRY(upload(run->dw, run->prim_weights.data(), run->prim_weights.size() * sizeof(double)));
 
+        // launch shapes: one resident wave of blocks for the trace and shade kernels
         int dev_sms = 0;
-        TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, sc->device)); if (e) break;
-        const int oct_threads = run->p.block_threads > 0 ? run->p.block_threads : 256;
-        int bps = run->p.blocks_per_sm;
-        if (bps <= 0) {
-            TRY(octave_kernel_occupancy(oct_threads, &bps)); if (e) break;
-            bps = std::max(bps, 1);
-        }
-        const int oct_blocks = dev_sms * bps;
+        TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, sc->device));
+        const int threads = run->p.block_threads > 0 ? std::max(32, std::min(256, run->p.block_threads / 32 * 32)) : 256;
+        int bps_tr = 0, bps_sh = 0;
+        // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
+        const int tr_variant = run->p.blocks_per_sm > 0 ? run->p.blocks_per_sm : 4;
+        TRY(wave_kernel_occupancy(tr_variant, threads, (int)sizeof(float4) * std::max(R, 1), &bps_tr, &bps_sh));
+        const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
-        // Queue sizing: every primary emits at most bound items in phase A.
+        // ring and wave sizing
         const bool pure = run->p.pure_specular != 0;
         const unsigned long long per_bounce = (unsigned long long)kBands * ((hs.has_trans && !pure) ? 3 : 1);
         const unsigned long long bound = per_bounce * run->max_broad + kBands;
-        const unsigned long long budget = run->p.queue_budget_items > 0 ? (unsigned long long)run->p.queue_budget_items
-                                                                        : (1ull << 25);
-        const long long N = run->p.ray_count;
-        long long chunk = (long long)std::max<unsigned long long>(1, budget / bound);
-        chunk = std::min(chunk, N);
-        const unsigned long long qa_cap = (unsigned long long)chunk * bound;
-        const unsigned long long spill_cap = std::max<unsigned long long>(1ull << 20, qa_cap / 16);
-        TRY(run->qa.alloc(qa_cap * sizeof(ORayItem))); if (e) break;
-        TRY(run->qs0.alloc(spill_cap * sizeof(ORayItem))); if (e) break;
-        TRY(run->qs1.alloc(spill_cap * sizeof(ORayItem))); if (e) break;
-        if (!run->prim_dirs.empty()) { TRY(run->ddirs.alloc(sizeof(double) * 3 * chunk)); if (e) break; }
-        if (!run->prim_weights.empty()) { TRY(run->dw.alloc(sizeof(double) * chunk)); if (e) break; }
+        const int ring_log2 = run->p.ring_log2 > 0 ? std::min(32, std::max(16, run->p.ring_log2)) : 27;
+        const unsigned long long ring_cap = 1ull << ring_log2;
+        const unsigned long long max_wave = run->p.wave_kilo_items > 0 ? 1024ull * run->p.wave_kilo_items : (1ull << 21);
+        if (bound * 4 > ring_cap) {
+            status = PACH_ERR_BOUNDS;
+            msg = "the ring queue (2^" + std::to_string(ring_log2) + " rays) cannot hold the phase-A output of one "
+                  "primary (" + std::to_string(bound) + " rays); raise ring_log2 or set max_broadband_bounces";
+            final_state = PACH_RUN_FAILED;
+            break;
+        }
+        TRY(run->qa.alloc(ring_cap * sizeof(ORayItem)));
+        TRY(run->qs0.alloc(std::min(max_wave, ring_cap) * sizeof(int2)));
 
         DevRun r{};
         r.S = sc->dev;
@@ -219,6 +218,9 @@ void run_worker(pach_run *run) {
         r.src = run->dsrc.as<float4>();
         r.e0 = run->de0.as<float>();
         r.geo = run->dgeo.as<float4>();
+        r.prim_dirs = run->prim_dirs.empty() ? nullptr : run->ddirs.as<double>();
+        r.prim_weights = run->prim_weights.empty() ? nullptr : run->dw.as<double>();
+        r.prim_base = run->p.ray_begin;
         r.h_oct = run->h_oct;
         r.oct_lo = run->p.oct_lo;
         r.oct_hi = run->p.oct_hi;
@@ -230,147 +232,156 @@ void run_worker(pach_run *run) {
         r.hE = run->hE.as<double>(); r.hP = run->hP.as<double>(); r.hDp = run->hDp.as<double>();
         r.hDn = run->hDn.as<double>(); r.hAn = run->hAn.as<double>();
         r.cnt = run->cnt.as<DevCounters>();
-        unsigned long long *ctl = run->qctl.as<unsigned long long>();  // [qa_count, qa_head, s0_count, s0_head, s1_count, s1_head]
-
-        float oct_ms = 0.f;
-        long long oct_launches = 0, launches = 0;
-        int chunks = 0;
-        unsigned long long *h_ctl = nullptr;
-        TRY(cudaMallocHost(&h_ctl, 8 * sizeof(unsigned long long))); if (e) break;
-        DevCounters *h_cnt = nullptr;
-        TRY(cudaMallocHost(&h_cnt, sizeof(DevCounters))); if (e) { cudaFreeHost(h_ctl); break; }
+        r.ring = run->qa.as<ORayItem>();
+        r.ring_cap = ring_cap;
+        r.ctl = run->qctl.as<WaveCtl>();
+        r.hits = run->qs0.as<int2>();
+        r.max_wave = std::min(max_wave, ring_cap);
+        r.feed_bound = bound;
+        r.low_water = std::min(ring_cap / 4, 2 * r.max_wave);
+        const long long N = run->p.ray_count;
+        const long long fb_default = std::max<long long>(4096, (long long)(r.max_wave / 32));
+        r.feed_batch = run->p.feed_batch > 0 ? run->p.feed_batch : fb_default;
+        const int bb_threads = 128;
+        const int bb_blocks = (int)std::max<long long>(1, std::min<long long>((r.feed_batch + bb_threads - 1) / bb_threads,
+                                                                              (long long)dev_sms * 16));
+        // initial schedule
+        std::memset(h_ctl, 0, sizeof(WaveCtl));
+        h_ctl->next_prim = run->p.ray_begin;
+        h_ctl->prim_end = run->p.ray_begin + N;
+        h_ctl->prim_first = run->p.ray_begin;
+        TRY(cudaMemcpyAsync(run->qctl.p, h_ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
+        const bool timing = run->p.kernel_timing != 0;
+        double t_trace = 0, t_shade = 0, t_bb = 0;
+        long long launches = 0;
+        int batch = 8;
+        bool cancelled = false;
         TRY(cudaEventRecord(ev0, stream));
-        const long long first = run->p.ray_begin;
-        for (long long q0 = 0; q0 < N && !e; q0 += chunk) {
-            const long long q1 = std::min(N, q0 + chunk);
-            const long long p0 = first + q0, p1 = first + q1;  // global primary indices (RNG keys)
-            TRY(cudaMemsetAsync(ctl, 0, 8 * sizeof(unsigned long long), stream)); if (e) break;
-            r.prim_base = p0;
-            r.prim_dirs = nullptr;
-            r.prim_weights = nullptr;
-            if (!run->prim_dirs.empty()) {
-                TRY(cudaMemcpyAsync(run->ddirs.p, run->prim_dirs.data() + 3 * q0, sizeof(double) * 3 * (q1 - q0),
-                                    cudaMemcpyHostToDevice, stream)); if (e) break;
-                r.prim_dirs = run->ddirs.as<double>();
+        for (long long it = 0; !e; ) {
+            // one batch of iterations, no host synchronisation inside
+            if (timing && kev.size() < (size_t)batch * 6) {
+                while (kev.size() < (size_t)batch * 6) {
+                    cudaEvent_t x;
+                    TRY(cudaEventCreate(&x));
+                    kev.push_back(x);
+                }
+                if (e) break;
             }
-            if (!run->prim_weights.empty()) {
-                TRY(cudaMemcpyAsync(run->dw.p, run->prim_weights.data() + q0, sizeof(double) * (q1 - q0),
-                                    cudaMemcpyHostToDevice, stream)); if (e) break;
-                r.prim_weights = run->dw.as<double>();
-            }
-            // phase A
-            r.q_out = run->qa.as<ORayItem>();
-            r.q_out_count = ctl + 0;
-            r.q_out_cap = qa_cap;
-            const int bb_threads = 128;
-            const long long need_blocks = (p1 - p0 + bb_threads - 1) / bb_threads;
-            const int bb_blocks = (int)std::max<long long>(1, std::min<long long>(need_blocks, (long long)dev_sms * 16));
-            TRY(launch_broadband(r, p0, p1, bb_blocks, bb_threads, stream)); if (e) break;
-            ++launches;
-            // phases B and C
-            // Input: the phase-A queue; output: spill queue 0.  While a launch spilled, the spill
-            // queue it filled becomes the next input and the other spill queue the next output.
-            ORayItem *spq[2] = {run->qs0.as<ORayItem>(), run->qs1.as<ORayItem>()};
-            unsigned long long *spc[2] = {ctl + 2, ctl + 4};
-            r.q_in = run->qa.as<ORayItem>();
-            r.q_in_count = ctl + 0;
-            r.q_in_head = ctl + 1;
-            r.q_in_cap = qa_cap;
-            int out_idx = 0, pass = 0;
-            for (; pass < 1000; ++pass) {
-                r.q_out = spq[out_idx];
-                r.q_out_count = spc[out_idx];
-                r.q_out_cap = spill_cap;
-                TRY(cudaMemsetAsync(spc[out_idx], 0, 2 * sizeof(unsigned long long), stream)); if (e) break;
-                TRY(cudaEventRecord(eo0, stream)); if (e) break;
-                TRY(launch_octave(r, oct_blocks, oct_threads, stream)); if (e) break;
-                TRY(cudaEventRecord(eo1, stream)); if (e) break;
-                ++launches;
-                ++oct_launches;
-                TRY(cudaMemcpyAsync(h_ctl, ctl, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)); if (e) break;
-                TRY(cudaStreamSynchronize(stream)); if (e) break;
-                float ms = 0.f;
-                TRY(cudaEventElapsedTime(&ms, eo0, eo1)); if (e) break;
-                oct_ms += ms;
-                if (h_ctl[2 + 2 * out_idx] == 0) break;
-                r.q_in = spq[out_idx];
-                r.q_in_count = spc[out_idx];
-                r.q_in_head = spc[out_idx] + 1;
-                r.q_in_cap = spill_cap;
-                out_idx ^= 1;
+            for (int k = 0; k < batch && !e; ++k, ++it) {
+                TRY(launch_feed(r, stream));
+                if (timing) TRY(cudaEventRecord(kev[6 * k], stream));
+                TRY(launch_broadband(r, bb_blocks, bb_threads, stream));
+                if (timing) TRY(cudaEventRecord(kev[6 * k + 1], stream));
+                TRY(launch_wave(r, stream));
+                if (timing) TRY(cudaEventRecord(kev[6 * k + 2], stream));
+                TRY(launch_trace(r, tr_variant, tr_blocks, threads, stream));
+                if (timing) TRY(cudaEventRecord(kev[6 * k + 3], stream));
+                if (timing) TRY(cudaEventRecord(kev[6 * k + 4], stream));
+                TRY(launch_shade(r, sh_blocks, threads, stream));
+                if (timing) TRY(cudaEventRecord(kev[6 * k + 5], stream));
+                launches += 5;
             }
             if (e) break;
-            if (pass >= 1000) {
-                status = PACH_ERR_GAVE_UP;
-                msg = "spill queue still non-empty after 1000 drain launches";
-                final_state = PACH_RUN_FAILED;
-                break;
+            TRY(cudaMemcpyAsync(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
+            TRY(cudaMemcpyAsync(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost, stream));
+            TRY(cudaStreamSynchronize(stream));
+            if (timing) {
+                for (int k = 0; k < batch; ++k) {
+                    float a = 0, b = 0, c = 0;
+                    TRY(cudaEventElapsedTime(&a, kev[6 * k], kev[6 * k + 1]));
+                    TRY(cudaEventElapsedTime(&b, kev[6 * k + 2], kev[6 * k + 3]));
+                    TRY(cudaEventElapsedTime(&c, kev[6 * k + 4], kev[6 * k + 5]));
+                    t_bb += a;
+                    t_trace += b;
+                    t_shade += c;
+                }
+                if (e) break;
             }
-            TRY(cudaMemcpyAsync(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost, stream)); if (e) break;
-            TRY(cudaStreamSynchronize(stream)); if (e) break;
-            run->rays_done = q1;
+            // progress: primaries whose phase A has run
+            run->rays_done = h_ctl->next_prim - run->p.ray_begin;
             run->end_traces = (long long)h_cnt->end_traces;
             run->segments = (long long)(h_cnt->seg_broad + h_cnt->seg_b + h_cnt->seg_c);
-            ++chunks;
-            if (h_cnt->queue_overflow) {
-                status = PACH_ERR_BOUNDS;
-                msg = "device queue capacity exceeded (" + std::to_string(h_cnt->queue_overflow) + " pushes dropped)";
+            if (h_ctl->done) break;
+            if (run->cancel && !cancelled) {
+                // stop feeding; the primaries already fed run to completion, so the histograms stay a
+                // consistent estimate over rays_done primaries
+                cancelled = true;
+                const long long stop = h_ctl->next_prim;
+                TRY(cudaMemcpyAsync(&run->qctl.as<WaveCtl>()->prim_end, &stop, sizeof(long long),
+                                    cudaMemcpyHostToDevice, stream));
+                TRY(cudaStreamSynchronize(stream));
+            }
+            if (batch < 64) batch *= 2;
+            if (it > (1ll << 26)) {
+                status = PACH_ERR_GAVE_UP;
+                msg = "wavefront loop did not finish";
                 final_state = PACH_RUN_FAILED;
                 break;
             }
-            if (run->cancel) {
-                status = PACH_ERR_CANCELLED;
-                msg = "run cancelled";
-                final_state = PACH_RUN_CANCELLED;
-                break;
-            }
         }
-        if (!e) { TRY(cudaEventRecord(ev1, stream)); }
-        if (!e) { TRY(cudaStreamSynchronize(stream)); }
+        if (e || status) break;
+        TRY(cudaEventRecord(ev1, stream));
+        TRY(cudaStreamSynchronize(stream));
         float dev_ms = 0.f;
-        if (!e) { TRY(cudaEventElapsedTime(&dev_ms, ev0, ev1)); }
-        if (!e) { TRY(cudaMemcpy(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost)); }
-        if (!e) {
-            pach_stats &s = run->stats;
-            s.primaries = (int64_t)h_cnt->primaries;
-            s.segments_broadband = (int64_t)h_cnt->seg_broad;
-            s.segments_phase_b = (int64_t)h_cnt->seg_b;
-            s.segments_phase_c = (int64_t)h_cnt->seg_c;
-            s.segments = s.segments_broadband + s.segments_phase_b + s.segments_phase_c;
-            s.octave_rays = (int64_t)h_cnt->octave_rays;
-            s.end_traces = (int64_t)h_cnt->end_traces;
-            s.detections = (int64_t)h_cnt->detections;
-            s.capped = (int64_t)h_cnt->capped;
-            s.fp64_retests = (int64_t)h_cnt->retests;
-            s.queue_overflows = (int64_t)h_cnt->queue_overflow;
-            s.stack_spills = (int64_t)h_cnt->stack_spills;
-            s.lost_energy = h_cnt->lost_energy;
-            s.initial_energy = h_cnt->initial_energy;
-            s.percent_lost = s.initial_energy > 0 ? 100.0 * s.lost_energy / s.initial_energy : 0.0;
-            s.h_oct = run->h_oct;
-            s.bins = T;
-            s.cotime_s = run->cotime;
-            s.sound_speed = hs.c;
-            s.rho_c = hs.rho_c;
-            for (int o = 0; o < kBands; ++o) s.air_atten_db_per_m[o] = hs.atten[o];
-            s.device_ms = dev_ms;
-            s.octave_kernel_ms = oct_ms;
-            s.octave_kernel_launches = oct_launches;
-            s.kernel_launches = launches;
-            for (int k = 0; k < 3; ++k) s.grid_dims[k] = hs.dims[k];
-            s.chunks = chunks;
-            run->segments = s.segments;
-            run->end_traces = s.end_traces;
+        TRY(cudaEventElapsedTime(&dev_ms, ev0, ev1));
+        TRY(cudaMemcpy(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost));
+        TRY(cudaMemcpy(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost));
+        pach_stats &s = run->stats;
+        s.primaries = (int64_t)h_cnt->primaries;
+        s.segments_broadband = (int64_t)h_cnt->seg_broad;
+        s.segments_phase_b = (int64_t)h_cnt->seg_b;
+        s.segments_phase_c = (int64_t)h_cnt->seg_c;
+        s.segments = s.segments_broadband + s.segments_phase_b + s.segments_phase_c;
+        s.octave_rays = (int64_t)h_cnt->octave_rays;
+        s.end_traces = (int64_t)h_cnt->end_traces;
+        s.detections = (int64_t)h_cnt->detections;
+        s.capped = (int64_t)h_cnt->capped;
+        s.fp64_retests = (int64_t)h_cnt->retests;
+        s.queue_overflows = (int64_t)h_ctl->overflow;
+        s.stack_spills = 0;
+        s.lost_energy = h_cnt->lost_energy;
+        s.initial_energy = h_cnt->initial_energy;
+        s.percent_lost = s.initial_energy > 0 ? 100.0 * s.lost_energy / s.initial_energy : 0.0;
+        s.h_oct = run->h_oct;
+        s.bins = T;
+        s.cotime_s = run->cotime;
+        s.sound_speed = hs.c;
+        s.rho_c = hs.rho_c;
+        for (int o = 0; o < kBands; ++o) s.air_atten_db_per_m[o] = hs.atten[o];
+        s.device_ms = dev_ms;
+        s.trace_ms = t_trace;
+        s.shade_ms = t_shade;
+        s.broadband_ms = t_bb;
+        s.waves = (int64_t)h_ctl->waves;
+        s.kernel_launches = launches;
+        s.peak_live_rays = (int64_t)h_ctl->peak_live;
+        s.bvh_nodes_visited = (int64_t)h_cnt->bvh_nodes;
+        s.tri_tests = (int64_t)h_cnt->tri_tests;
+        s.accel[0] = hs.bvh_nodes;
+        s.accel[1] = hs.bvh_leaves;
+        s.accel[2] = hs.bvh_depth;
+        run->rays_done = (long long)h_cnt->primaries;
+        run->segments = s.segments;
+        run->end_traces = s.end_traces;
+        if (h_ctl->overflow) {
+            status = PACH_ERR_BOUNDS;
+            msg = "ring queue full: raise ring_log2";
+            final_state = PACH_RUN_FAILED;
+        } else if (cancelled) {
+            status = PACH_ERR_CANCELLED;
+            msg = "run cancelled after " + std::to_string(s.primaries) + " primaries";
+            final_state = PACH_RUN_CANCELLED;
         }
-        cudaFreeHost(h_ctl);
-        cudaFreeHost(h_cnt);
 #undef TRY
     } while (0);
     run->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
-    for (cudaEvent_t ev : {ev0, ev1, eo0, eo1})
+    for (cudaEvent_t ev : kev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : {ev0, ev1})
         if (ev) cudaEventDestroy(ev);
+    if (h_ctl) cudaFreeHost(h_ctl);
+    if (h_cnt) cudaFreeHost(h_cnt);
     if (stream) cudaStreamDestroy(stream);
-    // release the queues; histograms and counters stay until the run is destroyed
+    // release the ring; histograms and counters stay until the run is destroyed
     for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw}) m->release();
     if (e != cudaSuccess) return finish(PACH_ERR_CUDA, cuda_msg(e, where.c_str()), PACH_RUN_FAILED);
     finish(status, msg, final_state);
@@ -465,8 +476,7 @@ pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
         (e = upload(sc->norm, norm.data(), norm.size() * sizeof(float4))) ||
         (e = upload(sc->mat, mat.data(), mat.size() * sizeof(float4))) ||
         (e = upload(sc->trans, trans.data(), trans.size() * sizeof(float))) ||
-        (e = upload(sc->cs, hs.cell_start.data(), hs.cell_start.size() * sizeof(uint32_t))) ||
-        (e = upload(sc->ct, hs.cell_tris.data(), std::max<size_t>(hs.cell_tris.size(), 1) * sizeof(uint32_t)))) {
+        (e = upload(sc->bvh, hs.bvh.data(), hs.bvh.size() * sizeof(float)))) {
         delete sc;
         return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
     }
@@ -476,18 +486,8 @@ pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
     d.pnormal = sc->norm.as<float4>();
     d.mat = sc->mat.as<float4>();
     d.trans = sc->trans.as<float>();
-    d.cell_start = sc->cs.as<uint32_t>();
-    d.cell_tris = sc->ct.as<uint32_t>();
-    d.nx = hs.dims[0]; d.ny = hs.dims[1]; d.nz = hs.dims[2];
+    d.bvh = sc->bvh.as<float4>();
     d.ntri = hs.ntri;
-    d.bminx = (float)hs.bmin[0]; d.bminy = (float)hs.bmin[1]; d.bminz = (float)hs.bmin[2];
-    d.bmaxx = (float)hs.bmax[0]; d.bmaxy = (float)hs.bmax[1]; d.bmaxz = (float)hs.bmax[2];
-    d.cellx = (float)((hs.bmax[0] - hs.bmin[0]) / hs.dims[0]);
-    d.celly = (float)((hs.bmax[1] - hs.bmin[1]) / hs.dims[1]);
-    d.cellz = (float)((hs.bmax[2] - hs.bmin[2]) / hs.dims[2]);
-    d.icellx = (float)(hs.dims[0] / (hs.bmax[0] - hs.bmin[0]));
-    d.icelly = (float)(hs.dims[1] / (hs.bmax[1] - hs.bmin[1]));
-    d.icellz = (float)(hs.dims[2] / (hs.bmax[2] - hs.bmin[2]));
     d.t_eps = (float)(2e-7 * hs.scale);
     d.has_trans = hs.has_trans ? 1 : 0;
     *out = sc;
@@ -686,6 +686,30 @@ pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double
         (e = cudaMemcpy(t_out, t.p, sizeof(double) * k, cudaMemcpyDeviceToHost)) ||
         (e = cudaMemcpy(pts_out, pt.p, sizeof(double) * 3 * k, cudaMemcpyDeviceToHost)))
         return fail(PACH_ERR_CUDA, cuda_msg(e, "specular paths"));
+    return PACH_OK;
+}
+
+pach_status pach_scene_shoot_host(const pach_scene_desc *desc, int32_t n, const double *origins, const double *dirs,
+                                  int32_t *poly_out, double *t_out) {
+    if (n < 0 || (n > 0 && (!origins || !dirs || !poly_out || !t_out))) return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+    HostScene hs;
+    std::string err;
+    if (!build_host_scene(desc, hs, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
+    for (int i = 0; i < n; ++i) {
+        const double o[3] = {origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]};
+        double d[3] = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+        const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (double &x : d) x /= l;
+        int tri = -1;
+        double t = 0;
+        if (bvh_shoot_host(hs, o, d, 1e-10, tri, t)) {
+            poly_out[i] = hs.tri_poly[tri];
+            t_out[i] = t;
+        } else {
+            poly_out[i] = -1;
+            t_out[i] = 0;
+        }
+    }
     return PACH_OK;
 }
 

@@ -1,0 +1,440 @@
+// device_common.cuh -- device helpers shared by the tracer kernels: Philox streams, vector math,
+// the Lambert direction, the FP32/FP64 triangle test, the BVH walk, receiver detection with FP64
+// histogram accumulation, emission directions and the octave-ray queue item.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "engine.h"
+
+namespace pach {
+namespace {
+
+constexpr float kInvPi = 0.318309886183790671538f;
+constexpr float kBaryEps = 2e-5f;
+constexpr float kTP1 = 1e-2f;                  // TaskAll:351
+constexpr float kTP2 = 3.16227766016837933e-5f;  // 10^-4.5, TaskAll:331, 355
+constexpr float kTP3 = 1e-9f;                  // TaskAll:356
+
+// ------------------------------------------------------------------------------------------
+// RNG (Philox4x32-10, Salmon et al. SC'11) and stream identities
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += W0; k1 += W1; }
+        const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ float u24(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+__device__ __forceinline__ float4 draw(unsigned long long seed, uint32_t prim, unsigned long long sid, uint32_t b) {
+    const uint4 c = philox(make_uint4(b, prim, (uint32_t)sid, (uint32_t)(sid >> 32)), (uint32_t)seed,
+                           (uint32_t)(seed >> 32));
+    return make_float4(u24(c.x), u24(c.y), u24(c.z), u24(c.w));
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ unsigned long long sid_early(int k, int o, int q) {
+    return (1ull << 62) | ((unsigned long long)k << 5) | ((unsigned long long)o << 2) | (unsigned long long)q;
+}
+__device__ __forceinline__ unsigned long long sid_final(int o) { return (2ull << 62) | (unsigned long long)o; }
+__device__ __forceinline__ unsigned long long sid_late(unsigned long long parent, uint32_t nb) {
+    return (3ull << 62) |
+           (mix64(parent + 0x9E3779B97F4A7C15ull * (unsigned long long)(nb + 1)) & ((1ull << 62) - 1));
+}
+
+// ------------------------------------------------------------------------------------------
+// small vector helpers
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 unit3(float3 a) { return a * rsqrtf(dot3(a, a)); }
+
+// Uniform-hemisphere direction about n (Lambert_Scattering, Classes_Materials.cs:4521-4552): frame
+// z = n, x from (0,0,1) unless |n.z| in (0.99, 1.01) then (1,0,0); azimuth 2 pi U1; cos(zenith) = U2.
+__device__ __forceinline__ float3 lambert(float3 n, float U1, float U2) {
+    float3 dx = make_float3(0.f, 0.f, 1.f);
+    const float proj = fabsf(n.z);
+    if (0.99f < proj && proj < 1.01f) dx = make_float3(1.f, 0.f, 0.f);
+    float3 dy = cross3(n, dx);
+    dx = cross3(dy, n);
+    dx = unit3(dx);
+    dy = unit3(dy);
+    float s, c;
+    sincospif(2.0f * U1, &s, &c);
+    const float sz = sqrtf(fmaxf(0.f, 1.f - U2 * U2));
+    return unit3(dx * (c * sz) + dy * (s * sz) + n * U2);
+}
+
+// ------------------------------------------------------------------------------------------
+// geometry
+// ------------------------------------------------------------------------------------------
+// FP64 re-test of triangle i (the FP32 ray converted exactly).
+__device__ __noinline__ bool retest64(const DevScene &S, int i, float3 of, float3 df, double &t) {
+    const double *T = S.tri64 + 9 * (size_t)i;
+    const double ox = of.x, oy = of.y, oz = of.z, dx = df.x, dy = df.y, dz = df.z;
+    const double e1x = T[3], e1y = T[4], e1z = T[5], e2x = T[6], e2y = T[7], e2z = T[8];
+    const double px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+    const double det = e1x * px + e1y * py + e1z * pz;
+    if (det == 0.0) return false;
+    const double inv = 1.0 / det;
+    const double sx = ox - T[0], sy = oy - T[1], sz = oz - T[2];
+    const double u = (sx * px + sy * py + sz * pz) * inv;
+    if (u < 0.0 || u > 1.0) return false;
+    const double qx = sy * e1z - sz * e1y, qy = sz * e1x - sx * e1z, qz = sx * e1y - sy * e1x;
+    const double v = (dx * qx + dy * qy + dz * qz) * inv;
+    if (v < 0.0 || u + v > 1.0) return false;
+    t = (e2x * qx + e2y * qy + e2z * qz) * inv;
+    return true;
+}
+
+// Traversal work of one thread: FP64 re-tests, inner BVH nodes visited, triangles tested.
+struct TraceWork {
+    unsigned long long retests = 0;
+    unsigned long long nodes = 0, tris = 0;
+};
+
+// One candidate triangle: FP32 Moller-Trumbore, FP64 re-test inside the epsilon band.
+__device__ __forceinline__ void test_tri(const DevScene &S, int i, float3 o, float3 d, int skip, float &best, int &bi,
+                                         TraceWork &w) {
+    const float4 A = __ldg(S.tri + 3 * i);
+    if (__float_as_int(A.w) == skip) return;
+    const float4 B = __ldg(S.tri + 3 * i + 1);
+    const float4 C = __ldg(S.tri + 3 * i + 2);
+    const float3 e1 = f3(B), e2 = f3(C);
+    const float3 p = cross3(d, e2);
+    const float det = dot3(e1, p);
+    const float3 s = o - f3(A);
+    const float inv = 1.0f / det;
+    const float u = dot3(s, p) * inv;
+    const float3 q = cross3(s, e1);
+    const float v = dot3(d, q) * inv;
+    const float t = dot3(e2, q) * inv;
+    const float margin = fminf(fminf(u, v), 1.0f - u - v);
+    const bool grazing = fabsf(det) < C.w;
+    if (grazing || !(fabsf(margin) > kBaryEps)) {
+        // near grazing, near an edge, or not finite: decide in FP64.  Away from grazing the FP32
+        // distance is accurate, so a candidate well outside (t_eps, best) needs no re-test.
+        if (!grazing && isfinite(t) && (t < 0.5f * S.t_eps || t > 1.0001f * best)) return;
+        double td;
+        ++w.retests;
+        if (retest64(S, i, o, d, td)) {
+            const float tf = (float)td;
+            if (tf > S.t_eps && tf < best) { best = tf; bi = i; }
+        }
+    } else if (margin > 0.f && t > S.t_eps && t < best) {
+        best = t;
+        bi = i;
+    }
+}
+
+// Empty child slot of a 4-wide node (no leaf can have this code below 2^27 triangles).
+constexpr int kEmptyChild = (int)0x80000000;
+
+__device__ __forceinline__ void cswap(float &ka, int &va, float &kb, int &vb) {
+    if (kb < ka) {
+        const float k = ka; ka = kb; kb = k;
+        const int v = va; va = vb; vb = v;
+    }
+}
+
+// One 4-wide node: slab-test the children against [0, best], order the hit ones by entry distance
+// (5-exchange sorting network), push all but the nearest (farthest first), return the nearest in
+// `next`.  Returns false when no child is hit.
+__device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int node, float ix, float iy, float iz,
+                                          float ox, float oy, float oz, float best, int *stack, int &sp, int &next) {
+    const float4 *N = bvh + (kBvhNodeFloats / 4) * node;
+    const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3);
+    const float4 lz = __ldg(N + 4), hz = __ldg(N + 5);
+    const int4 ch = __ldg(reinterpret_cast<const int4 *>(N + 6));
+    const float alx[4] = {lx.x, lx.y, lx.z, lx.w}, ahx[4] = {hx.x, hx.y, hx.z, hx.w};
+    const float aly[4] = {ly.x, ly.y, ly.z, ly.w}, ahy[4] = {hy.x, hy.y, hy.z, hy.w};
+    const float alz[4] = {lz.x, lz.y, lz.z, lz.w}, ahz[4] = {hz.x, hz.y, hz.z, hz.w};
+    int id[4] = {ch.x, ch.y, ch.z, ch.w};
+    float tk[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float t0x = fmaf(alx[k], ix, -ox), t1x = fmaf(ahx[k], ix, -ox);
+        const float t0y = fmaf(aly[k], iy, -oy), t1y = fmaf(ahy[k], iy, -oy);
+        const float t0z = fmaf(alz[k], iz, -oz), t1z = fmaf(ahz[k], iz, -oz);
+        const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.f));
+        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), best));
+        tk[k] = (tn <= tf && id[k] != kEmptyChild) ? tn : FLT_MAX;
+    }
+    cswap(tk[0], id[0], tk[1], id[1]);
+    cswap(tk[2], id[2], tk[3], id[3]);
+    cswap(tk[0], id[0], tk[2], id[2]);
+    cswap(tk[1], id[1], tk[3], id[3]);
+    cswap(tk[1], id[1], tk[2], id[2]);
+    if (tk[0] == FLT_MAX) return false;
+#pragma unroll
+    for (int k = 3; k >= 1; --k)
+        if (tk[k] != FLT_MAX && sp < kBvhStack) stack[sp++] = id[k];
+    next = id[0];
+    return true;
+}
+
+// Nearest hit along o + t d with t > t_eps, skipping triangles of plane `skip` (the surface the ray
+// leaves).  4-wide BVH, nearest-child-first walk with a per-thread stack of the other hit
+// children; a child box is entered only if the ray meets it before the best hit so far.
+__device__ __forceinline__ bool trace_ray(const DevScene &S, float3 o, float3 d, int skip, float &t_best,
+                                          int &tri_best, TraceWork &w) {
+    const float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
+    const float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
+    const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
+    const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+    const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
+    int stack[kBvhStack];
+    int sp = 0;
+    int node = 0;
+    float best = FLT_MAX;
+    int bi = -1;
+    for (;;) {
+        bool done = false;
+        while (node >= 0) {
+            ++w.nodes;
+            int next;
+            if (!bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) {
+                if (sp == 0) { done = true; break; }
+                node = stack[--sp];
+                continue;
+            }
+            node = next;
+        }
+        if (done) break;
+        // leaf ~(first * 16 + count - 1)
+        const int code = ~node;
+        const int f0 = code >> 4, cnt = (code & 15) + 1;
+        w.tris += (unsigned)cnt;
+        for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    if (bi < 0) return false;
+    t_best = best;
+    tri_best = bi;
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------
+// receivers
+// ------------------------------------------------------------------------------------------
+// Sphere test of segment [o, o + tseg d] (Classes_Receivers.cs:839-849).  The discriminant is
+// formed as r^2 - |m - b d|^2 (equal to b^2 - c for a unit d) to avoid cancellation in FP32.
+__device__ __forceinline__ bool sphere_hit(float4 c, float3 o, float3 d, float tseg, float &t, float &half) {
+    const float3 m = make_float3(o.x - c.x, o.y - c.y, o.z - c.z);
+    const float b = dot3(m, d);
+    const float cc = dot3(m, m) - c.w;
+    if (cc > 0.f && b > 0.f) return false;
+    const float3 perp = m - d * b;
+    const float disc = c.w - dot3(perp, perp);
+    if (disc < 0.f) return false;
+    t = -b;  // chord midpoint (t1 + t2) / 2
+    if (!(t > 0.f && t < tseg)) return false;
+    half = sqrtf(disc);  // (t2 - t1) / 2
+    return true;
+}
+
+// Directional_Histogram.Add (Classes_Receivers.cs:1813-1825) + Reflection_Analysis_Data.
+__device__ __forceinline__ void hist_add(const DevRun &r, int k, int oct, long long bin, float e, float3 d, int kind) {
+    const size_t base = ((size_t)k * kBands + oct) * r.T + bin;
+    atomicAdd(r.hE + base, (double)e);
+    atomicAdd(r.hP + base, (double)sqrtf(e * r.rho_c));
+    const float ca[3] = {-d.x, -d.y, -d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const size_t j = (((size_t)k * 3 + a) * kBands + oct) * r.T + bin;
+        atomicAdd((ca[a] > 0.f ? r.hDp : r.hDn) + j, (double)(ca[a] * e));
+    }
+    atomicAdd(r.hAn + (((size_t)k * 3 + kind) * kBands + oct) * r.T + bin, (double)e);
+}
+
+// Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half.
+__device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
+                                                  double t_sum, float Iabs, int oct, int mask) {
+    uint32_t n = 0;
+    for (int k = 0; k < r.R; ++k) {
+        float t, half;
+        if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
+        ++n;
+        const double time = t_sum + (double)(t * r.inv_c);
+        const long long bin = (long long)(time * r.fs);
+        if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
+        const float e = Iabs * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
+        hist_add(r, k, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
+    }
+    return n;
+}
+
+// Spherical_Receiver.CheckBroadbandRay (Classes_Receivers.cs:803-829): every band of the range,
+// analysis bin 0 (specular).
+__device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
+                                                 double t_sum, const float (&E)[kBands], const float (&sc)[kBands]) {
+    uint32_t n = 0;
+    for (int k = 0; k < r.R; ++k) {
+        float t, half;
+        if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
+        ++n;
+        const double time = t_sum + (double)(t * r.inv_c);
+        const long long bin = (long long)(time * r.fs);
+        if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
+#pragma unroll
+        for (int oct = 0; oct < kBands; ++oct) {
+            if (oct < r.oct_lo || oct > r.oct_hi) continue;
+            const float e = E[oct] * sc[oct] * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
+            hist_add(r, k, oct, bin, e, d, 0);
+        }
+    }
+    return n;
+}
+
+// ------------------------------------------------------------------------------------------
+// emission
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float3 emit_dir(const DevRun &r, long long prim, int kind) {
+    const float4 U = draw(r.seed, (uint32_t)prim, 0ull, 0u);
+    if (kind == PACH_SOURCE_RANDOM) {  // RandomSource (Classes_Sources.cs:256-265)
+        float st, ct, sp, cp;
+        sincospif(2.0f * U.x, &st, &ct);
+        sincospif(2.0f * U.y, &sp, &cp);
+        return make_float3(st * cp, st * sp, ct);
+    }
+    if (kind == PACH_SOURCE_UNIFORM) {
+        const float z = 1.0f - 2.0f * U.x;
+        const float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float sp, cp;
+        sincospif(2.0f * U.y, &sp, &cp);
+        return make_float3(rr * cp, rr * sp, z);
+    }
+    // GeodesicSource (Classes_Sources.cs:390-403): face (per-source ray count) mod 80, point on face
+    const long long j = prim / r.nsrc;
+    const int f = (int)(j % kGeoFaces);
+    float u = U.x, v = U.y;
+    if (u + v > 1.f) { u = 1.f - u; v = 1.f - v; }
+    const float3 a = f3(r.geo[3 * f]), b = f3(r.geo[3 * f + 1]), c = f3(r.geo[3 * f + 2]);
+    return unit3(a + (b - a) * u + (c - a) * v);
+}
+
+// ------------------------------------------------------------------------------------------
+// queue items
+// ------------------------------------------------------------------------------------------
+struct Ray {
+    float3 p, d;
+    float I, scale;
+    double t_sum;
+    uint32_t prim, nb;
+    unsigned long long sid;
+    int oct, mask, phase, plane;
+};
+
+__device__ __forceinline__ ORayItem to_item(const Ray &R) {
+    ORayItem it;
+    it.px = R.p.x; it.py = R.p.y; it.pz = R.p.z; it.I = R.I;
+    it.dx = R.d.x; it.dy = R.d.y; it.dz = R.d.z; it.scale = R.scale;
+    it.t_sum = R.t_sum; it.prim = R.prim; it.nb = R.nb; it.sid = R.sid;
+    it.meta = (uint32_t)R.oct | ((uint32_t)R.mask << 3) | ((uint32_t)R.phase << 5);
+    it.plane = R.plane;
+    return it;
+}
+
+__device__ __forceinline__ Ray to_ray(const ORayItem &it) {
+    Ray R;
+    R.p = make_float3(it.px, it.py, it.pz);
+    R.d = make_float3(it.dx, it.dy, it.dz);
+    R.I = it.I; R.scale = it.scale; R.t_sum = it.t_sum; R.prim = it.prim; R.nb = it.nb; R.sid = it.sid;
+    R.oct = (int)(it.meta & 7u); R.mask = (int)((it.meta >> 3) & 3u); R.phase = (int)((it.meta >> 5) & 1u);
+    R.plane = it.plane;
+    return R;
+}
+
+__device__ __forceinline__ Ray new_ray(float3 p, float3 d, float I, float scale, double t_sum, uint32_t prim,
+                                       unsigned long long sid, int oct, int mask, int plane) {
+    Ray R;
+    R.p = p; R.d = d; R.I = I; R.scale = scale; R.t_sum = t_sum; R.prim = prim; R.nb = 0; R.sid = sid;
+    R.oct = oct; R.mask = mask; R.phase = 0; R.plane = plane;
+    return R;
+}
+
+// Reserves n consecutive queue slots only if they all fit; bounded retries under contention.
+__device__ __forceinline__ bool reserve(unsigned long long *count, unsigned long long n, unsigned long long cap,
+                                        unsigned long long &slot) {
+    unsigned long long old = *reinterpret_cast<volatile unsigned long long *>(count);
+    for (int tries = 0; tries < 64; ++tries) {
+        if (old + n > cap) return false;
+        const unsigned long long prev = atomicCAS(count, old, old + n);
+        if (prev == old) { slot = old; return true; }
+        old = prev;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void store_item(ORayItem *q, unsigned long long slot, const ORayItem &it) {
+    float4 *dst = reinterpret_cast<float4 *>(q + slot);
+    const float4 *src = reinterpret_cast<const float4 *>(&it);
+    dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
+}
+
+__device__ __forceinline__ ORayItem load_item(const ORayItem *q, unsigned long long i) {
+    const float4 *s = reinterpret_cast<const float4 *>(q + i);
+    ORayItem it;
+    float4 *d = reinterpret_cast<float4 *>(&it);
+    d[0] = __ldcs(s); d[1] = __ldcs(s + 1); d[2] = __ldcs(s + 2); d[3] = __ldcs(s + 3);
+    return it;
+}
+
+// ------------------------------------------------------------------------------------------
+// counters
+// ------------------------------------------------------------------------------------------
+struct LocalCounters {
+    unsigned long long v[11] = {0};  // prim, seg_broad, seg_b, seg_c, oct, end_traces, det, capped, retests, overflow, spills
+    double lost = 0, init = 0;
+};
+enum { C_PRIM, C_SEGA, C_SEGB, C_SEGC, C_OCT, C_END, C_DET, C_CAP, C_RET, C_OVF, C_SPILL };
+
+__device__ void flush_counters(const DevRun &r, const LocalCounters &L) {
+    __shared__ unsigned long long s_u[11];
+    __shared__ double s_d[2];
+    if (threadIdx.x < 11) s_u[threadIdx.x] = 0;
+    if (threadIdx.x < 2) s_d[threadIdx.x] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 11; ++i)
+        if (L.v[i]) atomicAdd(&s_u[i], L.v[i]);
+    if (L.lost != 0) atomicAdd(&s_d[0], L.lost);
+    if (L.init != 0) atomicAdd(&s_d[1], L.init);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        DevCounters *c = r.cnt;
+        unsigned long long *dst[11] = {&c->primaries, &c->seg_broad, &c->seg_b, &c->seg_c, &c->octave_rays,
+                                       &c->end_traces, &c->detections, &c->capped, &c->retests, &c->queue_overflow,
+                                       &c->stack_spills};
+        for (int i = 0; i < 11; ++i)
+            if (s_u[i]) atomicAdd(dst[i], s_u[i]);
+        if (s_d[0] != 0) atomicAdd(&c->lost_energy, s_d[0]);
+        if (s_d[1] != 0) atomicAdd(&c->initial_energy, s_d[1]);
+    }
+}
+
+__device__ __forceinline__ void load_receivers(const DevRun &r, float4 *rec) {
+    for (int i = threadIdx.x; i < r.R; i += blockDim.x) rec[i] = r.rec[i];
+    __syncthreads();
+}
+
+}  // namespace
+}  // namespace pach

@@ -25,27 +25,29 @@ struct HostScene {
     std::vector<double> alpha, scat, trans;  // [npoly][8]
     bool has_trans = false;
     double bmin[3], bmax[3];
-    int dims[3];
-    std::vector<uint32_t> cell_start;  // [ncell+1]
-    std::vector<uint32_t> cell_tris;
+    // BVH: 4-wide, collapsed from an SAH binary tree; triangles above are stored in leaf order.
+    // node n = 8 float4 (128 B): lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4], child[4] (int
+    // bits), unused; a child >= 0 is an inner node, < 0 the leaf ~(first * 16 + count - 1); an
+    // empty slot has an inverted box.
+    std::vector<float> bvh;          // [nodes*32]
+    int bvh_nodes = 0, bvh_leaves = 0, bvh_depth = 0;
     double c = 343, rho = 1.2, rho_c = 411.6, atten[kBands] = {0};
     double scale = 1;                // largest box extent
 };
 
+constexpr int kBvhStack = 64;
+constexpr int kBvhNodeFloats = 32;
+constexpr int kLeafMax = 8;
+
 // Device scene view (passed by value to kernels).
 struct DevScene {
-    const float4 *tri;          // [ntri*3]: (v0, plane bits) (e1, poly bits) (e2, 0)
+    const float4 *tri;          // [ntri*3]: (v0, plane bits) (e1, poly bits) (e2, grazing threshold)
     const double *tri64;        // [ntri*9]
     const float4 *pnormal;      // [npoly]
     const float4 *mat;          // [npoly*8]: (1-alpha, s_lo, s_mid, s_hi)
     const float *trans;         // [npoly*8]
-    const uint32_t *cell_start; // [ncell+1]
-    const uint32_t *cell_tris;
-    int nx, ny, nz, ntri;
-    float bminx, bminy, bminz;
-    float cellx, celly, cellz;
-    float icellx, icelly, icellz;
-    float bmaxx, bmaxy, bmaxz;
+    const float4 *bvh;          // [nodes*4]
+    int ntri;
     float t_eps;
     int has_trans;
 };
@@ -65,9 +67,24 @@ struct __align__(16) ORayItem {
 // Counters accumulated by the kernels (one instance in device memory).
 struct DevCounters {
     unsigned long long primaries, seg_broad, seg_b, seg_c, octave_rays, end_traces, detections, capped,
-        retests, queue_overflow, stack_spills, lost_items;
+        retests, queue_overflow, stack_spills, lost_items, bvh_nodes, tri_tests;
     double lost_energy, initial_energy;
 };
+
+// Device-side schedule of the wavefront loop (one instance in device memory).
+struct WaveCtl {
+    unsigned long long head, tail;  // ring indices, monotonic
+    unsigned long long m;           // items in the current wave
+    long long next_prim, prim_end;  // primaries still to feed: [next_prim, prim_end)
+    long long pa_begin, pa_count;   // phase-A batch of the current iteration
+    unsigned long long waves, overflow, peak_live;
+    long long prim_first;           // first primary of the run
+    unsigned long long per_prim;    // ring footprint per primary measured by the pilot batch (0 = not yet)
+    unsigned long long trace_next;  // next wave item a trace thread takes (dynamic fetch)
+    int done, pad;
+};
+
+constexpr long long kPilotPrimaries = 256;
 
 // Launch-wide parameters (kernel argument).
 struct DevRun {
@@ -95,23 +112,30 @@ struct DevRun {
     // outputs
     double *hE, *hP, *hDp, *hDn, *hAn;
     DevCounters *cnt;
-    // queues
-    ORayItem *q_in;             // input of the octave kernel
-    const unsigned long long *q_in_count;
-    unsigned long long q_in_cap;
-    unsigned long long *q_in_head;
-    ORayItem *q_out;            // spill / phase-A output
-    unsigned long long *q_out_count;
-    unsigned long long q_out_cap;
+    // wavefront ring of octave rays (live items are [head, tail) modulo ring_cap)
+    ORayItem *ring;
+    unsigned long long ring_cap;   // power of two
+    WaveCtl *ctl;
+    int2 *hits;                    // per wave slot: (triangle, t bits); triangle -1 = miss
+    unsigned long long max_wave;   // items per wave at most
+    long long feed_batch;          // primaries per phase-A launch at most
+    unsigned long long feed_bound; // ring slots one primary can fill in phase A
+    unsigned long long low_water;  // feed new primaries when fewer live items remain
 };
 
-// trace.cu entry points (host wrappers)
-cudaError_t launch_broadband(const DevRun &r, long long p0, long long p1, int blocks, int threads, cudaStream_t s);
-cudaError_t launch_octave(const DevRun &r, int blocks, int threads, cudaStream_t s);
+// trace.cu entry points (host wrappers).  One wavefront iteration:
+//   feed (1 thread) -> broadband (phase A of the fed primaries) -> wave (1 thread: size the wave)
+//   -> trace (BVH walk of every ray of the wave) -> shade (detect, absorb, scatter, append).
+cudaError_t launch_feed(const DevRun &r, cudaStream_t s);
+cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s);
+cudaError_t launch_wave(const DevRun &r, cudaStream_t s);
+// variant: 256-thread blocks per SM the trace kernel is compiled for (3..6; others -> 4)
+cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s);
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s);
+cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
                          double *t, double *pts, cudaStream_t s);
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s);
-cudaError_t octave_kernel_occupancy(int threads, int *blocks_per_sm);
 
 // scene.cpp
 bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err);
@@ -119,5 +143,7 @@ void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, 
                        double *c, double *rho);
 void geodesic_faces(std::vector<double> &faces);  // [80][3][3]
 unsigned long long derived_broadband_bound(const HostScene &hs, int h_oct, bool pure_specular);
+// Host walk of hs.bvh with the device's box test and FP64 triangle tests (t > t_min).
+bool bvh_shoot_host(const HostScene &hs, const double o[3], const double d[3], double t_min, int &tri, double &t);
 
 }  // namespace pach

@@ -3,8 +3,9 @@
 // Restates Polygon_Scene.Construct / partition (Classes_Scenes.cs:447-630, 727-755) for a GPU:
 // polygons are fan-triangulated (polygon id kept per triangle), flat polygon normals and areas are
 // computed in FP64 (Classes_Scenes.cs:864-872, 894-897), coplanar triangles share a plane id (used
-// to skip the surface a ray leaves), and a uniform grid (count -> scan -> fill) replaces Hare's
-// Voxel_Grid.  Air properties follow Uniform_Medium (Classes_Medium_Props.cs:286-299).
+// to skip the surface a ray leaves), and a binned-SAH bounding volume hierarchy replaces Hare's
+// Voxel_Grid as the nearest-hit structure (any structure that returns the nearest hit with t > eps
+// gives the same answer).  Air properties follow Uniform_Medium (Classes_Medium_Props.cs:286-299).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -24,34 +25,218 @@ inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 inline D3 unit(D3 a) { double l = std::sqrt(dot(a, a)); return l > 0 ? mul(a, 1.0 / l) : a; }
 
-// Separating-axis overlap of a triangle and an axis-aligned box (Akenine-Moller, JGT 2001),
-// restated: 9 edge-cross axes, the 3 box normals and the triangle normal.
-bool tri_box(D3 a, D3 b, D3 c, D3 ctr, D3 h) {
-    D3 v0 = sub(a, ctr), v1 = sub(b, ctr), v2 = sub(c, ctr);
-    D3 e[3] = {sub(v1, v0), sub(v2, v1), sub(v0, v2)};
-    D3 V[3] = {v0, v1, v2};
-    const double hh[3] = {h.x, h.y, h.z};
-    for (int i = 0; i < 3; ++i) {
+// ---- BVH: binned SAH (16 bins, 3 axes), leaves of at most kLeafMax triangles ----
+struct BTri { float lo[3], hi[3], c[3]; };
+struct BNode { double lo[3], hi[3]; int left = -1, right = -1, first = 0, count = 0; };
+
+struct BvhBuilder {
+    std::vector<BTri> t;
+    std::vector<int> idx;
+    std::vector<BNode> nodes;
+    std::vector<int> order;
+    int max_depth = 0, leaves = 0;
+
+    static double area(const double lo[3], const double hi[3]) {
+        double e0 = std::max(0.0, hi[0] - lo[0]), e1 = std::max(0.0, hi[1] - lo[1]), e2 = std::max(0.0, hi[2] - lo[2]);
+        return 2 * (e0 * e1 + e1 * e2 + e2 * e0);
+    }
+
+    int make_leaf(int b, int e) {
+        BNode n;
+        bounds(b, e, n.lo, n.hi);
+        n.first = (int)order.size();
+        n.count = e - b;
+        for (int i = b; i < e; ++i) order.push_back(idx[i]);
+        nodes.push_back(n);
+        ++leaves;
+        return (int)nodes.size() - 1;
+    }
+
+    void bounds(int b, int e, double lo[3], double hi[3]) const {
+        for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+        for (int i = b; i < e; ++i)
+            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], (double)t[idx[i]].lo[k]); hi[k] = std::max(hi[k], (double)t[idx[i]].hi[k]); }
+    }
+
+    int build(int b, int e, int depth) {
+        max_depth = std::max(max_depth, depth);
+        const int n = e - b;
+        if (n <= 2 || depth >= 56) {
+            if (n <= kLeafMax) return make_leaf(b, e);
+        }
+        double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
+        for (int i = b; i < e; ++i)
+            for (int k = 0; k < 3; ++k) { clo[k] = std::min(clo[k], (double)t[idx[i]].c[k]); chi[k] = std::max(chi[k], (double)t[idx[i]].c[k]); }
+        double nlo[3], nhi[3];
+        bounds(b, e, nlo, nhi);
+        const double parea = area(nlo, nhi);
+        constexpr int NB = 16;
+        double best = 1e300;
+        int best_axis = -1, best_split = -1;
+        for (int ax = 0; ax < 3; ++ax) {
+            const double ext = chi[ax] - clo[ax];
+            if (!(ext > 0)) continue;
+            int cnt[NB] = {0};
+            double blo[NB][3], bhi[NB][3];
+            for (int q = 0; q < NB; ++q)
+                for (int k = 0; k < 3; ++k) { blo[q][k] = 1e300; bhi[q][k] = -1e300; }
+            for (int i = b; i < e; ++i) {
+                const BTri &x = t[idx[i]];
+                int q = std::min(NB - 1, (int)((x.c[ax] - clo[ax]) / ext * NB));
+                ++cnt[q];
+                for (int k = 0; k < 3; ++k) { blo[q][k] = std::min(blo[q][k], (double)x.lo[k]); bhi[q][k] = std::max(bhi[q][k], (double)x.hi[k]); }
+            }
+            double rarea[NB];
+            int rcnt[NB];
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            int c = 0;
+            for (int q = NB - 1; q > 0; --q) {
+                c += cnt[q];
+                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], blo[q][k]); hi[k] = std::max(hi[k], bhi[q][k]); }
+                rarea[q] = area(lo, hi);
+                rcnt[q] = c;
+            }
+            for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+            c = 0;
+            for (int q = 0; q < NB - 1; ++q) {
+                c += cnt[q];
+                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], blo[q][k]); hi[k] = std::max(hi[k], bhi[q][k]); }
+                if (c == 0 || rcnt[q + 1] == 0) continue;
+                const double cost = 1.0 + (area(lo, hi) * c + rarea[q + 1] * rcnt[q + 1]) / parea;
+                if (cost < best) { best = cost; best_axis = ax; best_split = q; }
+            }
+        }
+        if (n <= kLeafMax && (best_axis < 0 || best >= (double)n)) return make_leaf(b, e);
+        int mid;
+        if (best_axis < 0) {
+            mid = b + n / 2;  // coincident centroids: split the list
+        } else {
+            const double ext = chi[best_axis] - clo[best_axis];
+            auto it = std::partition(idx.begin() + b, idx.begin() + e, [&](int i) {
+                int q = std::min(NB - 1, (int)((t[i].c[best_axis] - clo[best_axis]) / ext * NB));
+                return q <= best_split;
+            });
+            mid = (int)(it - idx.begin());
+            if (mid == b || mid == e) mid = b + n / 2;
+        }
+        BNode node;
+        for (int k = 0; k < 3; ++k) { node.lo[k] = nlo[k]; node.hi[k] = nhi[k]; }
+        nodes.push_back(node);
+        const int me = (int)nodes.size() - 1;
+        const int l = build(b, mid, depth + 1);
+        const int r = build(mid, e, depth + 1);
+        nodes[me].left = l;
+        nodes[me].right = r;
+        return me;
+    }
+};
+
+// Builds hs.bvh and reorders the triangle arrays into leaf order.
+void build_bvh(HostScene &hs) {
+    BvhBuilder B;
+    B.t.resize(hs.ntri);
+    for (int i = 0; i < hs.ntri; ++i) {
+        const double *q = &hs.tri64[9 * (size_t)i];
         for (int k = 0; k < 3; ++k) {
-            D3 ax = k == 0 ? D3{0, -e[i].z, e[i].y} : (k == 1 ? D3{e[i].z, 0, -e[i].x} : D3{-e[i].y, e[i].x, 0});
-            double p0 = dot(V[0], ax), p1 = dot(V[1], ax), p2 = dot(V[2], ax);
-            double mn = std::min({p0, p1, p2}), mx = std::max({p0, p1, p2});
-            double r = hh[0] * std::fabs(ax.x) + hh[1] * std::fabs(ax.y) + hh[2] * std::fabs(ax.z);
-            double tol = 1e-9 * (r + std::fabs(mn) + std::fabs(mx)) + 1e-15;
-            if (mn > r + tol || mx < -r - tol) return false;
+            const double a = q[k], b = q[k] + q[3 + k], c = q[k] + q[6 + k];
+            B.t[i].lo[k] = (float)std::min({a, b, c});
+            B.t[i].hi[k] = (float)std::max({a, b, c});
+            B.t[i].c[k] = (float)((a + b + c) / 3.0);
         }
     }
-    const double cs[3][3] = {{v0.x, v1.x, v2.x}, {v0.y, v1.y, v2.y}, {v0.z, v1.z, v2.z}};
-    for (int a2 = 0; a2 < 3; ++a2) {
-        double mn = std::min({cs[a2][0], cs[a2][1], cs[a2][2]}), mx = std::max({cs[a2][0], cs[a2][1], cs[a2][2]});
-        double tol = 1e-9 * hh[a2] + 1e-15;
-        if (mn > hh[a2] + tol || mx < -hh[a2] - tol) return false;
+    B.idx.resize(hs.ntri);
+    for (int i = 0; i < hs.ntri; ++i) B.idx[i] = i;
+    int root = B.build(0, hs.ntri, 0);
+    // The device walk starts at an inner node: wrap a leaf root.
+    if (B.nodes[root].left < 0) {
+        BNode top;
+        for (int k = 0; k < 3; ++k) { top.lo[k] = B.nodes[root].lo[k]; top.hi[k] = B.nodes[root].hi[k]; }
+        BNode empty;
+        for (int k = 0; k < 3; ++k) { empty.lo[k] = 1e300; empty.hi[k] = -1e300; }
+        empty.first = 0;
+        empty.count = 1;
+        B.nodes.push_back(empty);
+        top.left = root;
+        top.right = (int)B.nodes.size() - 1;
+        B.nodes.push_back(top);
+        root = (int)B.nodes.size() - 1;
     }
-    D3 n = cross(e[0], e[1]);
-    double d = dot(n, v0);
-    double r = hh[0] * std::fabs(n.x) + hh[1] * std::fabs(n.y) + hh[2] * std::fabs(n.z);
-    return std::fabs(d) <= r * (1 + 1e-9) + 1e-15;
+    // Collapse to a 4-wide tree: an inner node's children are its binary descendants, opened
+    // largest-surface-area first until four (or only leaves) remain.  Nodes are laid out
+    // breadth-first so that the levels every ray walks share cache lines.
+    auto area_of = [&](int n) { return BvhBuilder::area(B.nodes[n].lo, B.nodes[n].hi); };
+    auto open = [&](int n, std::vector<int> &kids) {
+        kids.assign({B.nodes[n].left, B.nodes[n].right});
+        while (kids.size() < 4) {
+            int best = -1;
+            double ba = -1;
+            for (int k = 0; k < (int)kids.size(); ++k)
+                if (B.nodes[kids[k]].left >= 0 && area_of(kids[k]) > ba) { ba = area_of(kids[k]); best = k; }
+            if (best < 0) break;
+            const int x = kids[best];
+            kids[best] = B.nodes[x].left;
+            kids.push_back(B.nodes[x].right);
+        }
+    };
+    std::vector<int> order4{root};            // binary ids of the 4-wide inner nodes, BFS order
+    std::vector<std::vector<int>> kids4;
+    for (size_t q = 0; q < order4.size(); ++q) {
+        std::vector<int> kids;
+        open(order4[q], kids);
+        for (int k : kids)
+            if (B.nodes[k].left >= 0) order4.push_back(k);
+        kids4.push_back(kids);
+    }
+    std::vector<int> id4(B.nodes.size(), -1);
+    for (size_t q = 0; q < order4.size(); ++q) id4[order4[q]] = (int)q;
+    const double pad = 2e-6 * hs.scale;
+    auto lo_f = [&](double v) { return v > 1e299 ? INFINITY : (float)(v - pad); };
+    auto hi_f = [&](double v) { return v < -1e299 ? -INFINITY : (float)(v + pad); };
+    hs.bvh.assign(order4.size() * kBvhNodeFloats, 0.f);
+    int max_depth4 = 0;
+    std::vector<int> depth4(order4.size(), 0);
+    for (size_t q = 0; q < order4.size(); ++q) {
+        float *f = &hs.bvh[kBvhNodeFloats * q];
+        const std::vector<int> &kids = kids4[q];
+        for (int k = 0; k < 4; ++k) {
+            int code;
+            if (k < (int)kids.size()) {
+                const BNode &x = B.nodes[kids[k]];
+                f[0 + k] = lo_f(x.lo[0]); f[4 + k] = hi_f(x.hi[0]);
+                f[8 + k] = lo_f(x.lo[1]); f[12 + k] = hi_f(x.hi[1]);
+                f[16 + k] = lo_f(x.lo[2]); f[20 + k] = hi_f(x.hi[2]);
+                if (x.left >= 0) {
+                    code = id4[kids[k]];
+                    depth4[code] = depth4[q] + 1;
+                    max_depth4 = std::max(max_depth4, depth4[code]);
+                } else {
+                    code = ~(x.first * 16 + (x.count - 1));
+                }
+            } else {  // empty slot: flagged by its code (a slab test cannot reject an inverted box)
+                f[0 + k] = f[4 + k] = f[8 + k] = f[12 + k] = f[16 + k] = f[20 + k] = 0.f;
+                code = (int)0x80000000;
+            }
+            std::memcpy(&f[24 + k], &code, 4);
+        }
+    }
+    B.max_depth = max_depth4 + 1;
+    hs.bvh_nodes = (int)order4.size();
+    hs.bvh_leaves = B.leaves;
+    hs.bvh_depth = B.max_depth;
+    // reorder triangles into leaf order
+    std::vector<double> t64(hs.tri64.size());
+    std::vector<int32_t> tp(hs.ntri), tl(hs.ntri);
+    for (int i = 0; i < hs.ntri; ++i) {
+        const int s = B.order[i];
+        std::copy(&hs.tri64[9 * (size_t)s], &hs.tri64[9 * (size_t)s] + 9, &t64[9 * (size_t)i]);
+        tp[i] = hs.tri_poly[s];
+        tl[i] = hs.tri_plane[s];
+    }
+    hs.tri64.swap(t64);
+    hs.tri_poly.swap(tp);
+    hs.tri_plane.swap(tl);
 }
+
 
 }  // namespace
 
@@ -143,6 +328,79 @@ unsigned long long derived_broadband_bound(const HostScene &hs, int h, bool pure
     return (unsigned long long)std::min(k, 1e6);
 }
 
+bool bvh_shoot_host(const HostScene &hs, const double o[3], const double d[3], double t_min, int &tri, double &t) {
+    auto safe = [](double x) { return std::fabs(x) < 1e-20 ? std::copysign(1e-20, x) : x; };
+    const float ix = (float)(1.0 / safe(d[0])), iy = (float)(1.0 / safe(d[1])), iz = (float)(1.0 / safe(d[2]));
+    const float ox = (float)o[0] * ix, oy = (float)o[1] * iy, oz = (float)o[2] * iz;
+    std::vector<int> stack;
+    int node = 0;
+    double best = 1e300;
+    float bestf = 3.4e38f;
+    int bi = -1;
+    for (;;) {
+        bool done = false;
+        while (node >= 0) {
+            // one 4-wide node, as the device walks it (bvh4_step)
+            const float *f = &hs.bvh[kBvhNodeFloats * (size_t)node];
+            float tk[4];
+            int id[4];
+            for (int k = 0; k < 4; ++k) {
+                std::memcpy(&id[k], &f[24 + k], 4);
+                auto slab = [&](float a, float b, float inv, float oi, float &lo, float &hi) {
+                    const float t0 = std::fma(a, inv, -oi), t1 = std::fma(b, inv, -oi);
+                    lo = std::min(t0, t1);
+                    hi = std::max(t0, t1);
+                };
+                float x0, x1, y0, y1, z0, z1;
+                slab(f[0 + k], f[4 + k], ix, ox, x0, x1);
+                slab(f[8 + k], f[12 + k], iy, oy, y0, y1);
+                slab(f[16 + k], f[20 + k], iz, oz, z0, z1);
+                const float tn = std::max(std::max(x0, y0), std::max(z0, 0.f));
+                const float tf = std::min(std::min(x1, y1), std::min(z1, bestf));
+                tk[k] = (tn <= tf && id[k] != (int)0x80000000) ? tn : 3.4028235e38f;
+            }
+            auto cs = [&](int a, int b) {
+                if (tk[b] < tk[a]) { std::swap(tk[a], tk[b]); std::swap(id[a], id[b]); }
+            };
+            cs(0, 1); cs(2, 3); cs(0, 2); cs(1, 3); cs(1, 2);
+            if (tk[0] == 3.4028235e38f) {
+                if (stack.empty()) { done = true; break; }
+                node = stack.back();
+                stack.pop_back();
+                continue;
+            }
+            for (int k = 3; k >= 1; --k)
+                if (tk[k] != 3.4028235e38f) stack.push_back(id[k]);
+            node = id[0];
+        }
+        if (done) break;
+        const int code = ~node, f0 = code >> 4, cnt = (code & 15) + 1;
+        for (int k = 0; k < cnt; ++k) {
+            const double *q = &hs.tri64[9 * (size_t)(f0 + k)];
+            const D3 e1{q[3], q[4], q[5]}, e2{q[6], q[7], q[8]}, dd{d[0], d[1], d[2]};
+            const D3 p = cross(dd, e2);
+            const double det = dot(e1, p);
+            if (det == 0) continue;
+            const double inv = 1.0 / det;
+            const D3 s{o[0] - q[0], o[1] - q[1], o[2] - q[2]};
+            const double u = dot(s, p) * inv;
+            if (u < 0 || u > 1) continue;
+            const D3 qq = cross(s, e1);
+            const double v = dot(dd, qq) * inv;
+            if (v < 0 || u + v > 1) continue;
+            const double tt = dot(e2, qq) * inv;
+            if (tt > t_min && tt < best) { best = tt; bestf = (float)tt * 1.0000002f; bi = f0 + k; }
+        }
+        if (stack.empty()) break;
+        node = stack.back();
+        stack.pop_back();
+    }
+    if (bi < 0) return false;
+    tri = bi;
+    t = best;
+    return true;
+}
+
 bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err) {
     if (!d || d->n_vertices <= 0 || !d->vertices || d->n_polys <= 0 || !d->poly_offsets || !d->poly_indices ||
         !d->absorption || !d->scattering) {
@@ -224,52 +482,7 @@ bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err)
         hs.tri_plane[i] = it->second;
     }
 
-    // Uniform grid: about `lambda` cells per triangle, cubic cells.
-    double lambda = d->grid_cells_per_tri > 0 ? d->grid_cells_per_tri : 4.0;
-    double vol = ext[0] * ext[1] * ext[2];
-    double h = std::cbrt(vol / (lambda * hs.ntri));
-    long long total = 1;
-    for (int k = 0; k < 3; ++k) {
-        hs.dims[k] = (int)std::max(1.0, std::min(1024.0, std::round(ext[k] / h)));
-        total *= hs.dims[k];
-    }
-    while (total > (1ll << 24)) {
-        total = 1;
-        for (int k = 0; k < 3; ++k) { hs.dims[k] = std::max(1, hs.dims[k] / 2); total *= hs.dims[k]; }
-    }
-    const D3 bmin{hs.bmin[0], hs.bmin[1], hs.bmin[2]};
-    const D3 cell{ext[0] / hs.dims[0], ext[1] / hs.dims[1], ext[2] / hs.dims[2]};
-    std::vector<uint32_t> counts((size_t)total + 1, 0);
-    std::vector<std::pair<uint32_t, uint32_t>> pairs;  // (cell, tri)
-    pairs.reserve((size_t)hs.ntri * 4);
-    for (int i = 0; i < hs.ntri; ++i) {
-        const double *t = &hs.tri64[9 * (size_t)i];
-        D3 a{t[0], t[1], t[2]}, b = add(a, D3{t[3], t[4], t[5]}), c = add(a, D3{t[6], t[7], t[8]});
-        D3 lo{std::min({a.x, b.x, c.x}), std::min({a.y, b.y, c.y}), std::min({a.z, b.z, c.z})};
-        D3 hi{std::max({a.x, b.x, c.x}), std::max({a.y, b.y, c.y}), std::max({a.z, b.z, c.z})};
-        auto cl = [&](double v, double mn, double cs, int n) {
-            int k = (int)std::floor((v - mn) / cs);
-            return std::min(std::max(k, 0), n - 1);
-        };
-        int x0 = cl(lo.x, bmin.x, cell.x, hs.dims[0]), x1 = cl(hi.x, bmin.x, cell.x, hs.dims[0]);
-        int y0 = cl(lo.y, bmin.y, cell.y, hs.dims[1]), y1 = cl(hi.y, bmin.y, cell.y, hs.dims[1]);
-        int z0 = cl(lo.z, bmin.z, cell.z, hs.dims[2]), z1 = cl(hi.z, bmin.z, cell.z, hs.dims[2]);
-        D3 hh = mul(cell, 0.5 * (1 + 1e-6));
-        for (int x = x0; x <= x1; ++x)
-            for (int y = y0; y <= y1; ++y)
-                for (int z = z0; z <= z1; ++z) {
-                    D3 ctr{bmin.x + (x + 0.5) * cell.x, bmin.y + (y + 0.5) * cell.y, bmin.z + (z + 0.5) * cell.z};
-                    if (!tri_box(a, b, c, ctr, hh)) continue;
-                    uint32_t ci = (uint32_t)(((size_t)z * hs.dims[1] + y) * hs.dims[0] + x);
-                    pairs.emplace_back(ci, (uint32_t)i);
-                    counts[ci]++;
-                }
-    }
-    hs.cell_start.assign((size_t)total + 1, 0);
-    for (long long ci = 0; ci < total; ++ci) hs.cell_start[ci + 1] = hs.cell_start[ci] + counts[ci];
-    hs.cell_tris.assign(pairs.size(), 0);
-    std::vector<uint32_t> fill(hs.cell_start.begin(), hs.cell_start.end() - 1);
-    for (auto &pr : pairs) hs.cell_tris[fill[pr.first]++] = pr.second;
+    build_bvh(hs);
 
     medium_properties(d->temp_c, d->rel_humidity, d->pressure_hpa, d->air_choice, d->edge_correction, hs.atten,
                       &hs.c, &hs.rho);

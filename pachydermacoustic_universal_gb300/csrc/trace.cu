@@ -1,406 +1,122 @@
-// trace.cu -- sm_103a kernels of the stochastic split ray tracer.
+// trace.cu -- sm_103a kernels of the stochastic split ray tracer, as a wavefront pipeline.
 //
 // Hot path of SplitRayTracer.cast_ray_distributed / End_Trace ("Classes_Complete_Trace -
-// TaskAll.cs":335-536) on the GPU:
-//   k_broadband  phase A: one thread per primary ray -- emission (Classes_Sources.cs:256-265,
-//                390-403), grid traversal, broadband receiver detection (Classes_Receivers.cs:803-829),
-//                absorption (Classes_Materials.cs:166-178) and Scatter_Early (4498-4570); the band
-//                children of every bounce and the final split go to a device queue.
-//   k_octave     phases B and C: a persistent kernel whose threads pull octave rays from the queue
-//                (warp-aggregated tickets) and advance one bounce per loop iteration, so that every
-//                lane of a warp traverses in lock-step whatever phase its ray is in (Scatter_Late
-//                4629-4701, Scatter_VeryLate 4572-4627, Spherical_Receiver.CheckRay 837-877).
-//                Scatter_Late's specular children go to a per-thread stack: the lower-energy branch
-//                continues and the other is pushed, which keeps the depth near log2 of the subtree;
-//                a full stack spills to a device queue that the host drains with another launch.
-// Geometry is FP32 (Moller-Trumbore) with an FP64 re-test of candidates whose barycentric margin
-// lies in an epsilon band or whose determinant is near grazing.  Histograms accumulate in FP64 with
-// global atomics.  Random numbers: Philox4x32-10 keyed by (seed, primary, stream id, block) -- the
-// streams the CPU oracle draws -- so a ray's decisions do not depend on scheduling.
-#include <cfloat>
-#include <cstdint>
-
-#include "engine.h"
+// TaskAll.cs":335-536).  Octave rays live in a ring queue in HBM; every iteration of the device
+// loop runs five kernels on one stream:
+//   k_feed       1 thread: retire the last wave, hand the next batch of primaries to phase A while
+//                the ring runs low (primaries stream in until the run is done, so no launch tail).
+//   k_broadband  phase A, one thread per fed primary: emission (Classes_Sources.cs:256-265,
+//                390-403), BVH walk, broadband detection (Classes_Receivers.cs:803-829), absorption
+//                (Classes_Materials.cs:166-178) and Scatter_Early (4498-4570); the band children of
+//                every bounce and the final split are appended to the ring (TaskAll:347-424).
+//   k_wave       1 thread: size the wave -- as many ring items as leave room for their outputs.
+//   k_trace      one thread per wave item: the BVH walk only, a lean kernel that keeps many warps
+//                resident to hide L1/L2 latency; writes (triangle, t) per item.
+//   k_shade      one thread per wave item: receiver detection into FP64 histograms (837-877),
+//                absorption, one Philox draw block, Scatter_Late (phase B, 4629-4701) or
+//                Scatter_VeryLate (phase C, 4572-4627), then the surviving ray and a split child are
+//                appended to the ring with one atomic per warp (TaskAll:429-536).
+// Random numbers are Philox4x32-10 streams keyed by (seed, primary, stream id, block): the streams
+// the CPU oracle draws, so a ray's decisions do not depend on scheduling.
+#include "device_common.cuh"
 
 namespace pach {
 namespace {
 
-constexpr int kStack = 16;
-constexpr float kInvPi = 0.318309886183790671538f;
-constexpr float kBaryEps = 2e-5f;
-constexpr float kTP1 = 1e-2f;                  // TaskAll:351
-constexpr float kTP2 = 3.16227766016837933e-5f;  // 10^-4.5, TaskAll:331, 355
-constexpr float kTP3 = 1e-9f;                  // TaskAll:356
+constexpr unsigned FULL = 0xffffffffu;
 
-// ------------------------------------------------------------------------------------------
-// RNG (Philox4x32-10, Salmon et al. SC'11) and stream identities
-// ------------------------------------------------------------------------------------------
-__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
-    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+__device__ __forceinline__ ORayItem ring_load(const DevRun &r, unsigned long long i) {
+    return load_item(r.ring, i & (r.ring_cap - 1));
+}
+
+__device__ __forceinline__ void ring_store(const DevRun &r, unsigned long long i, const ORayItem &it) {
+    store_item(r.ring, i & (r.ring_cap - 1), it);
+}
+
+// All 32 lanes call: lane gets the first of its n ring slots; one atomic per warp.
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long *tail, int n) {
+    const int lane = threadIdx.x & 31;
+    int incl = n;
 #pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r) { k0 += W0; k1 += W1; }
-        const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-        const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
-        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
     }
-    return c;
-}
-
-__device__ __forceinline__ float u24(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
-
-__device__ __forceinline__ float4 draw(unsigned long long seed, uint32_t prim, unsigned long long sid, uint32_t b) {
-    const uint4 c = philox(make_uint4(b, prim, (uint32_t)sid, (uint32_t)(sid >> 32)), (uint32_t)seed,
-                           (uint32_t)(seed >> 32));
-    return make_float4(u24(c.x), u24(c.y), u24(c.z), u24(c.w));
-}
-
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-__device__ __forceinline__ unsigned long long sid_early(int k, int o, int q) {
-    return (1ull << 62) | ((unsigned long long)k << 5) | ((unsigned long long)o << 2) | (unsigned long long)q;
-}
-__device__ __forceinline__ unsigned long long sid_final(int o) { return (2ull << 62) | (unsigned long long)o; }
-__device__ __forceinline__ unsigned long long sid_late(unsigned long long parent, uint32_t nb) {
-    return (3ull << 62) |
-           (mix64(parent + 0x9E3779B97F4A7C15ull * (unsigned long long)(nb + 1)) & ((1ull << 62) - 1));
+    const int total = __shfl_sync(FULL, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(tail, (unsigned long long)total);
+    base = __shfl_sync(FULL, base, 31);
+    return base + (unsigned long long)(incl - n);
 }
 
 // ------------------------------------------------------------------------------------------
-// small vector helpers
+// scheduling (single thread)
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
-__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
-__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
-    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ float3 unit3(float3 a) { return a * rsqrtf(dot3(a, a)); }
-
-// Uniform-hemisphere direction about n (Lambert_Scattering, Classes_Materials.cs:4521-4552): frame
-// z = n, x from (0,0,1) unless |n.z| in (0.99, 1.01) then (1,0,0); azimuth 2 pi U1; cos(zenith) = U2.
-__device__ __forceinline__ float3 lambert(float3 n, float U1, float U2) {
-    float3 dx = make_float3(0.f, 0.f, 1.f);
-    const float proj = fabsf(n.z);
-    if (0.99f < proj && proj < 1.01f) dx = make_float3(1.f, 0.f, 0.f);
-    float3 dy = cross3(n, dx);
-    dx = cross3(dy, n);
-    dx = unit3(dx);
-    dy = unit3(dy);
-    float s, c;
-    sincospif(2.0f * U1, &s, &c);
-    const float sz = sqrtf(fmaxf(0.f, 1.f - U2 * U2));
-    return unit3(dx * (c * sz) + dy * (s * sz) + n * U2);
-}
-
-// ------------------------------------------------------------------------------------------
-// geometry
-// ------------------------------------------------------------------------------------------
-// FP64 re-test of triangle i (the FP32 ray converted exactly).
-__device__ __noinline__ bool retest64(const DevScene &S, int i, float3 of, float3 df, double &t) {
-    const double *T = S.tri64 + 9 * (size_t)i;
-    const double ox = of.x, oy = of.y, oz = of.z, dx = df.x, dy = df.y, dz = df.z;
-    const double e1x = T[3], e1y = T[4], e1z = T[5], e2x = T[6], e2y = T[7], e2z = T[8];
-    const double px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
-    const double det = e1x * px + e1y * py + e1z * pz;
-    if (det == 0.0) return false;
-    const double inv = 1.0 / det;
-    const double sx = ox - T[0], sy = oy - T[1], sz = oz - T[2];
-    const double u = (sx * px + sy * py + sz * pz) * inv;
-    if (u < 0.0 || u > 1.0) return false;
-    const double qx = sy * e1z - sz * e1y, qy = sz * e1x - sx * e1z, qz = sx * e1y - sy * e1x;
-    const double v = (dx * qx + dy * qy + dz * qz) * inv;
-    if (v < 0.0 || u + v > 1.0) return false;
-    t = (e2x * qx + e2y * qy + e2z * qz) * inv;
-    return true;
-}
-
-// Nearest hit along o + t d with t > t_eps, skipping triangles of plane `skip` (the surface the ray
-// leaves).  Uniform-grid DDA; a candidate is accepted once the walk has passed its distance.
-__device__ __forceinline__ bool trace_ray(const DevScene &S, float3 o, float3 d, int skip, float &t_best,
-                                          int &tri_best, unsigned long long &retests) {
-    const float idx_ = 1.0f / d.x, idy_ = 1.0f / d.y, idz_ = 1.0f / d.z;
-    float rx = (o.x - S.bminx) * S.icellx, ry = (o.y - S.bminy) * S.icelly, rz = (o.z - S.bminz) * S.icellz;
-    if (rx < 0.f || ry < 0.f || rz < 0.f || rx >= (float)S.nx || ry >= (float)S.ny || rz >= (float)S.nz) {
-        // origin outside the grid: clip to the box (Hare OBox.Intersect)
-        const float tx1 = (S.bminx - o.x) * idx_, tx2 = (S.bmaxx - o.x) * idx_;
-        const float ty1 = (S.bminy - o.y) * idy_, ty2 = (S.bmaxy - o.y) * idy_;
-        const float tz1 = (S.bminz - o.z) * idz_, tz2 = (S.bmaxz - o.z) * idz_;
-        const float tn = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
-        const float tf = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
-        if (!(tn <= tf) || tf < 0.f) return false;
-        const float t0 = fmaxf(tn, 0.f);
-        rx = (o.x + d.x * t0 - S.bminx) * S.icellx;
-        ry = (o.y + d.y * t0 - S.bminy) * S.icelly;
-        rz = (o.z + d.z * t0 - S.bminz) * S.icellz;
+__global__ void k_feed(DevRun r) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    WaveCtl *c = r.ctl;
+    c->head += c->m;  // retire the previous wave
+    c->m = 0;
+    c->pa_count = 0;
+    if (c->done) return;
+    const unsigned long long live = c->tail - c->head;
+    const long long fed = c->next_prim - c->prim_first;
+    if (c->per_prim == 0 && fed >= kPilotPrimaries) {
+        // the pilot batch ran alone: once its split trees are done, the octave rays it made per
+        // primary (x 1.5) is the ring footprint to plan the following batches with
+        if (live != 0) return;
+        c->per_prim = r.cnt->octave_rays / (unsigned long long)fed * 3 / 2 + 1;
+        if (c->per_prim < r.feed_bound) c->per_prim = r.feed_bound;
     }
-    int ix = min(max((int)floorf(rx), 0), S.nx - 1);
-    int iy = min(max((int)floorf(ry), 0), S.ny - 1);
-    int iz = min(max((int)floorf(rz), 0), S.nz - 1);
-    const int sx = d.x < 0.f ? -1 : 1, sy = d.y < 0.f ? -1 : 1, sz = d.z < 0.f ? -1 : 1;
-    float tmx = d.x != 0.f ? (S.bminx + (float)(ix + (sx > 0)) * S.cellx - o.x) * idx_ : FLT_MAX;
-    float tmy = d.y != 0.f ? (S.bminy + (float)(iy + (sy > 0)) * S.celly - o.y) * idy_ : FLT_MAX;
-    float tmz = d.z != 0.f ? (S.bminz + (float)(iz + (sz > 0)) * S.cellz - o.z) * idz_ : FLT_MAX;
-    const float tdx = d.x != 0.f ? S.cellx * fabsf(idx_) : FLT_MAX;
-    const float tdy = d.y != 0.f ? S.celly * fabsf(idy_) : FLT_MAX;
-    const float tdz = d.z != 0.f ? S.cellz * fabsf(idz_) : FLT_MAX;
-    float best = FLT_MAX;
-    int bi = -1;
-    const int max_steps = S.nx + S.ny + S.nz + 3;
-    for (int step = 0; step < max_steps; ++step) {
-        const uint32_t cell = ((uint32_t)iz * S.ny + iy) * S.nx + ix;
-        const uint32_t beg = __ldg(S.cell_start + cell), end = __ldg(S.cell_start + cell + 1);
-        for (uint32_t k = beg; k < end; ++k) {
-            const int i = (int)__ldg(S.cell_tris + k);
-            const float4 A = __ldg(S.tri + 3 * i);
-            if (__float_as_int(A.w) == skip) continue;
-            const float4 B = __ldg(S.tri + 3 * i + 1);
-            const float4 C = __ldg(S.tri + 3 * i + 2);
-            const float3 e1 = f3(B), e2 = f3(C);
-            const float3 p = cross3(d, e2);
-            const float det = dot3(e1, p);
-            const float3 s = o - f3(A);
-            const float inv = 1.0f / det;
-            const float u = dot3(s, p) * inv;
-            const float3 q = cross3(s, e1);
-            const float v = dot3(d, q) * inv;
-            const float t = dot3(e2, q) * inv;
-            const float margin = fminf(fminf(u, v), 1.0f - u - v);
-            if (fabsf(det) < C.w || !(fabsf(margin) > kBaryEps)) {
-                // near grazing, near an edge, or not finite: decide in FP64
-                double td;
-                ++retests;
-                if (retest64(S, i, o, d, td)) {
-                    const float tf = (float)td;
-                    if (tf > S.t_eps && tf < best) { best = tf; bi = i; }
-                }
-            } else if (margin > 0.f && t > S.t_eps && t < best) {
-                best = t;
-                bi = i;
-            }
-        }
-        const float texit = fminf(fminf(tmx, tmy), tmz);
-        if (best <= texit) break;
-        if (tmx < tmy) {
-            if (tmx < tmz) { ix += sx; if (ix < 0 || ix >= S.nx) break; tmx += tdx; }
-            else { iz += sz; if (iz < 0 || iz >= S.nz) break; tmz += tdz; }
-        } else {
-            if (tmy < tmz) { iy += sy; if (iy < 0 || iy >= S.ny) break; tmy += tdy; }
-            else { iz += sz; if (iz < 0 || iz >= S.nz) break; tmz += tdz; }
+    if (c->next_prim < c->prim_end && live <= r.low_water) {
+        // Hard limit: the phase-A output of every fed primary must fit.  Soft limit: the split trees
+        // grown from this batch keep the ring at most half full.
+        unsigned long long room = (r.ring_cap - live) / r.feed_bound;
+        const unsigned long long per_prim = c->per_prim ? c->per_prim : r.feed_bound;
+        const unsigned long long half = r.ring_cap / 2;
+        const unsigned long long soft = live < half ? (half - live) / per_prim : 0;
+        if (soft < room) room = soft > 0 ? soft : (live == 0 ? 1 : 0);
+        long long n = c->prim_end - c->next_prim;
+        if (n > r.feed_batch) n = r.feed_batch;
+        if (c->per_prim == 0 && n > kPilotPrimaries - fed) n = kPilotPrimaries - fed;
+        if ((unsigned long long)n > room) n = (long long)room;
+        if (n > 0) {
+            c->pa_begin = c->next_prim;
+            c->pa_count = n;
+            c->next_prim += n;
         }
     }
-    if (bi < 0) return false;
-    t_best = best;
-    tri_best = bi;
-    return true;
 }
 
-// ------------------------------------------------------------------------------------------
-// receivers
-// ------------------------------------------------------------------------------------------
-// Sphere test of segment [o, o + tseg d] (Classes_Receivers.cs:839-849).  The discriminant is
-// formed as r^2 - |m - b d|^2 (equal to b^2 - c for a unit d) to avoid cancellation in FP32.
-__device__ __forceinline__ bool sphere_hit(float4 c, float3 o, float3 d, float tseg, float &t, float &half) {
-    const float3 m = make_float3(o.x - c.x, o.y - c.y, o.z - c.z);
-    const float b = dot3(m, d);
-    const float cc = dot3(m, m) - c.w;
-    if (cc > 0.f && b > 0.f) return false;
-    const float3 perp = m - d * b;
-    const float disc = c.w - dot3(perp, perp);
-    if (disc < 0.f) return false;
-    t = -b;  // chord midpoint (t1 + t2) / 2
-    if (!(t > 0.f && t < tseg)) return false;
-    half = sqrtf(disc);  // (t2 - t1) / 2
-    return true;
-}
-
-// Directional_Histogram.Add (Classes_Receivers.cs:1813-1825) + Reflection_Analysis_Data.
-__device__ __forceinline__ void hist_add(const DevRun &r, int k, int oct, long long bin, float e, float3 d, int kind) {
-    const size_t base = ((size_t)k * kBands + oct) * r.T + bin;
-    atomicAdd(r.hE + base, (double)e);
-    atomicAdd(r.hP + base, (double)sqrtf(e * r.rho_c));
-    const float ca[3] = {-d.x, -d.y, -d.z};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const size_t j = (((size_t)k * 3 + a) * kBands + oct) * r.T + bin;
-        atomicAdd((ca[a] > 0.f ? r.hDp : r.hDn) + j, (double)(ca[a] * e));
-    }
-    atomicAdd(r.hAn + (((size_t)k * 3 + kind) * kBands + oct) * r.T + bin, (double)e);
-}
-
-// Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half.
-__device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
-                                                  double t_sum, float Iabs, int oct, int mask) {
-    uint32_t n = 0;
-    for (int k = 0; k < r.R; ++k) {
-        float t, half;
-        if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
-        ++n;
-        const double time = t_sum + (double)(t * r.inv_c);
-        const long long bin = (long long)(time * r.fs);
-        if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
-        const float e = Iabs * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
-        hist_add(r, k, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
-    }
-    return n;
-}
-
-// Spherical_Receiver.CheckBroadbandRay (Classes_Receivers.cs:803-829): every band of the range,
-// analysis bin 0 (specular).
-__device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
-                                                 double t_sum, const float (&E)[kBands], const float (&sc)[kBands]) {
-    uint32_t n = 0;
-    for (int k = 0; k < r.R; ++k) {
-        float t, half;
-        if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
-        ++n;
-        const double time = t_sum + (double)(t * r.inv_c);
-        const long long bin = (long long)(time * r.fs);
-        if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
-#pragma unroll
-        for (int oct = 0; oct < kBands; ++oct) {
-            if (oct < r.oct_lo || oct > r.oct_hi) continue;
-            const float e = E[oct] * sc[oct] * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
-            hist_add(r, k, oct, bin, e, d, 0);
-        }
-    }
-    return n;
-}
-
-// ------------------------------------------------------------------------------------------
-// emission
-// ------------------------------------------------------------------------------------------
-__device__ __forceinline__ float3 emit_dir(const DevRun &r, long long prim, int kind) {
-    const float4 U = draw(r.seed, (uint32_t)prim, 0ull, 0u);
-    if (kind == PACH_SOURCE_RANDOM) {  // RandomSource (Classes_Sources.cs:256-265)
-        float st, ct, sp, cp;
-        sincospif(2.0f * U.x, &st, &ct);
-        sincospif(2.0f * U.y, &sp, &cp);
-        return make_float3(st * cp, st * sp, ct);
-    }
-    if (kind == PACH_SOURCE_UNIFORM) {
-        const float z = 1.0f - 2.0f * U.x;
-        const float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
-        float sp, cp;
-        sincospif(2.0f * U.y, &sp, &cp);
-        return make_float3(rr * cp, rr * sp, z);
-    }
-    // GeodesicSource (Classes_Sources.cs:390-403): face (per-source ray count) mod 80, point on face
-    const long long j = prim / r.nsrc;
-    const int f = (int)(j % kGeoFaces);
-    float u = U.x, v = U.y;
-    if (u + v > 1.f) { u = 1.f - u; v = 1.f - v; }
-    const float3 a = f3(r.geo[3 * f]), b = f3(r.geo[3 * f + 1]), c = f3(r.geo[3 * f + 2]);
-    return unit3(a + (b - a) * u + (c - a) * v);
-}
-
-// ------------------------------------------------------------------------------------------
-// queue items
-// ------------------------------------------------------------------------------------------
-struct Ray {
-    float3 p, d;
-    float I, scale;
-    double t_sum;
-    uint32_t prim, nb;
-    unsigned long long sid;
-    int oct, mask, phase, plane;
-};
-
-__device__ __forceinline__ ORayItem to_item(const Ray &R) {
-    ORayItem it;
-    it.px = R.p.x; it.py = R.p.y; it.pz = R.p.z; it.I = R.I;
-    it.dx = R.d.x; it.dy = R.d.y; it.dz = R.d.z; it.scale = R.scale;
-    it.t_sum = R.t_sum; it.prim = R.prim; it.nb = R.nb; it.sid = R.sid;
-    it.meta = (uint32_t)R.oct | ((uint32_t)R.mask << 3) | ((uint32_t)R.phase << 5);
-    it.plane = R.plane;
-    return it;
-}
-
-__device__ __forceinline__ Ray to_ray(const ORayItem &it) {
-    Ray R;
-    R.p = make_float3(it.px, it.py, it.pz);
-    R.d = make_float3(it.dx, it.dy, it.dz);
-    R.I = it.I; R.scale = it.scale; R.t_sum = it.t_sum; R.prim = it.prim; R.nb = it.nb; R.sid = it.sid;
-    R.oct = (int)(it.meta & 7u); R.mask = (int)((it.meta >> 3) & 3u); R.phase = (int)((it.meta >> 5) & 1u);
-    R.plane = it.plane;
-    return R;
-}
-
-__device__ __forceinline__ Ray new_ray(float3 p, float3 d, float I, float scale, double t_sum, uint32_t prim,
-                                       unsigned long long sid, int oct, int mask, int plane) {
-    Ray R;
-    R.p = p; R.d = d; R.I = I; R.scale = scale; R.t_sum = t_sum; R.prim = prim; R.nb = 0; R.sid = sid;
-    R.oct = oct; R.mask = mask; R.phase = 0; R.plane = plane;
-    return R;
-}
-
-__device__ __forceinline__ void store_item(ORayItem *q, unsigned long long slot, const ORayItem &it) {
-    float4 *dst = reinterpret_cast<float4 *>(q + slot);
-    const float4 *src = reinterpret_cast<const float4 *>(&it);
-    dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-}
-
-__device__ __forceinline__ ORayItem load_item(const ORayItem *q, unsigned long long i) {
-    const float4 *s = reinterpret_cast<const float4 *>(q + i);
-    ORayItem it;
-    float4 *d = reinterpret_cast<float4 *>(&it);
-    d[0] = __ldcs(s); d[1] = __ldcs(s + 1); d[2] = __ldcs(s + 2); d[3] = __ldcs(s + 3);
-    return it;
-}
-
-// ------------------------------------------------------------------------------------------
-// counters
-// ------------------------------------------------------------------------------------------
-struct LocalCounters {
-    unsigned long long v[11] = {0};  // prim, seg_broad, seg_b, seg_c, oct, end_traces, det, capped, retests, overflow, spills
-    double lost = 0, init = 0;
-};
-enum { C_PRIM, C_SEGA, C_SEGB, C_SEGC, C_OCT, C_END, C_DET, C_CAP, C_RET, C_OVF, C_SPILL };
-
-__device__ void flush_counters(const DevRun &r, const LocalCounters &L) {
-    __shared__ unsigned long long s_u[11];
-    __shared__ double s_d[2];
-    if (threadIdx.x < 11) s_u[threadIdx.x] = 0;
-    if (threadIdx.x < 2) s_d[threadIdx.x] = 0;
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 11; ++i)
-        if (L.v[i]) atomicAdd(&s_u[i], L.v[i]);
-    if (L.lost != 0) atomicAdd(&s_d[0], L.lost);
-    if (L.init != 0) atomicAdd(&s_d[1], L.init);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        DevCounters *c = r.cnt;
-        unsigned long long *dst[11] = {&c->primaries, &c->seg_broad, &c->seg_b, &c->seg_c, &c->octave_rays,
-                                       &c->end_traces, &c->detections, &c->capped, &c->retests, &c->queue_overflow,
-                                       &c->stack_spills};
-        for (int i = 0; i < 11; ++i)
-            if (s_u[i]) atomicAdd(dst[i], s_u[i]);
-        if (s_d[0] != 0) atomicAdd(&c->lost_energy, s_d[0]);
-        if (s_d[1] != 0) atomicAdd(&c->initial_energy, s_d[1]);
-    }
-}
-
-__device__ __forceinline__ void load_receivers(const DevRun &r, float4 *rec) {
-    for (int i = threadIdx.x; i < r.R; i += blockDim.x) rec[i] = r.rec[i];
-    __syncthreads();
+__global__ void k_wave(DevRun r) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    WaveCtl *c = r.ctl;
+    if (c->done) { c->m = 0; return; }
+    const unsigned long long live = c->tail - c->head;
+    if (live > c->peak_live) c->peak_live = live;
+    unsigned long long m = (r.ring_cap - live) / 2;  // each item leaves at most two
+    if (m > live) m = live;
+    if (m > r.max_wave) m = r.max_wave;
+    c->m = m;
+    c->trace_next = 0;
+    if (m) ++c->waves;
+    if (live == 0 && c->next_prim >= c->prim_end) c->done = 1;
+    if (live > 0 && m == 0) { ++c->overflow; c->done = 1; }  // ring full: cannot make progress
 }
 
 // ------------------------------------------------------------------------------------------
 // phase A: broadband rays (cast_ray_distributed, TaskAll:347-424)
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_broadband(DevRun r, long long p0, long long p1) {
+__global__ void __launch_bounds__(128) k_broadband(DevRun r) {
     extern __shared__ float4 s_rec[];
     load_receivers(r, s_rec);
     LocalCounters L;
     const DevScene &S = r.S;
+    WaveCtl *c = r.ctl;
+    const long long p0 = c->pa_begin, cnt = c->pa_count;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long prim = p0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; prim < p1; prim += stride) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += stride) {
+        const long long prim = p0 + i;
         const int s = (int)((prim + 1) % r.nsrc);  // SourceCluster round robin (Classes_Sources.cs:712-722)
         const float4 src = r.src[s];
         float3 d;
@@ -427,7 +143,9 @@ __global__ void __launch_bounds__(256) k_broadband(DevRun r, long long p0, long 
         do {
             float t;
             int tri;
-            const bool hit = trace_ray(S, pos, d, plane, t, tri, L.v[C_RET]);
+            TraceWork tw;
+            const bool hit = trace_ray(S, pos, d, plane, t, tri, tw);
+            L.v[C_RET] += tw.retests;
             ++L.v[C_SEGA];
             if (!hit) {
                 if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, 1e6f, t_sum, E, sc);
@@ -458,13 +176,7 @@ __global__ void __launch_bounds__(256) k_broadband(DevRun r, long long p0, long 
             int nchild = 0;
 #pragma unroll
             for (int o = 0; o < kBands; ++o) nchild += (E[o] != 0.f) ? (tau[o] > 0.f ? 3 : 1) : 0;
-            unsigned long long slot = 0;
-            bool room = false;
-            if (nchild) {
-                slot = atomicAdd(r.q_out_count, (unsigned long long)nchild);
-                room = slot + nchild <= r.q_out_cap;
-                if (!room) ++L.v[C_OVF];
-            }
+            unsigned long long slot = nchild ? atomicAdd(&c->tail, (unsigned long long)nchild) : 0ull;
 #pragma unroll
             for (int o = 0; o < kBands; ++o) {
                 if (E[o] == 0.f) continue;
@@ -480,10 +192,11 @@ __global__ void __launch_bounds__(256) k_broadband(DevRun r, long long p0, long 
                     ch.I *= (1.f - tau[o]);
                     td.d = ch.d * -1.f;
                     td.sid = sid_early(k, o, 2);
-                    if (room) { store_item(r.q_out, slot++, to_item(tr)); store_item(r.q_out, slot++, to_item(td)); }
+                    ring_store(r, slot++, to_item(tr));
+                    ring_store(r, slot++, to_item(td));
                     L.v[C_OCT] += 2;
                 }
-                if (room) store_item(r.q_out, slot++, to_item(ch));
+                ring_store(r, slot++, to_item(ch));
                 ++L.v[C_OCT];
             }
             d = d - n * (2.f * cos_t);
@@ -494,14 +207,12 @@ __global__ void __launch_bounds__(256) k_broadband(DevRun r, long long p0, long 
         } while (eh > kTP1);
         if (!lost) {
             const int nfin = r.oct_hi - r.oct_lo + 1;
-            unsigned long long slot = atomicAdd(r.q_out_count, (unsigned long long)nfin);
-            const bool room = slot + nfin <= r.q_out_cap;
-            if (!room) ++L.v[C_OVF];
+            unsigned long long slot = atomicAdd(&c->tail, (unsigned long long)nfin);
 #pragma unroll
             for (int o = 0; o < kBands; ++o) {
                 if (o < r.oct_lo || o > r.oct_hi) continue;
                 const Ray it = new_ray(pos, d, E[o], sc[o], t_sum, (uint32_t)prim, sid_final(o), o, 0, plane);
-                if (room) store_item(r.q_out, slot++, to_item(it));
+                ring_store(r, slot++, to_item(it));
                 ++L.v[C_OCT];
             }
         }
@@ -511,121 +222,179 @@ __global__ void __launch_bounds__(256) k_broadband(DevRun r, long long p0, long 
 }
 
 // ------------------------------------------------------------------------------------------
-// phases B and C: octave rays (TaskAll:429-536)
+// phases B and C, split into the BVH walk and the surface interaction
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_octave(DevRun r) {
+// Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
+// its next leaf and tests it; a lane whose walk has ended writes its hit and takes the next wave
+// item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
+    WaveCtl *c = r.ctl;
+    const unsigned long long m = c->m, head = c->head;
+    const DevScene &S = r.S;
+    const int lane = threadIdx.x & 31;
+    TraceWork w;
+    bool have = false, exhausted = false;
+    unsigned long long j = 0;
+    float3 o = make_float3(0.f, 0.f, 0.f), d = o;
+    float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f, best = FLT_MAX;
+    int skip = -1, node = 0, sp = 0, bi = -1;
+    int stack[kBvhStack];
+    for (;;) {
+        const unsigned need = __ballot_sync(FULL, !have && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&c->trace_next, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (!have && !exhausted) {
+                j = base + __popc(need & ((1u << lane) - 1u));
+                if (j < m) {
+                    const float4 *q = reinterpret_cast<const float4 *>(r.ring + ((head + j) & (r.ring_cap - 1)));
+                    const float4 P = __ldcs(q), D = __ldcs(q + 1), X = __ldcs(q + 3);
+                    o = f3(P);
+                    d = f3(D);
+                    skip = __float_as_int(X.w);
+                    const float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
+                    const float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
+                    const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
+                    ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
+                    ox = o.x * ix; oy = o.y * iy; oz = o.z * iz;
+                    node = 0; sp = 0; best = FLT_MAX; bi = -1;
+                    have = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(FULL, have)) break;
+        if (!have) continue;
+        bool fin = false;
+        while (node >= 0) {
+            ++w.nodes;
+            int next;
+            if (!bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) {
+                if (sp == 0) { fin = true; break; }
+                node = stack[--sp];
+                continue;
+            }
+            node = next;
+        }
+        if (!fin) {
+            const int code = ~node;
+            const int f0 = code >> 4, cnt = (code & 15) + 1;
+            w.tris += (unsigned)cnt;
+            for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+            if (sp == 0) fin = true;
+            else node = stack[--sp];
+        }
+        if (fin) {
+            r.hits[j] = make_int2(bi, __float_as_int(best));
+            have = false;
+        }
+    }
+    // one atomic per warp for each counter
+    unsigned long long a = w.retests, b = w.nodes, c2 = w.tris;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(FULL, a, o);
+        b += __shfl_down_sync(FULL, b, o);
+        c2 += __shfl_down_sync(FULL, c2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (a) atomicAdd(&r.cnt->retests, a);
+        if (b) atomicAdd(&r.cnt->bvh_nodes, b);
+        if (c2) atomicAdd(&r.cnt->tri_tests, c2);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shade(DevRun r) {
     extern __shared__ float4 s_rec[];
     load_receivers(r, s_rec);
     LocalCounters L;
     const DevScene &S = r.S;
-    const unsigned long long n_in = min(*r.q_in_count, r.q_in_cap);
-    ORayItem stack[kStack];
-    int sp = 0;
-    bool have = false;
-    Ray R;
+    WaveCtl *c = r.ctl;
+    const unsigned long long m = c->m, head = c->head;
+    const unsigned long long m32 = (m + 31) & ~31ull;
     const int lane = threadIdx.x & 31;
-    while (true) {
-        // ---- acquire work: own stack first, then the shared queue (one ticket atomic per warp) ----
-        const unsigned act = __activemask();
-        const bool need = !have && sp == 0;
-        const unsigned want = __ballot_sync(act, need);
-        if (want) {
-            const int leader = __ffs(want) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(r.q_in_head, (unsigned long long)__popc(want));
-            base = __shfl_sync(act, base, leader);
-            if (need) {
-                const unsigned long long idx = base + __popc(want & ((1u << lane) - 1u));
-                if (idx >= n_in) break;
-                R = to_ray(load_item(r.q_in, idx));
-                have = true;
-            }
-        }
-        if (!have) {
-            R = to_ray(stack[--sp]);
-            have = true;
-        }
-        // ---- one bounce ----
-        float t;
-        int tri;
-        const bool hit = trace_ray(S, R.p, R.d, R.plane, t, tri, L.v[C_RET]);
-        ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
-        L.v[C_DET] += detect_octave(r, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask);
-        if (!hit) {  // lost ray: no End_Trace after a miss in phase B (TaskAll:437-443)
-            L.lost += (double)(R.I * R.scale);
-            have = false;
-            continue;
-        }
-        R.t_sum += (double)t * r.inv_c_d;
-        R.p = R.p + R.d * t;
-        const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
-        R.plane = __float_as_int(A.w);
-        const int poly = __float_as_int(B.w);
-        const float3 n = f3(__ldg(S.pnormal + poly));
-        const float cos_t = dot3(n, R.d);
-        const float4 m = __ldg(S.mat + poly * kBands + R.oct);  // (1-alpha, s_lo, s_mid, s_hi)
-        R.I *= m.x;
-        const float4 U = draw(r.seed, R.prim, R.sid, 1u + R.nb);
-        const uint32_t nb = R.nb++;
-        const bool transmit = S.has_trans && !r.pure_specular && U.x < __ldg(S.trans + poly * kBands + R.oct);
-        const float3 spec = R.d - n * (2.f * cos_t);
-        const float3 nn = cos_t > 0.f ? n * -1.f : n;
-        bool test_loop = true;
-        if (R.phase == 0) {
-            // Scatter_Late
-            if (r.pure_specular || U.y > m.w) {
-                R.d = transmit ? spec * -1.f : spec;
-                R.mask &= ~1;
+    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ull;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = warp0; base < m32; base += stride) {
+        const unsigned long long j = base + lane;
+        int nout = 0;
+        Ray R, C;
+        if (j < m) {
+            R = to_ray(ring_load(r, head + j));
+            const int2 h = r.hits[j];
+            const bool hit = h.x >= 0;
+            const float t = __int_as_float(h.y);
+            ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
+            L.v[C_DET] += detect_octave(r, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask);
+            if (!hit) {
+                // lost: no End_Trace after a miss in phase B (TaskAll:437-443), loop exit in phase C (500-505)
+                L.lost += (double)(R.I * R.scale);
             } else {
-                const bool split = U.y > m.y;
-                Ray C;
-                if (split) {
-                    C = R;
-                    C.I = R.I * (1.f - m.z);
-                    R.I *= m.z;
-                    C.mask &= ~1;
-                    C.d = transmit ? spec * -1.f : spec;
-                    C.sid = sid_late(R.sid, nb);
-                    C.nb = 0;
-                    C.phase = 0;
-                    ++L.v[C_OCT];
-                }
-                const float3 ld = lambert(nn, U.z, U.w);
-                R.d = transmit ? ld * -1.f : ld;
-                R.mask |= 3;
-                if (split) {
-                    if (C.I < R.I) {
-                        // continue with the lower-energy child; the parent is mid-loop, settle its phase
-                        const Ray tmp = R;
-                        R = C;
-                        C = tmp;
-                        test_loop = false;
-                        if (!(C.t_sum < r.cotime && C.I > kTP2)) { C.phase = 1; ++L.v[C_END]; }
-                    }
-                    if (sp < kStack) {
-                        stack[sp++] = to_item(C);
+                R.t_sum += (double)t * r.inv_c_d;
+                R.p = R.p + R.d * t;
+                const float4 A = __ldg(S.tri + 3 * h.x), B = __ldg(S.tri + 3 * h.x + 1);
+                R.plane = __float_as_int(A.w);
+                const int poly = __float_as_int(B.w);
+                const float3 n = f3(__ldg(S.pnormal + poly));
+                const float cos_t = dot3(n, R.d);
+                const float4 mt = __ldg(S.mat + poly * kBands + R.oct);  // (1-alpha, s_lo, s_mid, s_hi)
+                R.I *= mt.x;
+                const float4 U = draw(r.seed, R.prim, R.sid, 1u + R.nb);
+                const uint32_t nb = R.nb++;
+                const bool transmit = S.has_trans && !r.pure_specular && U.x < __ldg(S.trans + poly * kBands + R.oct);
+                const float3 spec = R.d - n * (2.f * cos_t);
+                const float3 nn = cos_t > 0.f ? n * -1.f : n;
+                bool alive = true;
+                bool split = false;
+                if (R.phase == 0) {
+                    // Scatter_Late
+                    if (r.pure_specular || U.y > mt.w) {
+                        R.d = transmit ? spec * -1.f : spec;
+                        R.mask &= ~1;
                     } else {
-                        const unsigned long long slot = atomicAdd(r.q_out_count, 1ull);
-                        if (slot < r.q_out_cap) store_item(r.q_out, slot, to_item(C));
-                        else ++L.v[C_OVF];
-                        ++L.v[C_SPILL];
+                        if (U.y > mt.y) {
+                            split = true;
+                            C = R;
+                            C.I = R.I * (1.f - mt.z);
+                            R.I *= mt.z;
+                            C.mask &= ~1;
+                            C.d = transmit ? spec * -1.f : spec;
+                            C.sid = sid_late(R.sid, nb);
+                            C.nb = 0;
+                            C.phase = 0;
+                            ++L.v[C_OCT];
+                        }
+                        const float3 ld = lambert(nn, U.z, U.w);
+                        R.d = transmit ? ld * -1.f : ld;
+                        R.mask |= 3;
                     }
+                    // phase-B loop test (TaskAll:473): failing it enters End_Trace, which always
+                    // traces at least one more segment
+                    if (!(R.t_sum < r.cotime && R.I > kTP2)) { R.phase = 1; ++L.v[C_END]; }
+                } else {
+                    // Scatter_VeryLate
+                    if (!r.pure_specular && U.y < mt.z) {
+                        R.d = lambert(nn, U.z, U.w);
+                        R.mask |= 3;
+                    } else {
+                        R.d = spec;
+                        R.mask &= ~1;
+                    }
+                    if (transmit) R.d = R.d * -1.f;
+                    alive = R.t_sum < r.cotime && R.I > kTP3;  // TaskAll:534
                 }
+                if (alive && (long long)R.nb >= r.max_seg) { ++L.v[C_CAP]; alive = false; }
+                if (!alive && split) { R = C; split = false; alive = true; }
+                nout = (alive ? 1 : 0) + (split ? 1 : 0);
             }
-            if (test_loop && !(R.t_sum < r.cotime && R.I > kTP2)) { R.phase = 1; ++L.v[C_END]; }
-        } else {
-            // Scatter_VeryLate
-            if (!r.pure_specular && U.y < m.z) {
-                R.d = lambert(nn, U.z, U.w);
-                R.mask |= 3;
-            } else {
-                R.d = spec;
-                R.mask &= ~1;
-            }
-            if (transmit) R.d = R.d * -1.f;
-            if (!(R.t_sum < r.cotime && R.I > kTP3)) have = false;
         }
-        if (have && (long long)R.nb >= r.max_seg) { ++L.v[C_CAP]; have = false; }
+        const unsigned long long slot = warp_append(&c->tail, nout);
+        if (nout >= 1) ring_store(r, slot, to_item(R));
+        if (nout == 2) ring_store(r, slot + 1, to_item(C));
     }
     flush_counters(r, L);
 }
@@ -640,7 +409,7 @@ __global__ void k_paths(DevScene S, int n, const double *o, const double *dd, in
     float3 p = make_float3((float)o[3 * i], (float)o[3 * i + 1], (float)o[3 * i + 2]);
     float3 d = unit3(make_float3((float)dd[3 * i], (float)dd[3 * i + 1], (float)dd[3 * i + 2]));
     int plane = -1;
-    unsigned long long rt = 0;
+    TraceWork rt;
     for (int b = 0; b < maxb; ++b) {
         const size_t k = (size_t)i * maxb + b;
         poly[k] = -1; tout[k] = 0; pts[3 * k] = pts[3 * k + 1] = pts[3 * k + 2] = 0;
@@ -676,18 +445,48 @@ __global__ void k_emit(DevRun r, long long p0, int n, double *out) {
 // ------------------------------------------------------------------------------------------
 // host wrappers
 // ------------------------------------------------------------------------------------------
-cudaError_t launch_broadband(const DevRun &r, long long p0, long long p1, int blocks, int threads, cudaStream_t s) {
-    k_broadband<<<blocks, threads, sizeof(float4) * (size_t)(r.R > 0 ? r.R : 1), s>>>(r, p0, p1);
+static size_t rec_smem(const DevRun &r) { return sizeof(float4) * (size_t)(r.R > 0 ? r.R : 1); }
+
+cudaError_t launch_feed(const DevRun &r, cudaStream_t s) {
+    k_feed<<<1, 32, 0, s>>>(r);
     return cudaGetLastError();
 }
 
-cudaError_t launch_octave(const DevRun &r, int blocks, int threads, cudaStream_t s) {
-    k_octave<<<blocks, threads, sizeof(float4) * (size_t)(r.R > 0 ? r.R : 1), s>>>(r);
+cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s) {
+    k_broadband<<<blocks, threads, rec_smem(r), s>>>(r);
     return cudaGetLastError();
 }
 
-cudaError_t octave_kernel_occupancy(int threads, int *blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_octave, threads, sizeof(float4) * 64);
+cudaError_t launch_wave(const DevRun &r, cudaStream_t s) {
+    k_wave<<<1, 32, 0, s>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s) {
+    switch (variant) {
+        case 3: k_trace<3><<<blocks, threads, 0, s>>>(r); break;
+        case 5: k_trace<5><<<blocks, threads, 0, s>>>(r); break;
+        case 6: k_trace<6><<<blocks, threads, 0, s>>>(r); break;
+        default: k_trace<4><<<blocks, threads, 0, s>>>(r); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s) {
+    k_shade<<<blocks, threads, rec_smem(r), s>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade) {
+    cudaError_t e;
+    switch (variant) {
+        case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<3>, threads, 0); break;
+        case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<5>, threads, 0); break;
+        case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<6>, threads, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4>, threads, 0); break;
+    }
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade, threads, smem_shade);
 }
 
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,

@@ -12,7 +12,7 @@ from ._capi import check, dptr, iptr
 class DeviceScene:
     """A scene resident on the GPU (pach_scene_create)."""
 
-    def __init__(self, scene, grid_cells_per_tri: int = 0):
+    def __init__(self, scene):
         L = _capi.lib()
         self._v = np.ascontiguousarray(scene.vertices, dtype=np.float64).reshape(-1)
         self._o = np.ascontiguousarray(scene.poly_offsets, dtype=np.int32)
@@ -23,7 +23,7 @@ class DeviceScene:
         self._t = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1) if tr is not None else None
         desc = _capi.SceneDesc(self._v.size // 3, dptr(self._v), self._o.size - 1, iptr(self._o), iptr(self._i),
                                dptr(self._a), dptr(self._s), dptr(self._t), scene.temp_c, scene.rel_humidity,
-                               scene.pressure_hpa, scene.air_choice, scene.edge_correction, grid_cells_per_tri, 0)
+                               scene.pressure_hpa, scene.air_choice, scene.edge_correction, 0, 0)
         h = C.c_void_p()
         check(L.pach_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
@@ -69,8 +69,9 @@ def receiver_array(receivers):
 
 
 def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 7), is_order=-1, sample_rate=1000,
-                pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, queue_budget_items=0,
-                block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0):
+                pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
+                block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
+                ring_log2=0, kernel_timing=False):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -83,9 +84,12 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.pure_specular = int(bool(pure_specular))
     p.max_broadband_bounces = int(max_broadband_bounces)
     p.max_segments_per_ray = int(max_segments_per_ray)
-    p.queue_budget_items = int(queue_budget_items)
+    p.feed_batch = int(feed_batch)
     p.block_threads = int(block_threads)
     p.blocks_per_sm = int(blocks_per_sm)
+    p.wave_kilo_items = int(wave_kilo_items)
+    p.ring_log2 = int(ring_log2)
+    p.kernel_timing = int(bool(kernel_timing))
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
     return p
@@ -174,6 +178,25 @@ def specular_paths(dscene: DeviceScene, origins, dirs, max_bounces):
     check(_capi.lib().pach_trace_specular_paths(dscene.handle, n, dptr(o), dptr(d), max_bounces, iptr(poly), dptr(t),
                                                 dptr(pts)))
     return poly, t, pts
+
+
+def shoot_host(scene, origins, dirs):
+    """Nearest hits found by the engine's BVH walked on the host (no GPU needed)."""
+    v = np.ascontiguousarray(scene.vertices, dtype=np.float64).reshape(-1)
+    offs = np.ascontiguousarray(scene.poly_offsets, dtype=np.int32)
+    idx = np.ascontiguousarray(scene.poly_indices, dtype=np.int32)
+    a = np.ascontiguousarray(scene.absorption, dtype=np.float64).reshape(-1)
+    s = np.ascontiguousarray(scene.scattering, dtype=np.float64).reshape(-1)
+    desc = _capi.SceneDesc(v.size // 3, dptr(v), offs.size - 1, iptr(offs), iptr(idx), dptr(a), dptr(s), None,
+                           scene.temp_c, scene.rel_humidity, scene.pressure_hpa, scene.air_choice,
+                           scene.edge_correction, 0, 0)
+    o = np.ascontiguousarray(origins, dtype=np.float64)
+    d = np.ascontiguousarray(dirs, dtype=np.float64)
+    n = o.shape[0]
+    poly = np.zeros(n, dtype=np.int32)
+    t = np.zeros(n)
+    check(_capi.lib().pach_scene_shoot_host(C.byref(desc), n, dptr(o), dptr(d), iptr(poly), dptr(t)))
+    return poly, t
 
 
 def emit_directions(seed, ray_begin, n, n_sources, kind):

@@ -34,15 +34,21 @@ def _shoebox(L, alpha=0.1):
     return rooms.SceneArrays(v, offs, idx, np.full((P, 8), alpha), np.zeros((P, 8)), np.zeros((P, 8)))
 
 
-def params_of(h, fs=1000, direct=None):
+def direct_times(w):
+    """Direct-sound arrival (s) at each receiver from the nearest source: the start time of the
+    C80 / D50 windows (Clarity / Definition startTime)."""
+    c = 331.0 + 0.6 * w.scene.temp_c
+    return [min(np.linalg.norm(np.subtract(r.origin, s.origin)) for s in w.sources) / c for r in w.receivers]
+
+
+def params_of(h, w, fs=1000):
     """T30/EDT/C80/D50 per receiver and band from raw energy histograms."""
     E = h["energy"]
+    direct = direct_times(w)
     out = {k: np.zeros(E.shape[:2]) for k in JND}
     for r in range(E.shape[0]):
         for o in range(E.shape[1]):
-            etc = E[r, o]
-            start = 0.0 if direct is None else direct[r]
-            p = room_parameters(etc, fs, start)
+            p = room_parameters(E[r, o], fs, direct[r])
             for k in JND:
                 out[k][r, o] = p[k]
     return out
@@ -52,7 +58,8 @@ def assert_params_close(pg, po, frac):
     for k, j in JND.items():
         a, b = pg[k], po[k]
         ok = np.isfinite(a) & np.isfinite(b)
-        assert ok.mean() > 0.9, k
+        assert ok.mean() > 0.8, (k, ok.mean())
+        assert np.array_equal(np.isfinite(a), np.isfinite(b)), k
         if k in ("T30", "EDT"):
             err = np.abs(a[ok] - b[ok]) / np.abs(b[ok])
         else:
@@ -133,7 +140,7 @@ def test_stochastic_shoebox_matches_oracle_with_shared_streams():
     np.testing.assert_allclose(hg["energy"].sum(axis=2), ho["energy"].sum(axis=2), rtol=5e-3)
     assert abs(sg["segments"] - so["segments"]) <= 5e-3 * so["segments"]
     assert abs(sg["octave_rays"] - so["octave_rays"]) <= 5e-3 * so["octave_rays"]
-    assert_params_close(params_of(hg), params_of(ho), 0.1)
+    assert_params_close(params_of(hg, w), params_of(ho, w), 0.1)
 
 
 def test_stochastic_hall_matches_oracle_within_jnd():
@@ -144,7 +151,7 @@ def test_stochastic_hall_matches_oracle_within_jnd():
     assert sg["fp64_retests"] > 0 and sg["queue_overflows"] == 0
     np.testing.assert_allclose(hg["energy"].sum(), ho["energy"].sum(), rtol=0.03)
     assert abs(sg["segments"] - so["segments"]) <= 0.03 * so["segments"]
-    assert_params_close(params_of(hg), params_of(ho), 1.0)
+    assert_params_close(params_of(hg, w), params_of(ho, w), 1.0)
 
 
 # ---------------------------------------------------------------- properties at size
@@ -216,7 +223,7 @@ def test_cancel_stops_between_chunks():
     w = rooms.irregular_hall_c2()
     ds = tracer.DeviceScene(w.scene)
     params = tracer.make_params(rays=2_000_000, cutoff_length_m=w.cutoff_length_m, hist_cotime_ms=3000.0, seed=1,
-                                queue_budget_items=1 << 20)
+                                feed_batch=1 << 14)
     run = tracer.Run(ds, w.sources, w.receivers, params)
     run.cancel()
     with pytest.raises(_capi.PachError) as ei:

@@ -99,6 +99,27 @@ def test_oracle_grid_equals_brute_force_in_irregular_hall():
             assert pg == pb and tg == pytest.approx(tb, rel=1e-12)
 
 
+@pytest.mark.parametrize("make", [lambda: rooms.shoebox_c1().scene,
+                                  lambda: rooms.irregular_hall_c2().scene,
+                                  lambda: rooms.batched_rooms_c3(n_rooms=3)[2].scene])
+def test_engine_bvh_finds_the_nearest_hit(make):
+    """The engine's BVH (built and walked on the host with the device's FP32 box tests) returns the
+    same nearest polygon as the oracle's brute force over every polygon."""
+    sc = make()
+    lo, hi = sc.bounds()
+    rng = np.random.default_rng(17)
+    n = 3000
+    o = rng.uniform(lo + 0.3 * (hi - lo), hi - 0.3 * (hi - lo), size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pe, te = tracer.shoot_host(sc, o, d)
+    for i in range(0, n, 10 if sc.n_polys > 5000 else 1):
+        pb, tb, _ = O.shoot(sc, o[i], d[i], brute_force=True)
+        assert pe[i] == pb, i
+        if pb >= 0:
+            assert te[i] == pytest.approx(tb, rel=1e-12)
+
+
 def test_oracle_trace_grid_and_brute_force_agree():
     w = rooms.shoebox_c1()
     h1, s1 = O.trace(w, rays=64, threads=4)
