@@ -47,7 +47,7 @@ class TraceParams(C.Structure):
                 ("max_segments_per_ray", C.c_int64), ("feed_batch", C.c_int64),
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("wave_kilo_items", C.c_int32), ("ring_log2", C.c_int32),
-                ("kernel_timing", C.c_int32), ("reserved", C.c_int32),
+                ("kernel_timing", C.c_int32), ("ray_sort", C.c_int32),
                 ("prim_dirs", _dp), ("prim_weights", _dp)]
 
 
@@ -65,6 +65,7 @@ class Stats(C.Structure):
                 ("h_oct", C.c_int32), ("bins", C.c_int32), ("cotime_s", C.c_double), ("sound_speed", C.c_double),
                 ("rho_c", C.c_double), ("air_atten_db_per_m", C.c_double * 8), ("device_ms", C.c_double),
                 ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("broadband_ms", C.c_double),
+                ("sort_ms", C.c_double),
                 ("waves", C.c_int64), ("kernel_launches", C.c_int64), ("peak_live_rays", C.c_int64),
                 ("bvh_nodes_visited", C.c_int64), ("tri_tests", C.c_int64),
                 ("wall_ms", C.c_double), ("accel", C.c_int32 * 3), ("reserved", C.c_int32)]

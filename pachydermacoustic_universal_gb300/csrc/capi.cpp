@@ -73,7 +73,7 @@ struct pach_run {
     double cotime = 0;
     unsigned long long max_broad = 0;
     // device buffers
-    DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw;
+    DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw, sortbins;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -91,7 +91,8 @@ struct pach_run {
             worker.join();
         }
         cudaSetDevice(scene ? scene->device : 0);
-        for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw})
+        for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
+                          &sortbins})
             m->release();
     }
 };
@@ -202,6 +203,13 @@ void run_worker(pach_run *run) {
         }
         TRY(run->qa.alloc(ring_cap * sizeof(ORayItem)));
         TRY(run->qs0.alloc(std::min(max_wave, ring_cap) * sizeof(int2)));
+        const bool sorting = run->p.ray_sort > 0;
+        if (sorting) {
+            TRY(run->qs1.alloc(std::min(max_wave, ring_cap) * sizeof(ORayItem)));
+            TRY(run->sortbins.alloc(2 * kSortBins * sizeof(unsigned)));
+            TRY(cudaMemsetAsync(run->sortbins.p, 0, run->sortbins.bytes, stream));
+        }
+        const int sort_blocks = dev_sms * 4;
 
         DevRun r{};
         r.S = sc->dev;
@@ -236,6 +244,13 @@ void run_worker(pach_run *run) {
         r.ring_cap = ring_cap;
         r.ctl = run->qctl.as<WaveCtl>();
         r.hits = run->qs0.as<int2>();
+        r.wave_buf = sorting ? run->qs1.as<ORayItem>() : nullptr;
+        r.bin_count = sorting ? run->sortbins.as<unsigned>() : nullptr;
+        r.bin_cursor = sorting ? run->sortbins.as<unsigned>() + kSortBins : nullptr;
+        for (int k = 0; k < 3; ++k) {
+            r.sort_lo[k] = (float)hs.bmin[k];
+            r.sort_inv[k] = (float)(kSortGrid / (hs.bmax[k] - hs.bmin[k]));
+        }
         r.max_wave = std::min(max_wave, ring_cap);
         r.feed_bound = bound;
         r.low_water = std::min(ring_cap / 4, 2 * r.max_wave);
@@ -252,7 +267,7 @@ void run_worker(pach_run *run) {
         h_ctl->prim_first = run->p.ray_begin;
         TRY(cudaMemcpyAsync(run->qctl.p, h_ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
         const bool timing = run->p.kernel_timing != 0;
-        double t_trace = 0, t_shade = 0, t_bb = 0;
+        double t_trace = 0, t_shade = 0, t_bb = 0, t_sort = 0;
         long long launches = 0;
         int batch = 8;
         bool cancelled = false;
@@ -274,8 +289,12 @@ void run_worker(pach_run *run) {
                 if (timing) TRY(cudaEventRecord(kev[6 * k + 1], stream));
                 TRY(launch_wave(r, stream));
                 if (timing) TRY(cudaEventRecord(kev[6 * k + 2], stream));
-                TRY(launch_trace(r, tr_variant, tr_blocks, threads, stream));
+                if (sorting) {
+                    TRY(launch_sort(r, sort_blocks, stream));
+                    launches += 3;
+                }
                 if (timing) TRY(cudaEventRecord(kev[6 * k + 3], stream));
+                TRY(launch_trace(r, tr_variant, tr_blocks, threads, stream));
                 if (timing) TRY(cudaEventRecord(kev[6 * k + 4], stream));
                 TRY(launch_shade(r, sh_blocks, threads, stream));
                 if (timing) TRY(cudaEventRecord(kev[6 * k + 5], stream));
@@ -287,11 +306,13 @@ void run_worker(pach_run *run) {
             TRY(cudaStreamSynchronize(stream));
             if (timing) {
                 for (int k = 0; k < batch; ++k) {
-                    float a = 0, b = 0, c = 0;
+                    float a = 0, b = 0, c = 0, so = 0;
                     TRY(cudaEventElapsedTime(&a, kev[6 * k], kev[6 * k + 1]));
-                    TRY(cudaEventElapsedTime(&b, kev[6 * k + 2], kev[6 * k + 3]));
+                    TRY(cudaEventElapsedTime(&so, kev[6 * k + 2], kev[6 * k + 3]));
+                    TRY(cudaEventElapsedTime(&b, kev[6 * k + 3], kev[6 * k + 4]));
                     TRY(cudaEventElapsedTime(&c, kev[6 * k + 4], kev[6 * k + 5]));
                     t_bb += a;
+                    t_sort += so;
                     t_trace += b;
                     t_shade += c;
                 }
@@ -352,6 +373,7 @@ void run_worker(pach_run *run) {
         s.trace_ms = t_trace;
         s.shade_ms = t_shade;
         s.broadband_ms = t_bb;
+        s.sort_ms = t_sort;
         s.waves = (int64_t)h_ctl->waves;
         s.kernel_launches = launches;
         s.peak_live_rays = (int64_t)h_ctl->peak_live;
@@ -382,7 +404,7 @@ void run_worker(pach_run *run) {
     if (h_cnt) cudaFreeHost(h_cnt);
     if (stream) cudaStreamDestroy(stream);
     // release the ring; histograms and counters stay until the run is destroyed
-    for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw}) m->release();
+    for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw, &run->sortbins}) m->release();
     if (e != cudaSuccess) return finish(PACH_ERR_CUDA, cuda_msg(e, where.c_str()), PACH_RUN_FAILED);
     finish(status, msg, final_state);
 }

@@ -121,7 +121,15 @@ struct DevRun {
     long long feed_batch;          // primaries per phase-A launch at most
     unsigned long long feed_bound; // ring slots one primary can fill in phase A
     unsigned long long low_water;  // feed new primaries when fewer live items remain
+    // per-wave ray order (counting sort by direction octant and origin cell)
+    ORayItem *wave_buf;            // the wave, sorted (null: trace and shade read the ring in place)
+    unsigned *bin_count;           // [kSortBins], zero between waves
+    unsigned *bin_cursor;          // [kSortBins]
+    float sort_lo[3], sort_inv[3]; // origin grid: cell = (p - lo) * inv, 0..kSortGrid-1 per axis
 };
+
+constexpr int kSortGrid = 8;                       // origin cells per axis
+constexpr int kSortBins = 8 * kSortGrid * kSortGrid * kSortGrid;  // x 8 direction octants
 
 // trace.cu entry points (host wrappers).  One wavefront iteration:
 //   feed (1 thread) -> broadband (phase A of the fed primaries) -> wave (1 thread: size the wave)
@@ -129,6 +137,7 @@ struct DevRun {
 cudaError_t launch_feed(const DevRun &r, cudaStream_t s);
 cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s);
+cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count -> scan -> scatter
 // variant: 256-thread blocks per SM the trace kernel is compiled for (3..6; others -> 4)
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s);

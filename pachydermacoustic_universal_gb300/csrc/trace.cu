@@ -33,6 +33,11 @@ __device__ __forceinline__ void ring_store(const DevRun &r, unsigned long long i
     store_item(r.ring, i & (r.ring_cap - 1), it);
 }
 
+// Item j of the current wave: the sorted copy when the wave was sorted, else the ring in place.
+__device__ __forceinline__ const ORayItem *wave_item(const DevRun &r, unsigned long long head, unsigned long long j) {
+    return r.wave_buf ? r.wave_buf + j : r.ring + ((head + j) & (r.ring_cap - 1));
+}
+
 // All 32 lanes call: lane gets the first of its n ring slots; one atomic per warp.
 __device__ __forceinline__ unsigned long long warp_append(unsigned long long *tail, int n) {
     const int lane = threadIdx.x & 31;
@@ -222,6 +227,98 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
 }
 
 // ------------------------------------------------------------------------------------------
+// wave ordering: counting sort by (direction octant, Morton code of the origin cell) so that the
+// rays of a warp start close together heading the same way and walk similar BVH paths
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned spread3(unsigned x) {  // 3 bits -> every third bit
+    return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4);
+}
+
+__device__ __forceinline__ unsigned sort_key(const DevRun &r, float4 P, float4 D) {
+    const int cx = min(max((int)((P.x - r.sort_lo[0]) * r.sort_inv[0]), 0), kSortGrid - 1);
+    const int cy = min(max((int)((P.y - r.sort_lo[1]) * r.sort_inv[1]), 0), kSortGrid - 1);
+    const int cz = min(max((int)((P.z - r.sort_lo[2]) * r.sort_inv[2]), 0), kSortGrid - 1);
+    const unsigned morton = spread3((unsigned)cx) | (spread3((unsigned)cy) << 1) | (spread3((unsigned)cz) << 2);
+    const unsigned oct = (D.x < 0.f ? 1u : 0u) | (D.y < 0.f ? 2u : 0u) | (D.z < 0.f ? 4u : 0u);
+    return (oct << 9) | morton;
+}
+
+__global__ void __launch_bounds__(256) k_sort_count(DevRun r) {
+    __shared__ unsigned h[kSortBins];
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const unsigned long long m = r.ctl->m, head = r.ctl->head;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += stride) {
+        const float4 *q = reinterpret_cast<const float4 *>(r.ring + ((head + j) & (r.ring_cap - 1)));
+        atomicAdd(&h[sort_key(r, __ldg(q), __ldg(q + 1))], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&r.bin_count[i], h[i]);
+}
+
+// One block of 1024 threads, 4 bins each: exclusive scan into the cursors; clears the counts.
+__global__ void __launch_bounds__(1024) k_sort_scan(DevRun r) {
+    __shared__ unsigned warp_sum[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned c[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        c[k] = r.bin_count[4 * t + k];
+        r.bin_count[4 * t + k] = 0;
+        s += c[k];
+    }
+    unsigned incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = warp_sum[lane], wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(FULL, wi, o);
+            if (lane >= o) wi += v;
+        }
+        warp_sum[lane] = wi - w;  // exclusive warp offsets
+    }
+    __syncthreads();
+    unsigned run = warp_sum[warp] + incl - s;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        r.bin_cursor[4 * t + k] = run;
+        run += c[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(DevRun r) {
+    const unsigned long long m = r.ctl->m, head = r.ctl->head;
+    const unsigned long long m32 = (m + 31) & ~31ull;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ull;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = warp0; base < m32; base += stride) {
+        const unsigned long long j = base + lane;
+        const bool act = j < m;
+        const unsigned amask = __ballot_sync(FULL, act);
+        if (!act) continue;
+        const ORayItem it = load_item(r.ring, (head + j) & (r.ring_cap - 1));
+        const float4 *f = reinterpret_cast<const float4 *>(&it);
+        const unsigned key = sort_key(r, f[0], f[1]);
+        const unsigned peers = __match_any_sync(amask, key);
+        const int leader = __ffs(peers) - 1;
+        unsigned pos = 0;
+        if (lane == leader) pos = atomicAdd(&r.bin_cursor[key], (unsigned)__popc(peers));
+        pos = __shfl_sync(amask, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+        store_item(r.wave_buf, pos, it);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // phases B and C, split into the BVH walk and the surface interaction
 // ------------------------------------------------------------------------------------------
 // Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
@@ -250,7 +347,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             if (!have && !exhausted) {
                 j = base + __popc(need & ((1u << lane) - 1u));
                 if (j < m) {
-                    const float4 *q = reinterpret_cast<const float4 *>(r.ring + ((head + j) & (r.ring_cap - 1)));
+                    const float4 *q = reinterpret_cast<const float4 *>(wave_item(r, head, j));
                     const float4 P = __ldcs(q), D = __ldcs(q + 1), X = __ldcs(q + 3);
                     o = f3(P);
                     d = f3(D);
@@ -324,7 +421,7 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
         int nout = 0;
         Ray R, C;
         if (j < m) {
-            R = to_ray(ring_load(r, head + j));
+            R = to_ray(load_item(wave_item(r, head, j), 0));
             const int2 h = r.hits[j];
             const bool hit = h.x >= 0;
             const float t = __int_as_float(h.y);
@@ -459,6 +556,13 @@ cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStrea
 
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s) {
     k_wave<<<1, 32, 0, s>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s) {
+    k_sort_count<<<blocks, 256, 0, s>>>(r);
+    k_sort_scan<<<1, 1024, 0, s>>>(r);
+    k_sort_scatter<<<blocks, 256, 0, s>>>(r);
     return cudaGetLastError();
 }
 

@@ -71,7 +71,7 @@ def receiver_array(receivers):
 def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 7), is_order=-1, sample_rate=1000,
                 pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
                 block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
-                ring_log2=0, kernel_timing=False):
+                ring_log2=0, kernel_timing=False, ray_sort=0):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -90,6 +90,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.wave_kilo_items = int(wave_kilo_items)
     p.ring_log2 = int(ring_log2)
     p.kernel_timing = int(bool(kernel_timing))
+    p.ray_sort = int(ray_sort)
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
     return p
