@@ -199,6 +199,24 @@ pach_status pach_trace_run(pach_scene *scene, const pach_source_desc *sources, i
                            const pach_trace_params *params, int32_t scaled, double *energy, double *pressure,
                            double *dir_pos, double *dir_neg, double *analysis, size_t cap_bins, pach_stats *stats);
 
+/* No counterpart in the reference.  The tracer for callers that must not allocate device memory at
+ * trace time -- a host tracing from an audio or plug-in processing callback, or code whose device
+ * memory belongs to another framework's allocator: it creates the scene at set-up, then calls this
+ * per run with its own device buffers (energy/pressure R*8*T doubles, dir_pos/dir_neg/analysis
+ * R*24*T doubles; all five required; cleared by the call).  The call allocates nothing: its working
+ * memory is a fixed ~4.6 MB device array inside the library, resident on every GPU that loads the
+ * library until the process exits.  Limits: 16 sources, 256 receivers, 65536 octave rays in flight
+ * (a scene whose phase-A bound or split trees need more is rejected with PACH_ERR_INVALID_ARGUMENT
+ * or PACH_ERR_BOUNDS), no emission overrides.  The scene's device must be current.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress): make that first call before
+ * any stream capture.  Runs on `stream` (a cudaStream_t, NULL = default stream) and returns when done.
+ * Every call shares the one array, so calls that overlap on the GPU (other threads or streams) race. */
+pach_status pach_trace_run_noalloc(const pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
+                                   const pach_receiver_desc *receivers, int32_t n_receivers,
+                                   const pach_trace_params *params, void *stream, double *d_energy,
+                                   double *d_pressure, double *d_dir_pos, double *d_dir_neg, double *d_analysis,
+                                   pach_stats *stats);
+
 /* Pure-specular paths (oracle (a)): per bounce the hit polygon (-1 = miss), leg length and hit
  * point, traced by the same device traversal as the tracer. */
 pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double *origins, const double *dirs,

@@ -82,7 +82,7 @@ class Stats(C.Structure):
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
            "pach_scene_info", "pach_trace_begin", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
-           "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
+           "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
            "pach_math_strength", "pach_math_sound_speed"]
 
@@ -113,6 +113,8 @@ def _declare(L):
         "pach_trace_run": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
                                      C.POINTER(TraceParams), C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_size_t,
                                      C.POINTER(Stats)]),
+        "pach_trace_run_noalloc": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
+                                             C.POINTER(TraceParams), vp, vp, vp, vp, vp, vp, C.POINTER(Stats)]),
         "pach_trace_specular_paths": (C.c_int, [vp, C.c_int32, _dp, _dp, C.c_int32, _ip, _dp, _dp]),
         "pach_scene_shoot_host": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, _dp, _dp, _ip, _dp]),
         "pach_emit_directions": (C.c_int, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _dp]),

@@ -763,3 +763,11 @@ pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, in
 }
 
 }  // extern "C"
+
+// Read access to scene handles for entry points defined in other translation units.
+namespace pach {
+const HostScene *scene_host(const pach_scene *s) { return s ? &s->hs : nullptr; }
+const DevScene *scene_dev(const pach_scene *s) { return s ? &s->dev : nullptr; }
+int scene_device(const pach_scene *s) { return s ? s->device : -1; }
+void set_last_error(const char *msg) { g_err = msg; }
+}  // namespace pach

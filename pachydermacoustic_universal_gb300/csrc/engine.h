@@ -146,11 +146,18 @@ cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double
                          double *t, double *pts, cudaStream_t s);
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s);
 
+// capi.cpp: read access to a scene handle (for entry points in other translation units)
+const HostScene *scene_host(const pach_scene *s);
+const DevScene *scene_dev(const pach_scene *s);
+int scene_device(const pach_scene *s);
+void set_last_error(const char *msg);
+
 // scene.cpp
 bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err);
 void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, int edge, double atten[kBands],
                        double *c, double *rho);
 void geodesic_faces(std::vector<double> &faces);  // [80][3][3]
+void geodesic_faces_fixed(double out[kGeoFaces * 9]);
 unsigned long long derived_broadband_bound(const HostScene &hs, int h_oct, bool pure_specular);
 // Host walk of hs.bvh with the device's box test and FP64 triangle tests (t > t_min).
 bool bvh_shoot_host(const HostScene &hs, const double o[3], const double d[3], double t_min, int &tri, double &t);

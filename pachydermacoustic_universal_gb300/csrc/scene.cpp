@@ -314,6 +314,31 @@ void geodesic_faces(std::vector<double> &out) {
     }
 }
 
+// The same 80 faces into a caller-owned array (no heap use).
+void geodesic_faces_fixed(double out[kGeoFaces * 9]) {
+    const double s5 = std::sqrt(5.0), phi = (1.0 + s5) * 0.5;
+    const double ratio = std::sqrt(10.0 + 2.0 * s5) / (4.0 * phi);
+    const double a = (.25 / ratio) * 0.5, b = (.25 / ratio) / (2.0 * phi);
+    D3 P[12] = {{0, b, -a}, {b, a, 0}, {-b, a, 0}, {0, b, a}, {0, -b, a}, {-a, 0, b},
+                {0, -b, -a}, {a, 0, -b}, {a, 0, b}, {-a, 0, -b}, {b, -a, 0}, {-b, -a, 0}};
+    for (auto &p : P) p = unit(p);
+    static const int T[20][3] = {{0, 1, 2}, {3, 2, 1}, {3, 4, 5}, {3, 8, 4}, {0, 6, 7}, {0, 9, 6}, {4, 10, 11},
+                                 {6, 11, 10}, {2, 5, 9}, {11, 9, 5}, {1, 7, 8}, {10, 8, 7}, {3, 5, 2}, {3, 1, 8},
+                                 {0, 2, 9}, {0, 7, 1}, {6, 9, 11}, {6, 10, 7}, {4, 11, 5}, {4, 8, 10}};
+    int n = 0;
+    auto put = [&](D3 x, D3 y, D3 z) {
+        for (D3 v : {x, y, z}) { out[n++] = v.x; out[n++] = v.y; out[n++] = v.z; }
+    };
+    for (auto &t : T) {
+        D3 p0 = P[t[0]], p1 = P[t[1]], p2 = P[t[2]];
+        D3 p3 = unit(mul(add(p0, p1), 0.5)), p4 = unit(mul(add(p1, p2), 0.5)), p5 = unit(mul(add(p2, p0), 0.5));
+        put(p0, p3, p5);
+        put(p1, p4, p3);
+        put(p2, p5, p4);
+        put(p3, p4, p5);
+    }
+}
+
 // Phase A ends when E[h_oct] <= 1e-2 E0 (TaskAll:351, 417); each broadband bounce multiplies
 // E[h_oct] by at most max over surfaces of (1-alpha)(1-s)(1-tau), which bounds the bounce count.
 unsigned long long derived_broadband_bound(const HostScene &hs, int h, bool pure) {
