@@ -72,7 +72,7 @@ typedef struct {
     double pressure_hpa;           /* hPa, as the Scene ctor (1013.25 = 101.325 kPa) */
     int32_t air_choice;            /* 0 ISO 9613-1, 1 Evans-Bazley, 2 tables */
     int32_t edge_correction;
-    int32_t reserved0;
+    int32_t bvh_leaf_max;          /* triangles per BVH leaf at most (1..8); 0 = default (4) */
     int32_t reserved1;
 } pach_scene_desc;
 
@@ -110,6 +110,10 @@ typedef struct {
     int32_t ray_sort;              /* 1: order each wave by (direction octant, origin cell) before tracing;
                                       0 = default (off: measured +6 % walk rate in the 20k-triangle
                                       hall, less than the sort costs) */
+    int32_t traversal;             /* BVH walk of the trace kernel: 0 = default, 1 = one leaf at a time,
+                                      2 = speculative (lanes holding a leaf keep descending until the
+                                      whole warp holds one, then the warp tests its leaves together) */
+    int32_t reserved_p;            /* 0 */
     const double *prim_dirs;       /* optional [ray_count][3] emission directions (importance sampling) */
     const double *prim_weights;    /* optional [ray_count] emission weights (1/q) */
 } pach_trace_params;

@@ -28,7 +28,7 @@ class SceneDesc(C.Structure):
     _fields_ = [("n_vertices", C.c_int32), ("vertices", _dp), ("n_polys", C.c_int32), ("poly_offsets", _ip),
                 ("poly_indices", _ip), ("absorption", _dp), ("scattering", _dp), ("transmission", _dp),
                 ("temp_c", C.c_double), ("rel_humidity", C.c_double), ("pressure_hpa", C.c_double),
-                ("air_choice", C.c_int32), ("edge_correction", C.c_int32), ("reserved0", C.c_int32),
+                ("air_choice", C.c_int32), ("edge_correction", C.c_int32), ("bvh_leaf_max", C.c_int32),
                 ("reserved1", C.c_int32)]
 
 
@@ -48,6 +48,7 @@ class TraceParams(C.Structure):
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("wave_kilo_items", C.c_int32), ("ring_log2", C.c_int32),
                 ("kernel_timing", C.c_int32), ("ray_sort", C.c_int32),
+                ("traversal", C.c_int32), ("reserved_p", C.c_int32),
                 ("prim_dirs", _dp), ("prim_weights", _dp)]
 
 

@@ -183,7 +183,7 @@ void run_worker(pach_run *run) {
         const int threads = run->p.block_threads > 0 ? std::max(32, std::min(256, run->p.block_threads / 32 * 32)) : 256;
         int bps_tr = 0, bps_sh = 0;
         // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
-        const int tr_variant = run->p.blocks_per_sm > 0 ? run->p.blocks_per_sm : 4;
+        const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, (int)hs.tri_poly.size());
         TRY(wave_kernel_occupancy(tr_variant, threads, (int)sizeof(float4) * std::max(R, 1), &bps_tr, &bps_sh));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
@@ -547,6 +547,7 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
                     "ray_count must be >= 1 and ray_begin + ray_count <= 2^32 (convergence mode is not supported)");
     if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi) return fail(PACH_ERR_INVALID_ARGUMENT, "octave range must lie in 0..7");
     if (p.sample_rate < 1) return fail(PACH_ERR_INVALID_ARGUMENT, "sample_rate must be positive");
+    if (p.traversal < 0 || p.traversal > 2) return fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
     if (!(p.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, "cutoff_length_m must be positive");
     const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
     if (T < 1 || T > (1ll << 24)) return fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");

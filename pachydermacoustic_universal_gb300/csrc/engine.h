@@ -37,7 +37,8 @@ struct HostScene {
 
 constexpr int kBvhStack = 64;
 constexpr int kBvhNodeFloats = 32;
-constexpr int kLeafMax = 8;
+constexpr int kLeafMax = 8;      // largest leaf the node encoding holds
+constexpr int kLeafDefault = 4;  // leaf size used when the scene does not ask for one
 
 // Device scene view (passed by value to kernels).
 struct DevScene {
@@ -138,7 +139,17 @@ cudaError_t launch_feed(const DevRun &r, cudaStream_t s);
 cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s);
 cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count -> scan -> scatter
-// variant: 256-thread blocks per SM the trace kernel is compiled for (3..6; others -> 4)
+// variant: 256-thread blocks per SM the trace kernel is compiled for (3..6; others -> 4), plus 16 for the
+// speculative BVH walk (compiled for 4 and 6 blocks per SM).  traversal 0 picks the speculative walk for
+// scenes of more than kSpecMinTris triangles: measured on a 20k-triangle hall it walks 1.5x faster than
+// one leaf at a time, while on a 12-triangle shoebox (a two-level tree) it is 10 % slower.
+constexpr int kSpecMinTris = 64;
+inline int trace_variant(int blocks_per_sm, int traversal, int ntri) {
+    const int minb = blocks_per_sm > 0 ? blocks_per_sm : 4;
+    const bool spec = traversal == 2 || (traversal == 0 && ntri > kSpecMinTris);
+    if (spec) return 16 + (minb >= 6 ? 6 : 4);
+    return minb;
+}
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s);
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);

@@ -72,6 +72,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "bad octave range, sample rate or cutoff");
     const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
     if (T < 1 || T > (1ll << 24)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");
+    if (p.traversal < 0 || p.traversal > 2) return na_fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
     for (int i = 0; i < n_receivers; ++i)
         if (!(receivers[i].radius > 0)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "receiver radius must be positive");
     for (int s = 0; s < n_sources; ++s)
@@ -205,7 +206,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
 
         int sms = 0, bps_tr = 0, bps_sh = 0;
         NA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        const int variant = p.blocks_per_sm > 0 ? p.blocks_per_sm : 4;
+        const int variant = trace_variant(p.blocks_per_sm, p.traversal, (int)hs.tri_poly.size());
         NA_TRY(wave_kernel_occupancy(variant, 256, (int)sizeof(float4) * (n_receivers > 0 ? n_receivers : 1), &bps_tr,
                                      &bps_sh));
         const int tr_blocks = sms * (bps_tr > 0 ? bps_tr : 1), sh_blocks = sms * (bps_sh > 0 ? bps_sh : 1);

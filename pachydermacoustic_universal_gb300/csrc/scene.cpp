@@ -35,6 +35,7 @@ struct BvhBuilder {
     std::vector<BNode> nodes;
     std::vector<int> order;
     int max_depth = 0, leaves = 0;
+    int leaf_max = kLeafMax;
 
     static double area(const double lo[3], const double hi[3]) {
         double e0 = std::max(0.0, hi[0] - lo[0]), e1 = std::max(0.0, hi[1] - lo[1]), e2 = std::max(0.0, hi[2] - lo[2]);
@@ -62,7 +63,7 @@ struct BvhBuilder {
         max_depth = std::max(max_depth, depth);
         const int n = e - b;
         if (n <= 2 || depth >= 56) {
-            if (n <= kLeafMax) return make_leaf(b, e);
+            if (n <= leaf_max) return make_leaf(b, e);
         }
         double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
         for (int i = b; i < e; ++i)
@@ -106,7 +107,7 @@ struct BvhBuilder {
                 if (cost < best) { best = cost; best_axis = ax; best_split = q; }
             }
         }
-        if (n <= kLeafMax && (best_axis < 0 || best >= (double)n)) return make_leaf(b, e);
+        if (n <= leaf_max && (best_axis < 0 || best >= (double)n)) return make_leaf(b, e);
         int mid;
         if (best_axis < 0) {
             mid = b + n / 2;  // coincident centroids: split the list
@@ -132,8 +133,9 @@ struct BvhBuilder {
 };
 
 // Builds hs.bvh and reorders the triangle arrays into leaf order.
-void build_bvh(HostScene &hs) {
+void build_bvh(HostScene &hs, int leaf_max) {
     BvhBuilder B;
+    B.leaf_max = (leaf_max >= 1 && leaf_max <= kLeafMax) ? leaf_max : kLeafDefault;
     B.t.resize(hs.ntri);
     for (int i = 0; i < hs.ntri; ++i) {
         const double *q = &hs.tri64[9 * (size_t)i];
@@ -507,7 +509,7 @@ bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err)
         hs.tri_plane[i] = it->second;
     }
 
-    build_bvh(hs);
+    build_bvh(hs, d->bvh_leaf_max);
 
     medium_properties(d->temp_c, d->rel_humidity, d->pressure_hpa, d->air_choice, d->edge_correction, hs.atten,
                       &hs.c, &hs.rho);

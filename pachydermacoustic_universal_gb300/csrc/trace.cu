@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(DevRun r) {
 // Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
 // its next leaf and tests it; a lane whose walk has ended writes its hit and takes the next wave
 // item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
-template <int MINB>
+template <int MINB, bool SPEC>
 __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     WaveCtl *c = r.ctl;
     const unsigned long long m = c->m, head = c->head;
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     unsigned long long j = 0;
     float3 o = make_float3(0.f, 0.f, 0.f), d = o;
     float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f, best = FLT_MAX;
-    int skip = -1, node = 0, sp = 0, bi = -1;
+    int skip = -1, node = 0, sp = 0, bi = -1, leaf = 0;
     int stack[kBvhStack];
     for (;;) {
         const unsigned need = __ballot_sync(FULL, !have && !exhausted);
@@ -365,29 +365,63 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             }
         }
         if (!__any_sync(FULL, have)) break;
-        if (!have) continue;
-        bool fin = false;
-        while (node >= 0) {
-            ++w.nodes;
-            int next;
-            if (!bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) {
-                if (sp == 0) { fin = true; break; }
-                node = stack[--sp];
-                continue;
+        if constexpr (SPEC) {
+            // Speculative walk: a lane that has found a leaf keeps descending inner nodes while any
+            // lane of the warp is still looking for its first leaf; then the warp tests its leaves
+            // together.  node: >= 0 inner node, < 0 leaf, kEmptyChild nothing left; leaf: 0 none.
+            if (have && node < 0 && node != kEmptyChild && leaf == 0) {
+                leaf = node;
+                node = sp ? stack[--sp] : kEmptyChild;
             }
-            node = next;
-        }
-        if (!fin) {
-            const int code = ~node;
-            const int f0 = code >> 4, cnt = (code & 15) + 1;
-            w.tris += (unsigned)cnt;
-            for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
-            if (sp == 0) fin = true;
-            else node = stack[--sp];
-        }
-        if (fin) {
-            r.hits[j] = make_int2(bi, __float_as_int(best));
-            have = false;
+            for (;;) {
+                if (!__any_sync(FULL, have && node >= 0 && leaf == 0)) break;
+                if (have && node >= 0) {
+                    ++w.nodes;
+                    int next;
+                    if (bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) node = next;
+                    else node = sp ? stack[--sp] : kEmptyChild;
+                    if (node < 0 && node != kEmptyChild && leaf == 0) {
+                        leaf = node;
+                        node = sp ? stack[--sp] : kEmptyChild;
+                    }
+                }
+            }
+            if (have && leaf != 0) {
+                const int code = ~leaf;
+                const int f0 = code >> 4, cnt = (code & 15) + 1;
+                w.tris += (unsigned)cnt;
+                for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+                leaf = 0;
+            }
+            if (have && node == kEmptyChild) {
+                r.hits[j] = make_int2(bi, __float_as_int(best));
+                have = false;
+            }
+        } else {
+            if (!have) continue;
+            bool fin = false;
+            while (node >= 0) {
+                ++w.nodes;
+                int next;
+                if (!bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) {
+                    if (sp == 0) { fin = true; break; }
+                    node = stack[--sp];
+                    continue;
+                }
+                node = next;
+            }
+            if (!fin) {
+                const int code = ~node;
+                const int f0 = code >> 4, cnt = (code & 15) + 1;
+                w.tris += (unsigned)cnt;
+                for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+                if (sp == 0) fin = true;
+                else node = stack[--sp];
+            }
+            if (fin) {
+                r.hits[j] = make_int2(bi, __float_as_int(best));
+                have = false;
+            }
         }
     }
     // one atomic per warp for each counter
@@ -568,10 +602,12 @@ cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s) {
 
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s) {
     switch (variant) {
-        case 3: k_trace<3><<<blocks, threads, 0, s>>>(r); break;
-        case 5: k_trace<5><<<blocks, threads, 0, s>>>(r); break;
-        case 6: k_trace<6><<<blocks, threads, 0, s>>>(r); break;
-        default: k_trace<4><<<blocks, threads, 0, s>>>(r); break;
+        case 3: k_trace<3, false><<<blocks, threads, 0, s>>>(r); break;
+        case 5: k_trace<5, false><<<blocks, threads, 0, s>>>(r); break;
+        case 6: k_trace<6, false><<<blocks, threads, 0, s>>>(r); break;
+        case 16 + 4: k_trace<4, true><<<blocks, threads, 0, s>>>(r); break;
+        case 16 + 6: k_trace<6, true><<<blocks, threads, 0, s>>>(r); break;
+        default: k_trace<4, false><<<blocks, threads, 0, s>>>(r); break;
     }
     return cudaGetLastError();
 }
@@ -584,10 +620,12 @@ cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t 
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade) {
     cudaError_t e;
     switch (variant) {
-        case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<3>, threads, 0); break;
-        case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<5>, threads, 0); break;
-        case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<6>, threads, 0); break;
-        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4>, threads, 0); break;
+        case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<3, false>, threads, 0); break;
+        case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<5, false>, threads, 0); break;
+        case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<6, false>, threads, 0); break;
+        case 16 + 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, true>, threads, 0); break;
+        case 16 + 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<6, true>, threads, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false>, threads, 0); break;
     }
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade, threads, smem_shade);

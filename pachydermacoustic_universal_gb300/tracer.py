@@ -12,7 +12,7 @@ from ._capi import check, dptr, iptr
 class DeviceScene:
     """A scene resident on the GPU (pach_scene_create)."""
 
-    def __init__(self, scene):
+    def __init__(self, scene, bvh_leaf_max: int = 0):
         L = _capi.lib()
         self._v = np.ascontiguousarray(scene.vertices, dtype=np.float64).reshape(-1)
         self._o = np.ascontiguousarray(scene.poly_offsets, dtype=np.int32)
@@ -23,7 +23,7 @@ class DeviceScene:
         self._t = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1) if tr is not None else None
         desc = _capi.SceneDesc(self._v.size // 3, dptr(self._v), self._o.size - 1, iptr(self._o), iptr(self._i),
                                dptr(self._a), dptr(self._s), dptr(self._t), scene.temp_c, scene.rel_humidity,
-                               scene.pressure_hpa, scene.air_choice, scene.edge_correction, 0, 0)
+                               scene.pressure_hpa, scene.air_choice, scene.edge_correction, int(bvh_leaf_max), 0)
         h = C.c_void_p()
         check(L.pach_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
@@ -71,7 +71,7 @@ def receiver_array(receivers):
 def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 7), is_order=-1, sample_rate=1000,
                 pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
                 block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
-                ring_log2=0, kernel_timing=False, ray_sort=0):
+                ring_log2=0, kernel_timing=False, ray_sort=0, traversal=0):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -91,6 +91,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.ring_log2 = int(ring_log2)
     p.kernel_timing = int(bool(kernel_timing))
     p.ray_sort = int(ray_sort)
+    p.traversal = int(traversal)
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
     return p
