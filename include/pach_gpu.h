@@ -113,9 +113,15 @@ typedef struct {
     int32_t traversal;             /* BVH walk of the trace kernel: 0 = default, 1 = one leaf at a time,
                                       2 = speculative (lanes holding a leaf keep descending until the
                                       whole warp holds one, then the warp tests its leaves together) */
-    int32_t reserved_p;            /* 0 */
+    int32_t capture;               /* 1: record energy per receiver, time window and emission-direction
+                                      bin (pach_trace_get_capture, pach_proposal.h) */
     const double *prim_dirs;       /* optional [ray_count][3] emission directions (importance sampling) */
     const double *prim_weights;    /* optional [ray_count] emission weights (1/q) */
+    const float *proposal;         /* optional [n_proposal][160] learned-proposal lobes (pach_proposal.h) */
+    int32_t n_proposal;
+    int32_t reserved_q;            /* 0 */
+    double proposal_mix;           /* weight of uniform emission in the proposal, (0, 1]; 0 = 0.3 */
+    double capture_edges_ms[3];    /* capture windows, ms after the direct arrival; zeros = 80, 400, 1200 */
 } pach_trace_params;
 
 typedef struct {

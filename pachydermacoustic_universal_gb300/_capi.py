@@ -1,4 +1,4 @@
-"""ctypes binding of libpach_gpu.so (include/pach_gpu.h).
+"""ctypes binding of libpach_gpu.so (include/pach_gpu.h, include/pach_proposal.h).
 
 The library is the product: there is no CPU fallback.  Loading fails loudly when the shared library
 is missing and cannot be built, and every tracing entry point fails with PACH_ERR_NO_DEVICE when no
@@ -20,8 +20,12 @@ STATUS = {0: "PACH_OK", 1: "PACH_ERR_INVALID_ARGUMENT", 2: "PACH_ERR_OUT_OF_MEMO
           8: "PACH_ERR_NO_DEVICE", 9: "PACH_ERR_GAVE_UP"}
 RUN_STATE = {0: "RUNNING", 1: "STOPPED", 2: "FAILED", 3: "CANCELLED"}
 
+MLP_IN, MLP_HIDDEN, MLP_LOBES, MLP_OUT = 12, 256, 32, 160   # include/pach_proposal.h
+DIR_BINS, CAPTURE_WINDOWS = 1536, 4
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
+_fp = C.POINTER(C.c_float)
 
 
 class SceneDesc(C.Structure):
@@ -48,8 +52,10 @@ class TraceParams(C.Structure):
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("wave_kilo_items", C.c_int32), ("ring_log2", C.c_int32),
                 ("kernel_timing", C.c_int32), ("ray_sort", C.c_int32),
-                ("traversal", C.c_int32), ("reserved_p", C.c_int32),
-                ("prim_dirs", _dp), ("prim_weights", _dp)]
+                ("traversal", C.c_int32), ("capture", C.c_int32),
+                ("prim_dirs", _dp), ("prim_weights", _dp),
+                ("proposal", C.POINTER(C.c_float)), ("n_proposal", C.c_int32), ("reserved_q", C.c_int32),
+                ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3)]
 
 
 class Progress(C.Structure):
@@ -85,7 +91,11 @@ EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_c
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
-           "pach_math_strength", "pach_math_sound_speed"]
+           "pach_math_strength", "pach_math_sound_speed",
+           # include/pach_proposal.h
+           "pach_mlp_param_count", "pach_mlp_create", "pach_mlp_destroy", "pach_mlp_get_params", "pach_mlp_set_params",
+           "pach_mlp_set_data", "pach_mlp_loss_grad", "pach_mlp_train", "pach_mlp_forward", "pach_mlp_gemm",
+           "pach_direction_bins", "pach_direction_bin", "pach_proposal_sample", "pach_trace_get_capture"]
 
 
 class PachError(RuntimeError):
@@ -128,6 +138,20 @@ def _declare(L):
         "pach_math_center_time": (C.c_double, [_dp, C.c_int32, C.c_int32, C.c_double, C.c_int32]),
         "pach_math_strength": (C.c_double, [_dp, C.c_int32, C.c_double, C.c_int32]),
         "pach_math_sound_speed": (C.c_double, [C.c_double]),
+        "pach_mlp_param_count": (C.c_int64, []),
+        "pach_mlp_create": (C.c_int, [C.c_uint64, C.c_int32, C.POINTER(vp)]),
+        "pach_mlp_destroy": (None, [vp]),
+        "pach_mlp_get_params": (C.c_int, [vp, _fp, C.c_int64]),
+        "pach_mlp_set_params": (C.c_int, [vp, _fp, C.c_int64]),
+        "pach_mlp_set_data": (C.c_int, [vp, _fp, _fp, C.c_int32]),
+        "pach_mlp_loss_grad": (C.c_int, [vp, _fp, _fp]),
+        "pach_mlp_train": (C.c_int, [vp, C.c_int32, C.c_float, C.c_float, _fp]),
+        "pach_mlp_forward": (C.c_int, [vp, _fp, C.c_int32, _fp]),
+        "pach_mlp_gemm": (C.c_int, [_fp, _fp, C.c_int32, C.c_int32, C.c_int32, _fp]),
+        "pach_direction_bins": (C.c_int, [_fp, _fp, C.c_int32]),
+        "pach_direction_bin": (C.c_int32, [C.c_double, C.c_double, C.c_double]),
+        "pach_proposal_sample": (C.c_int, [_fp, C.c_int32, C.c_double, C.c_uint64, C.c_int64, C.c_int32, _fp, _fp]),
+        "pach_trace_get_capture": (C.c_int, [vp, _fp, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -167,6 +191,10 @@ def dptr(a):
 
 def iptr(a):
     return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def fptr(a):
+    return a.ctypes.data_as(_fp) if a is not None else None
 
 
 def device_count() -> int:

@@ -48,7 +48,8 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc=None) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     cu, cpp = sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(os.path.dirname(HERE), "include", "pach_gpu.h"))
+    inc_dir = os.path.join(os.path.dirname(HERE), "include")
+    headers += [os.path.join(inc_dir, f) for f in os.listdir(inc_dir) if f.endswith(".h")]
     jobs = []
     objs = []
     for f in cu:

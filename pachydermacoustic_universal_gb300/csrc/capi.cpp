@@ -69,11 +69,12 @@ struct pach_run {
     std::vector<pach_source_desc> src;
     std::vector<pach_receiver_desc> rec;
     std::vector<double> prim_dirs, prim_weights;
+    std::vector<float> prop;  // learned-proposal lobe table ([n_proposal][kLobes][8])
     int R = 0, T = 0, nsrc = 0, h_oct = 0;
     double cotime = 0;
     unsigned long long max_broad = 0;
     // device buffers
-    DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw, sortbins;
+    DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw, sortbins, dprop, dcap;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -92,7 +93,7 @@ struct pach_run {
         }
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
-                          &sortbins})
+                          &sortbins, &dprop, &dcap})
             m->release();
     }
 };
@@ -176,6 +177,11 @@ void run_worker(pach_run *run) {
         TRY(upload(run->dgeo, geo.data(), geo.size() * sizeof(float4)));
         if (!run->prim_dirs.empty()) TRY(upload(run->ddirs, run->prim_dirs.data(), run->prim_dirs.size() * sizeof(double)));
         if (!run->prim_weights.empty()) TRY(upload(run->dw, run->prim_weights.data(), run->prim_weights.size() * sizeof(double)));
+        if (!run->prop.empty()) TRY(upload(run->dprop, run->prop.data(), run->prop.size() * sizeof(float)));
+        if (run->p.capture) {
+            TRY(run->dcap.alloc((size_t)std::max(R, 1) * kCaptureWindows * kDirBins * sizeof(float)));
+            TRY(cudaMemset(run->dcap.p, 0, run->dcap.bytes));
+        }
 
         // launch shapes: one resident wave of blocks for the trace and shade kernels
         int dev_sms = 0;
@@ -229,6 +235,16 @@ void run_worker(pach_run *run) {
         r.prim_dirs = run->prim_dirs.empty() ? nullptr : run->ddirs.as<double>();
         r.prim_weights = run->prim_weights.empty() ? nullptr : run->dw.as<double>();
         r.prim_base = run->p.ray_begin;
+        r.prop = run->prop.empty() ? nullptr : run->dprop.as<float4>();
+        r.n_prop = run->prop.empty() ? 0 : run->p.n_proposal;
+        r.prop_mix = (float)(run->p.proposal_mix > 0 ? run->p.proposal_mix : 0.3);
+        r.capture = run->p.capture ? run->dcap.as<float>() : nullptr;
+        {
+            const bool given = run->p.capture_edges_ms[0] != 0 || run->p.capture_edges_ms[1] != 0 ||
+                               run->p.capture_edges_ms[2] != 0;
+            const double def[3] = {80.0, 400.0, 1200.0};
+            for (int i = 0; i < 3; ++i) r.cap_edge[i] = (float)(given ? run->p.capture_edges_ms[i] : def[i]);
+        }
         r.h_oct = run->h_oct;
         r.oct_lo = run->p.oct_lo;
         r.oct_hi = run->p.oct_hi;
@@ -557,8 +573,22 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
             return fail(PACH_ERR_INVALID_ARGUMENT, "receiver " + std::to_string(i) + ": radius must be positive, origin finite");
     for (int s = 0; s < n_sources; ++s)
         if (sources[s].kind < 0 || sources[s].kind > 2) return fail(PACH_ERR_INVALID_ARGUMENT, "unknown source kind");
+    if (p.proposal) {
+        if (p.n_proposal < 1 || p.n_proposal > 256)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "n_proposal must be 1..256 when proposal is given");
+        if (p.prim_dirs) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal and prim_dirs exclude each other");
+        if (p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "capture records uniform-emission runs only");
+        if (!(p.proposal_mix >= 0 && p.proposal_mix <= 1))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "proposal_mix must lie in [0, 1] (0 = default)");
+        for (long long i = 0; i < (long long)p.n_proposal * PACH_MLP_OUT; ++i)
+            if (!std::isfinite(p.proposal[i])) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal holds a non-finite value");
+    }
+    if (p.capture && (p.capture != 1 || n_receivers < 1))
+        return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0 or 1 and needs receivers");
     const HostScene &hs = scene->hs;
     auto *run = new pach_run();
+    if (p.proposal) proposal_lobes(p.proposal, p.n_proposal, run->prop);
+    run->p.proposal = nullptr;
     run->scene = scene;
     run->p = p;
     run->src.assign(sources, sources + n_sources);
@@ -665,6 +695,22 @@ pach_status pach_trace_get_histograms(pach_run *run, int32_t scaled, double *ene
     return PACH_OK;
 }
 
+pach_status pach_trace_get_capture(pach_run *run, float *out, size_t cap) {
+    if (pach_status s = check_run(run)) return s;
+    {
+        std::lock_guard<std::mutex> lk(run->mu);
+        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+    }
+    if (!run->p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "the run was made without capture");
+    const size_t n = (size_t)run->R * kCaptureWindows * kDirBins;
+    if (!out || cap < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap < receivers * 4 * 1536");
+    cudaSetDevice(run->scene->device);
+    cudaError_t e = cudaMemcpy(out, run->dcap.p, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "capture copy"));
+    return PACH_OK;
+}
+
 pach_status pach_trace_get_stats(pach_run *run, pach_stats *stats) {
     if (pach_status s = check_run(run)) return s;
     if (!stats) return fail(PACH_ERR_INVALID_ARGUMENT, "stats is null");
@@ -760,6 +806,35 @@ pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, in
     if ((e = launch_emit(r, ray_begin, n, dout.as<double>(), 0)) ||
         (e = cudaMemcpy(dirs_out, dout.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost)))
         return fail(PACH_ERR_CUDA, cuda_msg(e, "emit"));
+    return PACH_OK;
+}
+
+int32_t pach_direction_bin(double x, double y, double z) { return dir_bin((float)x, (float)y, (float)z); }
+
+pach_status pach_proposal_sample(const float *proposal, int32_t n_prop, double mix, uint64_t seed, int64_t ray_begin,
+                                 int32_t n, float *dirs, float *weights) {
+    if (!proposal || n_prop < 1 || n_prop > 256 || !(mix >= 0 && mix <= 1) || n < 0 || ray_begin < 0 ||
+        ray_begin + n > (1ll << 32) || (n > 0 && (!dirs || !weights)))
+        return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (n == 0) return PACH_OK;
+    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
+    std::vector<float> lobes;
+    proposal_lobes(proposal, n_prop, lobes);
+    DevMem dl, dd, dw;
+    cudaError_t e;
+    if ((e = upload(dl, lobes.data(), lobes.size() * sizeof(float))) || (e = dd.alloc(sizeof(float) * 3 * n)) ||
+        (e = dw.alloc(sizeof(float) * n)))
+        return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample setup"));
+    DevRun r{};
+    r.seed = seed;
+    r.nsrc = 1;
+    r.prop = dl.as<float4>();
+    r.n_prop = n_prop;
+    r.prop_mix = (float)(mix > 0 ? mix : 0.3);
+    if ((e = launch_prop_sample(r, ray_begin, n, dd.as<float>(), dw.as<float>(), 0)) ||
+        (e = cudaMemcpy(dirs, dd.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(weights, dw.p, sizeof(float) * n, cudaMemcpyDeviceToHost)))
+        return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample"));
     return PACH_OK;
 }
 

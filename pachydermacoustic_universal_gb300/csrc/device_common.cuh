@@ -265,9 +265,12 @@ __device__ __forceinline__ void hist_add(const DevRun &r, int k, int oct, long l
     atomicAdd(r.hAn + (((size_t)k * 3 + kind) * kBands + oct) * r.T + bin, (double)e);
 }
 
+__device__ __forceinline__ void capture_add(const DevRun &r, const float4 *rec, int k, uint32_t prim, double time,
+                                            float e);
+
 // Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half.
 __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
-                                                  double t_sum, float Iabs, int oct, int mask) {
+                                                  double t_sum, float Iabs, int oct, int mask, uint32_t prim) {
     uint32_t n = 0;
     for (int k = 0; k < r.R; ++k) {
         float t, half;
@@ -278,6 +281,7 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const float4 
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
         const float e = Iabs * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
         hist_add(r, k, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
+        if (r.capture) capture_add(r, rec, k, prim, time, e);
     }
     return n;
 }
@@ -285,7 +289,8 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const float4 
 // Spherical_Receiver.CheckBroadbandRay (Classes_Receivers.cs:803-829): every band of the range,
 // analysis bin 0 (specular).
 __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
-                                                 double t_sum, const float (&E)[kBands], const float (&sc)[kBands]) {
+                                                 double t_sum, const float (&E)[kBands], const float (&sc)[kBands],
+                                                 uint32_t prim) {
     uint32_t n = 0;
     for (int k = 0; k < r.R; ++k) {
         float t, half;
@@ -294,12 +299,15 @@ __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const float4 *
         const double time = t_sum + (double)(t * r.inv_c);
         const long long bin = (long long)(time * r.fs);
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
+        float esum = 0.f;
 #pragma unroll
         for (int oct = 0; oct < kBands; ++oct) {
             if (oct < r.oct_lo || oct > r.oct_hi) continue;
             const float e = E[oct] * sc[oct] * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
             hist_add(r, k, oct, bin, e, d, 0);
+            esum += e;
         }
+        if (r.capture) capture_add(r, rec, k, prim, time, esum);
     }
     return n;
 }
@@ -329,6 +337,83 @@ __device__ __forceinline__ float3 emit_dir(const DevRun &r, long long prim, int 
     if (u + v > 1.f) { u = 1.f - u; v = 1.f - v; }
     const float3 a = f3(r.geo[3 * f]), b = f3(r.geo[3 * f + 1]), c = f3(r.geo[3 * f + 2]);
     return unit3(a + (b - a) * u + (c - a) * v);
+}
+
+// ------------------------------------------------------------------------------------------
+// learned emission proposal and training capture (no counterpart in the reference)
+// ------------------------------------------------------------------------------------------
+constexpr float kInv4Pi = 0.0795774715459476679f;
+
+// Defensive mixture: uniform on the sphere with probability prop_mix, else a lobe of one of the n_prop
+// receiver mixtures (receiver uniform, lobe by its weight).  w = (1 / 4 pi) / q(d), the density ratio of
+// uniform emission to the mixture, keeps the estimate unbiased.
+__device__ __forceinline__ float3 proposal_dir(const DevRun &r, uint32_t prim, float &w) {
+    const float4 U = draw(r.seed, prim, 0ull, 1u);
+    const float4 V = draw(r.seed, prim, 0ull, 2u);
+    float3 d;
+    if (U.x < r.prop_mix) {
+        const float z = 1.0f - 2.0f * V.x;
+        const float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float sp, cp;
+        sincospif(2.0f * V.y, &sp, &cp);
+        d = make_float3(rr * cp, rr * sp, z);
+    } else {
+        const int j = min(r.n_prop - 1, (int)(U.y * (float)r.n_prop));
+        const float4 *L = r.prop + (size_t)j * kLobes * 2;
+        int k = 0;
+        while (k < kLobes - 1 && U.z >= __ldg(L + 2 * k + 1).y) ++k;
+        const float4 a = __ldg(L + 2 * k);
+        const float kap = a.w;
+        // Wood (1994) for the 2-sphere: cosine to the mean c = 1 + log(u + (1 - u) e^(-2 kappa)) / kappa
+        const float c = fminf(1.f, fmaxf(-1.f, 1.f + logf(V.x + (1.f - V.x) * expf(-2.f * kap)) / kap));
+        const float sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+        float sp, cp;
+        sincospif(2.0f * V.y, &sp, &cp);
+        const float3 mu = make_float3(a.x, a.y, a.z);
+        const float3 t = fabsf(mu.x) < 0.9f ? make_float3(1.f, 0.f, 0.f) : make_float3(0.f, 1.f, 0.f);
+        const float3 e1 = unit3(cross3(mu, t));
+        const float3 e2 = cross3(mu, e1);
+        d = unit3(mu * c + (e1 * cp + e2 * sp) * sn);
+    }
+    float qs = 0.f;
+    for (int j = 0; j < r.n_prop; ++j) {
+        const float4 *L = r.prop + (size_t)j * kLobes * 2;
+        for (int k = 0; k < kLobes; ++k) {
+            const float4 a = __ldg(L + 2 * k), b = __ldg(L + 2 * k + 1);
+            qs += expf(b.x + a.w * (a.x * d.x + a.y * d.y + a.z * d.z - 1.f));
+        }
+    }
+    const float q = r.prop_mix * kInv4Pi + (1.f - r.prop_mix) * qs / (float)r.n_prop;
+    w = kInv4Pi / q;
+    return d;
+}
+
+// Emission direction of primary prim and its weight (1 unless importance sampled).
+__device__ __forceinline__ float3 primary_dir(const DevRun &r, uint32_t prim, int kind, float &w) {
+    w = 1.f;
+    if (r.prim_dirs) {
+        const double *pd = r.prim_dirs + 3 * ((long long)prim - r.prim_base);
+        if (r.prim_weights) w = (float)r.prim_weights[(long long)prim - r.prim_base];
+        return make_float3((float)pd[0], (float)pd[1], (float)pd[2]);
+    }
+    if (r.prop) return proposal_dir(r, prim, w);
+    if (r.prim_weights) w = (float)r.prim_weights[(long long)prim - r.prim_base];
+    return emit_dir(r, prim, kind);
+}
+
+// Training capture: energy e detected at receiver k at time (s) from primary prim, added to the bin
+// of the primary's emission direction in the window of (time - direct arrival).
+__device__ __forceinline__ void capture_add(const DevRun &r, const float4 *rec, int k, uint32_t prim, double time,
+                                            float e) {
+    const int s = (int)((prim + 1ull) % (unsigned long long)r.nsrc);
+    const float4 src = r.src[s];
+    float w;
+    const float3 d0 = primary_dir(r, prim, (int)src.w, w);
+    const int b = dir_bin(d0.x, d0.y, d0.z);
+    const double dx = rec[k].x - src.x, dy = rec[k].y - src.y, dz = rec[k].z - src.z;
+    const float ms = (float)((time - sqrt(dx * dx + dy * dy + dz * dz) * r.inv_c_d) * 1000.0);
+    const int win = (ms >= r.cap_edge[0]) + (ms >= r.cap_edge[1]) + (ms >= r.cap_edge[2]);
+    atomicAdd(r.capture + ((size_t)k * kCaptureWindows + win) * kDirBins + b, e);
 }
 
 // ------------------------------------------------------------------------------------------

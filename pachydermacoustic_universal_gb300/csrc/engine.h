@@ -1,5 +1,6 @@
 // engine.h -- internal structures shared by the host side (scene build, C ABI) and the kernels.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -7,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pach_gpu.h"
+#include "../../include/pach_proposal.h"
 
 namespace pach {
 
@@ -127,7 +129,47 @@ struct DevRun {
     unsigned *bin_count;           // [kSortBins], zero between waves
     unsigned *bin_cursor;          // [kSortBins]
     float sort_lo[3], sort_inv[3]; // origin grid: cell = (p - lo) * inv, 0..kSortGrid-1 per axis
+    // learned emission proposal (null: the source's own emission)
+    const float4 *prop;            // [n_prop][kLobes][2]: (mu xyz, kappa), (log pi + log norm, cdf, 0, 0)
+    int n_prop;
+    float prop_mix;                // probability of the uniform component
+    // training capture (null: off): energy per receiver, time window and emission-direction bin
+    float *capture;                // [R][kCaptureWindows][kDirBins]
+    float cap_edge[3];             // window edges, ms after the direct arrival
 };
+
+constexpr int kLobes = PACH_MLP_LOBES;
+constexpr int kDirBins = PACH_DIR_BINS;
+constexpr int kCaptureWindows = PACH_CAPTURE_WINDOWS;
+
+// Emission-direction bin: cube map with faces +x -x +y -y +z -z, 16 x 16 cells each; a face's cell
+// (i, j) covers u, v in [i/8 - 1, (i+1)/8 - 1) x [j/8 - 1, (j+1)/8 - 1) of the face's two other
+// axes in x, y, z order (u = second / major, v = third / major).
+__host__ __device__ inline int dir_bin(float x, float y, float z) {
+    const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+    int f;
+    float u, v;
+    if (ax >= ay && ax >= az) {
+        f = x > 0.f ? 0 : 1;
+        u = y / ax;
+        v = z / ax;
+    } else if (ay >= az) {
+        f = y > 0.f ? 2 : 3;
+        u = x / ay;
+        v = z / ay;
+    } else {
+        f = z > 0.f ? 4 : 5;
+        u = x / az;
+        v = y / az;
+    }
+    int i = (int)((u + 1.f) * 8.f), j = (int)((v + 1.f) * 8.f);
+    i = i < 0 ? 0 : (i > 15 ? 15 : i);
+    j = j < 0 ? 0 : (j > 15 ? 15 : j);
+    return f * 256 + j * 16 + i;
+}
+
+// mlp.cu: raw network outputs [n][160] -> the lobe table DevRun::prop holds ([n][kLobes][8] floats)
+void proposal_lobes(const float *raw, int n, std::vector<float> &out);
 
 constexpr int kSortGrid = 8;                       // origin cells per axis
 constexpr int kSortBins = 8 * kSortGrid * kSortGrid * kSortGrid;  // x 8 direction octants
@@ -156,6 +198,7 @@ cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int 
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
                          double *t, double *pts, cudaStream_t s);
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s);
+cudaError_t launch_prop_sample(const DevRun &r, long long p0, int n, float *dirs, float *weights, cudaStream_t s);
 
 // capi.cpp: read access to a scene handle (for entry points in other translation units)
 const HostScene *scene_host(const pach_scene *s);

@@ -124,15 +124,8 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
         const long long prim = p0 + i;
         const int s = (int)((prim + 1) % r.nsrc);  // SourceCluster round robin (Classes_Sources.cs:712-722)
         const float4 src = r.src[s];
-        float3 d;
-        float w = 1.f;
-        if (r.prim_dirs) {
-            const double *pd = r.prim_dirs + 3 * (prim - r.prim_base);
-            d = make_float3((float)pd[0], (float)pd[1], (float)pd[2]);
-        } else {
-            d = emit_dir(r, prim, (int)src.w);
-        }
-        if (r.prim_weights) w = (float)r.prim_weights[prim - r.prim_base];
+        float w;
+        float3 d = primary_dir(r, (uint32_t)prim, (int)src.w, w);
         float E[kBands], sc[kBands];
 #pragma unroll
         for (int o = 0; o < kBands; ++o) {
@@ -153,13 +146,13 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             L.v[C_RET] += tw.retests;
             ++L.v[C_SEGA];
             if (!hit) {
-                if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, 1e6f, t_sum, E, sc);
+                if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
 #pragma unroll
                 for (int o = 0; o < kBands; ++o) L.lost += (double)(E[o] * sc[o]);
                 lost = true;
                 break;
             }
-            if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, t, t_sum, E, sc);
+            if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, t, t_sum, E, sc, (uint32_t)prim);
             t_sum += (double)t * r.inv_c_d;
             pos = pos + d * t;
             const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
@@ -460,7 +453,7 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
             const bool hit = h.x >= 0;
             const float t = __int_as_float(h.y);
             ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
-            L.v[C_DET] += detect_octave(r, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask);
+            L.v[C_DET] += detect_octave(r, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask, R.prim);
             if (!hit) {
                 // lost: no End_Trace after a miss in phase B (TaskAll:437-443), loop exit in phase C (500-505)
                 L.lost += (double)(R.I * R.scale);
@@ -571,6 +564,15 @@ __global__ void k_emit(DevRun r, long long p0, int n, double *out) {
     out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
 }
 
+__global__ void k_prop_sample(DevRun r, long long p0, int n, float *dirs, float *weights) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float w;
+    const float3 d = proposal_dir(r, (uint32_t)(p0 + i), w);
+    dirs[3 * i] = d.x; dirs[3 * i + 1] = d.y; dirs[3 * i + 2] = d.z;
+    weights[i] = w;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
@@ -639,6 +641,11 @@ cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double
 
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s) {
     k_emit<<<(n + 127) / 128, 128, 0, s>>>(r, p0, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prop_sample(const DevRun &r, long long p0, int n, float *dirs, float *weights, cudaStream_t s) {
+    k_prop_sample<<<(n + 127) / 128, 128, 0, s>>>(r, p0, n, dirs, weights);
     return cudaGetLastError();
 }
 

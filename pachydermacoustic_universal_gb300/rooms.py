@@ -160,6 +160,26 @@ def shoebox_c1(seed: int = 1, rays: int = 100_000, scattering: float = 0.2) -> W
     return Workload("shoebox_10x8x4_12tri", scene, [src], [ReceiverSpec(r) for r in recs], rays, 2.0)
 
 
+def proposal_room_c4(seed: int, rays: int = 1_000_000, n_receivers: int = 3) -> Workload:
+    """A room drawn like shoebox_c1 for the learned emission proposal: a shoebox of seeded size
+    (8-12 x 6-10 x 3-5 m), 12 triangles, per-face absorption U[0.05, 0.35], scattering 0.2, one omni
+    source and n_receivers receivers of radius 0.5 m at seeded interior points, 2 s cutoff."""
+    rng = np.random.default_rng(1_000_003 * seed + 17)
+    size = (rng.uniform(8, 12), rng.uniform(6, 10), rng.uniform(3, 5))
+    b = _Builder()
+    face_of = _box_faces(b, (0, 0, 0), size)
+    v, offs, idx = b.arrays()
+    face_abs = rng.uniform(0.05, 0.35, size=(6, BANDS))
+    absn = face_abs[np.asarray(face_of)]
+    scat = np.full((12, BANDS), 0.2)
+    trans = np.zeros((12, BANDS))
+    scene = SceneArrays(v, offs, idx, absn, scat, trans)
+    src = _interior_points(rng, (0, 0, 0), size, 1, margin=1.0)[0]
+    recs = _interior_points(rng, (0, 0, 0), size, n_receivers, margin=1.0, avoid=[src], min_sep=1.5)
+    return Workload(f"proposal_room_{seed}", scene, [SourceSpec(src)], [ReceiverSpec(r) for r in recs], rays, 2.0,
+                    extra={"size": size})
+
+
 def _tessellated_shell(b: _Builder, size, target_tris, rng, sigma):
     """Box shell whose 6 faces are grids of quads (2 triangles each), vertices shared along edges
     and jittered in 3-D with N(0, sigma) per unique vertex."""

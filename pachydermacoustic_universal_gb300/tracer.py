@@ -71,7 +71,8 @@ def receiver_array(receivers):
 def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 7), is_order=-1, sample_rate=1000,
                 pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
                 block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
-                ring_log2=0, kernel_timing=False, ray_sort=0, traversal=0):
+                ring_log2=0, kernel_timing=False, ray_sort=0, traversal=0, capture=False, capture_edges_ms=None,
+                proposal=None, proposal_mix=0.0):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -94,6 +95,13 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.traversal = int(traversal)
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
+    p.capture = int(bool(capture))
+    if capture_edges_ms is not None:
+        p.capture_edges_ms[:] = [float(x) for x in capture_edges_ms]
+    if proposal is not None:
+        p.proposal = _capi.fptr(proposal)
+        p.n_proposal = int(proposal.shape[0])
+        p.proposal_mix = float(proposal_mix)
     return p
 
 
@@ -135,6 +143,12 @@ class Run:
                                                     dptr(Dn), dptr(An), E.size))
         return {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}
 
+    def capture(self):
+        """Energy per receiver, capture window and emission-direction bin, [R][4][1536] (W, unscaled)."""
+        out = np.zeros((self.R, _capi.CAPTURE_WINDOWS, _capi.DIR_BINS), dtype=np.float32)
+        check(_capi.lib().pach_trace_get_capture(self.handle, _capi.fptr(out), out.size))
+        return out
+
     def stats(self):
         s = _capi.Stats()
         check(_capi.lib().pach_trace_get_stats(self.handle, C.byref(s)))
@@ -158,14 +172,19 @@ def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, **kw):
     n = workload.rays if rays is None else rays
     pd = kw.pop("prim_dirs", None)
     pw = kw.pop("prim_weights", None)
+    pr = kw.pop("proposal", None)
     pd = np.ascontiguousarray(pd, dtype=np.float64) if pd is not None else None
     pw = np.ascontiguousarray(pw, dtype=np.float64) if pw is not None else None
+    pr = np.ascontiguousarray(pr, dtype=np.float32).reshape(-1, _capi.MLP_OUT) if pr is not None else None
     params = make_params(rays=n, cutoff_length_m=workload.cutoff_length_m, hist_cotime_ms=workload.cutoff_s * 1000.0,
-                         seed=seed, sample_rate=workload.sample_rate, prim_dirs=pd, prim_weights=pw, **kw)
-    run = Run(ds, workload.sources, workload.receivers, params, keep=(pd, pw))
+                         seed=seed, sample_rate=workload.sample_rate, prim_dirs=pd, prim_weights=pw, proposal=pr, **kw)
+    run = Run(ds, workload.sources, workload.receivers, params, keep=(pd, pw, pr))
     try:
         run.wait()
-        return run.histograms(scaled=scaled), run.stats()
+        h = run.histograms(scaled=scaled)
+        if params.capture:
+            h["capture"] = run.capture()
+        return h, run.stats()
     finally:
         run.close()
 

@@ -187,8 +187,11 @@ def test_parameter_functions_engine_equals_oracle_on_noisy_curves():
 
 # ---------------------------------------------------------------- the C ABI
 def test_library_exports_every_declared_symbol():
-    header = open(os.path.join(ROOT, "include", "pach_gpu.h")).read()
-    declared = set(re.findall(r"\b(pach_[a-z0-9_]+)\s*\(", header))
+    declared = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if h.endswith(".h"):
+            header = open(os.path.join(ROOT, "include", h)).read()
+            declared |= set(re.findall(r"\b(pach_[a-z0-9_]+)\s*\(", header))
     assert declared == set(_capi.EXPORTS)
     L = _capi.lib()
     for name in declared:
