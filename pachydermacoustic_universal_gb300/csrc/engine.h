@@ -82,8 +82,9 @@ struct WaveCtl {
     long long pa_begin, pa_count;   // phase-A batch of the current iteration
     unsigned long long waves, overflow, peak_live;
     long long prim_first;           // first primary of the run
-    unsigned long long per_prim;    // ring footprint per primary measured by the pilot batch (0 = not yet)
+    unsigned long long per_prim;    // peak ring footprint per primary measured by the pilot batch (0 = not yet)
     unsigned long long trace_next;  // next wave item a trace thread takes (dynamic fetch)
+    unsigned long long last_live;   // live count at the previous feed decision
     int done, pad;
 };
 

@@ -67,15 +67,19 @@ __global__ void k_feed(DevRun r) {
     const unsigned long long live = c->tail - c->head;
     const long long fed = c->next_prim - c->prim_first;
     if (c->per_prim == 0 && fed >= kPilotPrimaries) {
-        // the pilot batch ran alone: once its split trees are done, the octave rays it made per
-        // primary (x 1.5) is the ring footprint to plan the following batches with
+        // the pilot batch ran alone: once its split trees are done, its peak live count per primary
+        // (x 1.5) is the ring footprint a batch of primaries fed together reaches
         if (live != 0) return;
-        c->per_prim = r.cnt->octave_rays / (unsigned long long)fed * 3 / 2 + 1;
+        c->per_prim = c->peak_live * 3 / 2 / (unsigned long long)fed + 1;
         if (c->per_prim < r.feed_bound) c->per_prim = r.feed_bound;
     }
-    if (c->next_prim < c->prim_end && live <= r.low_water) {
-        // Hard limit: the phase-A output of every fed primary must fit.  Soft limit: the split trees
-        // grown from this batch keep the ring at most half full.
+    // Split trees grow for many waves after phase A, so a batch is fed only once the previous one
+    // has peaked: the live count is low and no longer rising (generations of primaries).
+    const bool decaying = live <= c->last_live;
+    c->last_live = live;
+    if (c->next_prim < c->prim_end && live <= r.low_water && (decaying || live == 0)) {
+        // Hard limit: the phase-A output of every fed primary must fit.  Soft limit: the new batch's
+        // peak keeps the ring at most half full.
         unsigned long long room = (r.ring_cap - live) / r.feed_bound;
         const unsigned long long per_prim = c->per_prim ? c->per_prim : r.feed_bound;
         const unsigned long long half = r.ring_cap / 2;
