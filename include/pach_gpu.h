@@ -124,6 +124,17 @@ typedef struct {
     double capture_edges_ms[3];    /* capture windows, ms after the direct arrival; zeros = 80, 400, 1200 */
 } pach_trace_params;
 
+/* One room of a batch run (pach_batch_begin). */
+typedef struct {
+    const struct pach_scene *scene;
+    const pach_source_desc *sources;
+    int32_t n_sources;
+    int32_t n_receivers;
+    const pach_receiver_desc *receivers;
+    int64_t ray_count;             /* primary rays of this room */
+    double cutoff_length_m;        /* this room's SplitRayTracer cutoff length */
+} pach_room_desc;
+
 typedef struct {
     int32_t state;                 /* pach_run_state */
     int32_t last_status;           /* pach_status of a failed run */
@@ -189,6 +200,16 @@ pach_status pach_scene_info(const pach_scene *scene, int32_t *n_polys, int32_t *
 pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
                              const pach_receiver_desc *receivers, int32_t n_receivers,
                              const pach_trace_params *params, pach_run **out);
+/* Batch run: many rooms, each with its own scene, sources, receivers, primaries and cutoff, traced as
+ * one wavefront (one persistent device loop) -- no counterpart in the reference, which runs one
+ * SplitRayTracer per room.  params gives the shared settings (seed, octave range, histogram rate and
+ * length, tuning); its ray_count, cutoff_length_m, prim_dirs, prim_weights and proposal are not used
+ * (the emission overrides must be NULL).  Room i's primaries are numbered from ray_begin + the rays of
+ * rooms 0..i-1, so room i traces exactly as pach_trace_begin would with that ray_begin.  The run's
+ * receivers (histogram rows) are the rooms' receivers in room order; scaled histograms divide each
+ * room by its own primaries. */
+pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const pach_trace_params *params,
+                             pach_run **out);
 pach_status pach_trace_poll(pach_run *run, pach_progress *progress);
 pach_status pach_trace_cancel(pach_run *run);
 /* Blocks until the run stops or timeout_ms passes (timeout_ms < 0: no limit). */

@@ -58,6 +58,12 @@ class TraceParams(C.Structure):
                 ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3)]
 
 
+class RoomDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("sources", C.POINTER(SourceDesc)), ("n_sources", C.c_int32),
+                ("n_receivers", C.c_int32), ("receivers", C.POINTER(ReceiverDesc)), ("ray_count", C.c_int64),
+                ("cutoff_length_m", C.c_double)]
+
+
 class Progress(C.Structure):
     _fields_ = [("state", C.c_int32), ("last_status", C.c_int32), ("rays_done", C.c_int64),
                 ("rays_total", C.c_int64), ("end_traces", C.c_int64), ("segments", C.c_int64)]
@@ -87,7 +93,7 @@ class Stats(C.Structure):
 
 # Every symbol include/pach_gpu.h declares (checked by the CPU test suite).
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
-           "pach_scene_info", "pach_trace_begin", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
+           "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
@@ -115,6 +121,7 @@ def _declare(L):
         "pach_scene_info": (C.c_int, [vp, _ip, _ip, _dp, _dp, _dp, _dp]),
         "pach_trace_begin": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
                                        C.POINTER(TraceParams), C.POINTER(vp)]),
+        "pach_batch_begin": (C.c_int, [C.POINTER(RoomDesc), C.c_int32, C.POINTER(TraceParams), C.POINTER(vp)]),
         "pach_trace_poll": (C.c_int, [vp, C.POINTER(Progress)]),
         "pach_trace_cancel": (C.c_int, [vp]),
         "pach_trace_wait": (C.c_int, [vp, C.c_int64]),

@@ -63,18 +63,28 @@ struct pach_scene {
     }
 };
 
-struct pach_run {
+// One room of a run: a scene handle, its sources and receivers, its primaries and cutoff, and the
+// values the SplitRayTracer ctor derives from them (TaskAll:68-177).
+struct RoomSpec {
     pach_scene *scene = nullptr;
-    pach_trace_params p{};
     std::vector<pach_source_desc> src;
     std::vector<pach_receiver_desc> rec;
+    long long rays = 0, prim_begin = 0;
+    double cutoff_len = 0, cotime = 0;
+    int h_oct = 0;
+    unsigned long long max_broad = 0;
+};
+
+struct pach_run {
+    pach_scene *scene = nullptr;  // the first room's scene (device and single-room fast path)
+    pach_trace_params p{};
+    std::vector<RoomSpec> rooms;
     std::vector<double> prim_dirs, prim_weights;
     std::vector<float> prop;  // learned-proposal lobe table ([n_proposal][kLobes][8])
-    int R = 0, T = 0, nsrc = 0, h_oct = 0;
-    double cotime = 0;
-    unsigned long long max_broad = 0;
+    int R = 0, T = 0, nsrc = 0;   // receivers and sources over all rooms
     // device buffers
     DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw, sortbins, dprop, dcap;
+    DevMem droom, droomprim, btri, btri64, bnorm, bmat, btrans, bbvh;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -93,7 +103,7 @@ struct pach_run {
         }
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
-                          &sortbins, &dprop, &dcap})
+                          &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh})
             m->release();
     }
 };
@@ -106,9 +116,129 @@ cudaError_t upload(DevMem &m, const void *src, size_t bytes) {
     return bytes ? cudaMemcpy(m.p, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
 }
 
+// Device layout of scenes: triangles (FP32 with plane and polygon ids), FP64 triangles, polygon
+// normals, materials, transmission and the 4-wide BVH.  A batch run appends several scenes into one
+// set of arrays: triangle, polygon, plane and node ids are offset, and each scene's root is kept.
+struct SceneArrays {
+    std::vector<float4> tri, norm, mat;
+    std::vector<float> trans, bvh;
+    std::vector<double> tri64;
+    int planes = 0;
+    float t_eps = 0.f;
+    bool has_trans = false;
+};
+
+int append_scene(const HostScene &hs, SceneArrays &A) {
+    const int tri_off = (int)(A.tri.size() / 3), poly_off = (int)A.norm.size(), plane_off = A.planes;
+    const int node_off = (int)(A.bvh.size() / kBvhNodeFloats);
+    int max_plane = -1;
+    for (int i = 0; i < hs.ntri; ++i) {
+        const double *t = &hs.tri64[9 * (size_t)i];
+        const double ax = t[4] * t[8] - t[5] * t[7], ay = t[5] * t[6] - t[3] * t[8], az = t[3] * t[7] - t[4] * t[6];
+        const double graze = 1e-4 * std::sqrt(ax * ax + ay * ay + az * az);  // |det| < 1e-4 |e1 x e2|: near grazing
+        int plane = hs.tri_plane[i] + plane_off, poly = hs.tri_poly[i] + poly_off;
+        max_plane = std::max(max_plane, hs.tri_plane[i]);
+        float pw, qw;
+        std::memcpy(&pw, &plane, 4);
+        std::memcpy(&qw, &poly, 4);
+        A.tri.push_back(make_float4((float)t[0], (float)t[1], (float)t[2], pw));
+        A.tri.push_back(make_float4((float)t[3], (float)t[4], (float)t[5], qw));
+        A.tri.push_back(make_float4((float)t[6], (float)t[7], (float)t[8], (float)graze));
+    }
+    A.planes = plane_off + max_plane + 1;
+    A.tri64.insert(A.tri64.end(), hs.tri64.begin(), hs.tri64.end());
+    for (int p = 0; p < hs.npoly; ++p) {
+        A.norm.push_back(make_float4((float)hs.normal[3 * p], (float)hs.normal[3 * p + 1], (float)hs.normal[3 * p + 2], 0.f));
+        for (int o = 0; o < kBands; ++o) {
+            // Lambert_Scattering thresholds (Classes_Materials.cs:4466-4485)
+            const double s = hs.scat[p * 8 + o];
+            double lo, hi;
+            if (s < 0.25) { lo = 0.1; hi = 0.4; }
+            else { const double mod = std::fabs(1 - s) / 5; lo = s - mod; hi = s + mod; }
+            A.mat.push_back(make_float4((float)(1.0 - hs.alpha[p * 8 + o]), (float)lo, (float)s, (float)hi));
+            A.trans.push_back((float)hs.trans[p * 8 + o]);
+        }
+    }
+    const size_t b0 = A.bvh.size();
+    A.bvh.insert(A.bvh.end(), hs.bvh.begin(), hs.bvh.end());
+    if (tri_off || node_off)
+        for (size_t q = 0; q < hs.bvh.size() / kBvhNodeFloats; ++q)
+            for (int k = 0; k < 4; ++k) {
+                float *f = &A.bvh[b0 + q * kBvhNodeFloats + 24 + k];
+                int code;
+                std::memcpy(&code, f, 4);
+                if (code == (int)0x80000000) continue;       // empty slot
+                if (code >= 0) code += node_off;              // inner child
+                else {                                        // leaf ~(first * 16 + count - 1)
+                    const int c = ~code;
+                    code = ~(((c >> 4) + tri_off) * 16 + (c & 15));
+                }
+                std::memcpy(f, &code, 4);
+            }
+    A.t_eps = std::max(A.t_eps, (float)(2e-7 * hs.scale));
+    A.has_trans = A.has_trans || hs.has_trans;
+    return node_off;
+}
+
+cudaError_t upload_scene(const SceneArrays &A, DevMem &tri, DevMem &tri64, DevMem &norm, DevMem &mat, DevMem &trans,
+                         DevMem &bvh, DevScene &d) {
+    cudaError_t e;
+    if ((e = upload(tri, A.tri.data(), A.tri.size() * sizeof(float4))) ||
+        (e = upload(tri64, A.tri64.data(), A.tri64.size() * sizeof(double))) ||
+        (e = upload(norm, A.norm.data(), A.norm.size() * sizeof(float4))) ||
+        (e = upload(mat, A.mat.data(), A.mat.size() * sizeof(float4))) ||
+        (e = upload(trans, A.trans.data(), A.trans.size() * sizeof(float))) ||
+        (e = upload(bvh, A.bvh.data(), A.bvh.size() * sizeof(float))))
+        return e;
+    d.tri = tri.as<float4>();
+    d.tri64 = tri64.as<double>();
+    d.pnormal = norm.as<float4>();
+    d.mat = mat.as<float4>();
+    d.trans = trans.as<float>();
+    d.bvh = bvh.as<float4>();
+    d.ntri = (int)(A.tri.size() / 3);
+    d.t_eps = A.t_eps;
+    d.has_trans = A.has_trans ? 1 : 0;
+    return cudaSuccess;
+}
+
+// SplitRayTracer ctor values of one room (TaskAll:83-109): COTime from the cutoff length, h_oct (the
+// band of least total absorption among bands carrying >= 1e-6 of the peak power; a SourceCluster's
+// power is the per-band maximum over members, Classes_Sources.cs:680-688) and the phase-A bound.
+bool room_setup(RoomSpec &rm, const pach_trace_params &p, std::string &err) {
+    const HostScene &hs = rm.scene->hs;
+    rm.cotime = rm.cutoff_len / hs.c;
+    double total_abs[kBands] = {0}, power[kBands] = {0};
+    for (const pach_source_desc &s : rm.src)
+        for (int o = 0; o < kBands; ++o) power[o] = std::max(power[o], 1e-12 * std::pow(10.0, .1 * s.power_db[o]));
+    for (int q = 0; q < hs.npoly; ++q)
+        for (int o = p.oct_lo; o <= p.oct_hi; ++o) total_abs[o] += hs.area[q] * hs.alpha[q * 8 + o];
+    double mn = HUGE_VAL, octpower = 0;
+    for (int o = p.oct_lo; o <= p.oct_hi; ++o) octpower = std::max(octpower, power[o]);
+    rm.h_oct = p.oct_lo;
+    for (int o = p.oct_lo; o <= p.oct_hi; ++o) {
+        if (power[o] < octpower * 1e-6) continue;
+        if (mn > total_abs[o]) { mn = total_abs[o]; rm.h_oct = o; }
+    }
+    if (p.max_broadband_bounces > 0) {
+        rm.max_broad = (unsigned long long)p.max_broadband_bounces;
+    } else {
+        rm.max_broad = derived_broadband_bound(hs, rm.h_oct, p.pure_specular != 0);
+        if (rm.max_broad == 0) {
+            err = "a surface reflects band h_oct without loss: the broadband loop would not terminate; "
+                  "set max_broadband_bounces";
+            return false;
+        }
+    }
+    return true;
+}
+
 // The run worker: uploads the run's inputs, then drives the wavefront loop on one stream --
-// iterations of feed -> broadband -> wave -> trace -> shade, launched in batches between which the
-// host reads the device schedule (done flag, progress) once.
+// iterations of feed -> broadband -> wave -> trace -> shade.  By default the whole loop is one CUDA
+// graph launch: the iteration is captured into the body of a conditional while node whose last kernel
+// (k_cond) ends the loop when the run is done; progress and cancellation go through mapped host
+// memory.  With kernel_timing = 1 the host launches batches of iterations instead, with CUDA events
+// around every kernel.
 void run_worker(pach_run *run) {
     auto finish = [&](pach_status s, const std::string &msg, int st) {
         std::lock_guard<std::mutex> lk(run->mu);
@@ -125,12 +255,17 @@ void run_worker(pach_run *run) {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> kev;  // per-kernel timing events (kernel_timing = 1)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
     std::string where;
     pach_status status = PACH_OK;
     std::string msg;
     int final_state = PACH_RUN_STOPPED;
     WaveCtl *h_ctl = nullptr;
     DevCounters *h_cnt = nullptr;
+    HostMirror *h_mirror = nullptr;
+    int *h_cancel = nullptr;
+    const int n_rooms = (int)run->rooms.size();
     do {
 #define TRY(x)                                        \
     {                                                 \
@@ -142,7 +277,6 @@ void run_worker(pach_run *run) {
         TRY(cudaEventCreate(&ev1));
         TRY(cudaMallocHost(&h_ctl, sizeof(WaveCtl)));
         TRY(cudaMallocHost(&h_cnt, sizeof(DevCounters)));
-        const HostScene &hs = sc->hs;
         const int R = run->R, T = run->T;
         const size_t nE = (size_t)R * kBands * T, nD = (size_t)R * 3 * kBands * T;
         TRY(run->hE.alloc(std::max<size_t>(nE, 1) * 8));
@@ -155,21 +289,71 @@ void run_worker(pach_run *run) {
         for (DevMem *m : {&run->hE, &run->hP, &run->hDp, &run->hDn, &run->hAn, &run->cnt, &run->qctl})
             TRY(cudaMemsetAsync(m->p, 0, m->bytes, stream));
         if (e) break;
-        // receivers, sources, powers, geodesic faces
-        std::vector<float4> rec(std::max(R, 1));
-        for (int i = 0; i < R; ++i)
-            rec[i] = make_float4((float)run->rec[i].origin[0], (float)run->rec[i].origin[1], (float)run->rec[i].origin[2],
-                                 (float)(run->rec[i].radius * run->rec[i].radius));
-        TRY(upload(run->drec, rec.data(), rec.size() * sizeof(float4)));
-        std::vector<float4> src(run->nsrc);
-        std::vector<float> e0((size_t)run->nsrc * kBands);
-        for (int s = 0; s < run->nsrc; ++s) {
-            src[s] = make_float4((float)run->src[s].origin[0], (float)run->src[s].origin[1], (float)run->src[s].origin[2],
-                                 (float)run->src[s].kind);
-            for (int o = 0; o < kBands; ++o) e0[s * kBands + o] = (float)(1e-12 * std::pow(10.0, .1 * run->src[s].power_db[o]));
+
+        // scene: the first room's own device arrays, or the concatenation of every room's
+        DevScene S = sc->dev;
+        std::vector<int> roots(n_rooms, 0);
+        if (n_rooms > 1) {
+            SceneArrays A;
+            for (int i = 0; i < n_rooms; ++i) roots[i] = append_scene(run->rooms[i].scene->hs, A);
+            TRY(upload_scene(A, run->btri, run->btri64, run->bnorm, run->bmat, run->btrans, run->bbvh, S));
         }
+        // receivers, sources, powers and room table over all rooms
+        std::vector<float4> rec(std::max(R, 1)), src;
+        std::vector<float> e0;
+        std::vector<RoomParams> rp(n_rooms);
+        std::vector<long long> rprim(n_rooms + 1);
+        double bmin[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, bmax[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        unsigned long long bound = 0;
+        int ntri_max = 0;
+        bool has_trans = false;
+        const bool pure = run->p.pure_specular != 0;
+        for (int i = 0, k = 0; i < n_rooms; ++i) {
+            const RoomSpec &rm = run->rooms[i];
+            const HostScene &hs = rm.scene->hs;
+            RoomParams &P = rp[i];
+            P.prim_begin = rm.prim_begin;
+            P.prim_end = rm.prim_begin + rm.rays;
+            rprim[i] = rm.prim_begin;
+            P.inv_c_d = 1.0 / hs.c;
+            P.inv_c = (float)(1.0 / hs.c);
+            P.cotime = rm.cotime;
+            P.rho_c = (float)hs.rho_c;
+            for (int o = 0; o < kBands; ++o) P.atten_k[o] = (float)(-0.1 * std::log2(10.0) * hs.atten[o] * hs.c);
+            P.bvh_root = roots[i];
+            P.t_eps = (float)(2e-7 * hs.scale);
+            P.rec_begin = k;
+            P.R = (int)rm.rec.size();
+            for (const pach_receiver_desc &q : rm.rec)
+                rec[k++] = make_float4((float)q.origin[0], (float)q.origin[1], (float)q.origin[2],
+                                       (float)(q.radius * q.radius));
+            P.src_begin = (int)src.size();
+            P.nsrc = (int)rm.src.size();
+            for (const pach_source_desc &s : rm.src) {
+                src.push_back(make_float4((float)s.origin[0], (float)s.origin[1], (float)s.origin[2], (float)s.kind));
+                for (int o = 0; o < kBands; ++o) e0.push_back((float)(1e-12 * std::pow(10.0, .1 * s.power_db[o])));
+            }
+            P.h_oct = rm.h_oct;
+            P.oct_lo = run->p.oct_lo;
+            P.oct_hi = run->p.oct_hi;
+            P.is_order = run->p.is_order;
+            P.pure_specular = run->p.pure_specular;
+            P.max_broad = (int)std::min<unsigned long long>(rm.max_broad, 1u << 30);
+            const unsigned long long per_bounce = (unsigned long long)kBands * ((hs.has_trans && !pure) ? 3 : 1);
+            bound = std::max(bound, per_bounce * rm.max_broad + kBands);
+            ntri_max = std::max(ntri_max, hs.ntri);
+            has_trans = has_trans || hs.has_trans;
+            for (int a = 0; a < 3; ++a) {
+                bmin[a] = std::min(bmin[a], hs.bmin[a]);
+                bmax[a] = std::max(bmax[a], hs.bmax[a]);
+            }
+        }
+        rprim[n_rooms] = rp[n_rooms - 1].prim_end;
+        TRY(upload(run->drec, rec.data(), rec.size() * sizeof(float4)));
         TRY(upload(run->dsrc, src.data(), src.size() * sizeof(float4)));
         TRY(upload(run->de0, e0.data(), e0.size() * sizeof(float)));
+        TRY(upload(run->droom, rp.data(), rp.size() * sizeof(RoomParams)));
+        TRY(upload(run->droomprim, rprim.data(), rprim.size() * sizeof(long long)));
         std::vector<double> gf;
         geodesic_faces(gf);
         std::vector<float4> geo(kGeoFaces * 3);
@@ -189,14 +373,11 @@ void run_worker(pach_run *run) {
         const int threads = run->p.block_threads > 0 ? std::max(32, std::min(256, run->p.block_threads / 32 * 32)) : 256;
         int bps_tr = 0, bps_sh = 0;
         // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
-        const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, (int)hs.tri_poly.size());
+        const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max);
         TRY(wave_kernel_occupancy(tr_variant, threads, (int)sizeof(float4) * std::max(R, 1), &bps_tr, &bps_sh));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
         // ring and wave sizing
-        const bool pure = run->p.pure_specular != 0;
-        const unsigned long long per_bounce = (unsigned long long)kBands * ((hs.has_trans && !pure) ? 3 : 1);
-        const unsigned long long bound = per_bounce * run->max_broad + kBands;
         const int ring_log2 = run->p.ring_log2 > 0 ? std::min(32, std::max(16, run->p.ring_log2)) : 27;
         const unsigned long long ring_cap = 1ull << ring_log2;
         const unsigned long long max_wave = run->p.wave_kilo_items > 0 ? 1024ull * run->p.wave_kilo_items : (1ull << 21);
@@ -216,25 +397,29 @@ void run_worker(pach_run *run) {
             TRY(cudaMemsetAsync(run->sortbins.p, 0, run->sortbins.bytes, stream));
         }
         const int sort_blocks = dev_sms * 4;
+        const bool timing = run->p.kernel_timing != 0;
+        if (!timing) {
+            TRY(cudaHostAlloc(&h_mirror, sizeof(HostMirror), cudaHostAllocMapped));
+            TRY(cudaHostAlloc(&h_cancel, sizeof(int), cudaHostAllocMapped));
+            std::memset(h_mirror, 0, sizeof(HostMirror));
+            *h_cancel = 0;
+        }
 
         DevRun r{};
-        r.S = sc->dev;
+        r.S = S;
+        r.rooms = run->droom.as<RoomParams>();
+        r.room_prim = run->droomprim.as<long long>();
+        r.n_rooms = n_rooms;
         r.rec = run->drec.as<float4>();
         r.R = R;
         r.T = T;
         r.fs = (double)run->p.sample_rate;
-        r.inv_c = (float)(1.0 / hs.c);
-        r.inv_c_d = 1.0 / hs.c;
-        for (int o = 0; o < kBands; ++o) r.atten_k[o] = (float)(-0.1 * std::log2(10.0) * hs.atten[o] * hs.c);
-        r.rho_c = (float)hs.rho_c;
-        r.cotime = run->cotime;
-        r.nsrc = run->nsrc;
         r.src = run->dsrc.as<float4>();
         r.e0 = run->de0.as<float>();
         r.geo = run->dgeo.as<float4>();
         r.prim_dirs = run->prim_dirs.empty() ? nullptr : run->ddirs.as<double>();
         r.prim_weights = run->prim_weights.empty() ? nullptr : run->dw.as<double>();
-        r.prim_base = run->p.ray_begin;
+        r.prim_base = run->rooms[0].prim_begin;
         r.prop = run->prop.empty() ? nullptr : run->dprop.as<float4>();
         r.n_prop = run->prop.empty() ? 0 : run->p.n_proposal;
         r.prop_mix = (float)(run->p.proposal_mix > 0 ? run->p.proposal_mix : 0.3);
@@ -245,14 +430,16 @@ void run_worker(pach_run *run) {
             const double def[3] = {80.0, 400.0, 1200.0};
             for (int i = 0; i < 3; ++i) r.cap_edge[i] = (float)(given ? run->p.capture_edges_ms[i] : def[i]);
         }
-        r.h_oct = run->h_oct;
-        r.oct_lo = run->p.oct_lo;
-        r.oct_hi = run->p.oct_hi;
-        r.is_order = run->p.is_order;
-        r.pure_specular = run->p.pure_specular;
-        r.max_broad = (int)std::min<unsigned long long>(run->max_broad, 1u << 30);
         r.seed = run->p.seed;
         r.max_seg = run->p.max_segments_per_ray > 0 ? run->p.max_segments_per_ray : (1ll << 22);
+        if (!timing) {
+            void *dp = nullptr;
+            TRY(cudaHostGetDevicePointer(&dp, h_mirror, 0));
+            r.mirror = reinterpret_cast<HostMirror *>(dp);
+            TRY(cudaHostGetDevicePointer(&dp, h_cancel, 0));
+            r.cancel = reinterpret_cast<volatile int *>(dp);
+        }
+        r.max_iters = 1ull << 26;
         r.hE = run->hE.as<double>(); r.hP = run->hP.as<double>(); r.hDp = run->hDp.as<double>();
         r.hDn = run->hDn.as<double>(); r.hAn = run->hAn.as<double>();
         r.cnt = run->cnt.as<DevCounters>();
@@ -264,13 +451,13 @@ void run_worker(pach_run *run) {
         r.bin_count = sorting ? run->sortbins.as<unsigned>() : nullptr;
         r.bin_cursor = sorting ? run->sortbins.as<unsigned>() + kSortBins : nullptr;
         for (int k = 0; k < 3; ++k) {
-            r.sort_lo[k] = (float)hs.bmin[k];
-            r.sort_inv[k] = (float)(kSortGrid / (hs.bmax[k] - hs.bmin[k]));
+            r.sort_lo[k] = (float)bmin[k];
+            r.sort_inv[k] = (float)(kSortGrid / std::max(bmax[k] - bmin[k], 1e-9));
         }
         r.max_wave = std::min(max_wave, ring_cap);
         r.feed_bound = bound;
         r.low_water = std::min(ring_cap / 4, 2 * r.max_wave);
-        const long long N = run->p.ray_count;
+        const long long N = rprim[n_rooms] - rprim[0];
         const long long fb_default = std::max<long long>(4096, (long long)(r.max_wave / 32));
         r.feed_batch = run->p.feed_batch > 0 ? run->p.feed_batch : fb_default;
         const int bb_threads = 128;
@@ -278,49 +465,92 @@ void run_worker(pach_run *run) {
                                                                               (long long)dev_sms * 16));
         // initial schedule
         std::memset(h_ctl, 0, sizeof(WaveCtl));
-        h_ctl->next_prim = run->p.ray_begin;
-        h_ctl->prim_end = run->p.ray_begin + N;
-        h_ctl->prim_first = run->p.ray_begin;
+        h_ctl->next_prim = rprim[0];
+        h_ctl->prim_end = rprim[0] + N;
+        h_ctl->prim_first = rprim[0];
         TRY(cudaMemcpyAsync(run->qctl.p, h_ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
-        const bool timing = run->p.kernel_timing != 0;
         double t_trace = 0, t_shade = 0, t_bb = 0, t_sort = 0;
         long long launches = 0;
-        int batch = 8;
         bool cancelled = false;
+        auto one_iteration = [&](int k) -> cudaError_t {
+            cudaError_t x;
+            if ((x = launch_feed(r, stream))) return x;
+            if (timing && (x = cudaEventRecord(kev[6 * k], stream))) return x;
+            if ((x = launch_broadband(r, bb_blocks, bb_threads, stream))) return x;
+            if (timing && (x = cudaEventRecord(kev[6 * k + 1], stream))) return x;
+            if ((x = launch_wave(r, stream))) return x;
+            if (timing && (x = cudaEventRecord(kev[6 * k + 2], stream))) return x;
+            if (sorting && (x = launch_sort(r, sort_blocks, stream))) return x;
+            if (timing && (x = cudaEventRecord(kev[6 * k + 3], stream))) return x;
+            if ((x = launch_trace(r, tr_variant, tr_blocks, threads, stream))) return x;
+            if (timing && (x = cudaEventRecord(kev[6 * k + 4], stream))) return x;
+            if ((x = launch_shade(r, sh_blocks, threads, stream))) return x;
+            if (timing && (x = cudaEventRecord(kev[6 * k + 5], stream))) return x;
+            return cudaSuccess;
+        };
         TRY(cudaEventRecord(ev0, stream));
-        for (long long it = 0; !e; ) {
-            // one batch of iterations, no host synchronisation inside
-            if (timing && kev.size() < (size_t)batch * 6) {
+        if (!timing) {
+            // the whole loop as one graph launch: while (k_cond says so) { one iteration }
+            TRY(cudaGraphCreate(&graph, 0));
+            cudaGraphConditionalHandle handle;
+            TRY(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = handle;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            TRY(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            TRY(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            cudaError_t ce = one_iteration(0);
+            if (ce == cudaSuccess) ce = launch_cond(r, handle, stream);
+            cudaGraph_t captured = nullptr;
+            cudaError_t ee = cudaStreamEndCapture(stream, &captured);
+            TRY(ce);
+            TRY(ee);
+            TRY(cudaGraphInstantiate(&gexec, graph, 0));
+            TRY(cudaGraphLaunch(gexec, stream));
+            TRY(cudaEventRecord(ev1, stream));
+            launches = 6;
+            // poll: progress from the mapped mirror, cancellation through the mapped flag (1: stop
+            // feeding; 2, two seconds later: stop the loop without waiting for the fed primaries)
+            auto t_cancel = std::chrono::steady_clock::now();
+            for (;;) {
+                const cudaError_t q = cudaEventQuery(ev1);
+                run->rays_done = std::max(0ll, (long long)h_mirror->next_prim - rprim[0]);
+                run->end_traces = (long long)h_mirror->end_traces;
+                run->segments = (long long)h_mirror->segments;
+                if (q == cudaSuccess) break;
+                if (q != cudaErrorNotReady) { e = q; where = "graph run"; break; }
+                if (run->cancel && !cancelled) {
+                    cancelled = true;
+                    t_cancel = std::chrono::steady_clock::now();
+                    *reinterpret_cast<volatile int *>(h_cancel) = 1;
+                } else if (cancelled && std::chrono::steady_clock::now() - t_cancel > std::chrono::seconds(2)) {
+                    *reinterpret_cast<volatile int *>(h_cancel) = 2;
+                }
+                std::this_thread::sleep_for(std::chrono::microseconds(500));
+            }
+            if (e) break;
+        } else {
+            int batch = 8;
+            for (long long it = 0; !e;) {
+                // one batch of iterations, no host synchronisation inside
                 while (kev.size() < (size_t)batch * 6) {
                     cudaEvent_t x;
                     TRY(cudaEventCreate(&x));
                     kev.push_back(x);
                 }
                 if (e) break;
-            }
-            for (int k = 0; k < batch && !e; ++k, ++it) {
-                TRY(launch_feed(r, stream));
-                if (timing) TRY(cudaEventRecord(kev[6 * k], stream));
-                TRY(launch_broadband(r, bb_blocks, bb_threads, stream));
-                if (timing) TRY(cudaEventRecord(kev[6 * k + 1], stream));
-                TRY(launch_wave(r, stream));
-                if (timing) TRY(cudaEventRecord(kev[6 * k + 2], stream));
-                if (sorting) {
-                    TRY(launch_sort(r, sort_blocks, stream));
-                    launches += 3;
+                for (int k = 0; k < batch && !e; ++k, ++it) {
+                    TRY(one_iteration(k));
+                    launches += sorting ? 8 : 5;
                 }
-                if (timing) TRY(cudaEventRecord(kev[6 * k + 3], stream));
-                TRY(launch_trace(r, tr_variant, tr_blocks, threads, stream));
-                if (timing) TRY(cudaEventRecord(kev[6 * k + 4], stream));
-                TRY(launch_shade(r, sh_blocks, threads, stream));
-                if (timing) TRY(cudaEventRecord(kev[6 * k + 5], stream));
-                launches += 5;
-            }
-            if (e) break;
-            TRY(cudaMemcpyAsync(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
-            TRY(cudaMemcpyAsync(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost, stream));
-            TRY(cudaStreamSynchronize(stream));
-            if (timing) {
+                if (e) break;
+                TRY(cudaMemcpyAsync(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
+                TRY(cudaMemcpyAsync(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost, stream));
+                TRY(cudaStreamSynchronize(stream));
                 for (int k = 0; k < batch; ++k) {
                     float a = 0, b = 0, c = 0, so = 0;
                     TRY(cudaEventElapsedTime(&a, kev[6 * k], kev[6 * k + 1]));
@@ -333,36 +563,37 @@ void run_worker(pach_run *run) {
                     t_shade += c;
                 }
                 if (e) break;
+                // progress: primaries whose phase A has run
+                run->rays_done = h_ctl->next_prim - rprim[0];
+                run->end_traces = (long long)h_cnt->end_traces;
+                run->segments = (long long)(h_cnt->seg_broad + h_cnt->seg_b + h_cnt->seg_c);
+                if (h_ctl->done) break;
+                if (run->cancel && !cancelled) {
+                    // stop feeding; the primaries already fed run to completion, so the histograms stay
+                    // a consistent estimate over rays_done primaries
+                    cancelled = true;
+                    const long long stop = h_ctl->next_prim;
+                    TRY(cudaMemcpyAsync(&run->qctl.as<WaveCtl>()->prim_end, &stop, sizeof(long long),
+                                        cudaMemcpyHostToDevice, stream));
+                    TRY(cudaStreamSynchronize(stream));
+                }
+                if (batch < 64) batch *= 2;
+                if (it > (1ll << 26)) {
+                    status = PACH_ERR_GAVE_UP;
+                    msg = "wavefront loop did not finish";
+                    final_state = PACH_RUN_FAILED;
+                    break;
+                }
             }
-            // progress: primaries whose phase A has run
-            run->rays_done = h_ctl->next_prim - run->p.ray_begin;
-            run->end_traces = (long long)h_cnt->end_traces;
-            run->segments = (long long)(h_cnt->seg_broad + h_cnt->seg_b + h_cnt->seg_c);
-            if (h_ctl->done) break;
-            if (run->cancel && !cancelled) {
-                // stop feeding; the primaries already fed run to completion, so the histograms stay a
-                // consistent estimate over rays_done primaries
-                cancelled = true;
-                const long long stop = h_ctl->next_prim;
-                TRY(cudaMemcpyAsync(&run->qctl.as<WaveCtl>()->prim_end, &stop, sizeof(long long),
-                                    cudaMemcpyHostToDevice, stream));
-                TRY(cudaStreamSynchronize(stream));
-            }
-            if (batch < 64) batch *= 2;
-            if (it > (1ll << 26)) {
-                status = PACH_ERR_GAVE_UP;
-                msg = "wavefront loop did not finish";
-                final_state = PACH_RUN_FAILED;
-                break;
-            }
+            if (e || status) break;
+            TRY(cudaEventRecord(ev1, stream));
         }
-        if (e || status) break;
-        TRY(cudaEventRecord(ev1, stream));
         TRY(cudaStreamSynchronize(stream));
         float dev_ms = 0.f;
         TRY(cudaEventElapsedTime(&dev_ms, ev0, ev1));
         TRY(cudaMemcpy(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost));
         TRY(cudaMemcpy(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost));
+        const HostScene &hs = sc->hs;
         pach_stats &s = run->stats;
         s.primaries = (int64_t)h_cnt->primaries;
         s.segments_broadband = (int64_t)h_cnt->seg_broad;
@@ -379,9 +610,9 @@ void run_worker(pach_run *run) {
         s.lost_energy = h_cnt->lost_energy;
         s.initial_energy = h_cnt->initial_energy;
         s.percent_lost = s.initial_energy > 0 ? 100.0 * s.lost_energy / s.initial_energy : 0.0;
-        s.h_oct = run->h_oct;
+        s.h_oct = run->rooms[0].h_oct;
         s.bins = T;
-        s.cotime_s = run->cotime;
+        s.cotime_s = run->rooms[0].cotime;
         s.sound_speed = hs.c;
         s.rho_c = hs.rho_c;
         for (int o = 0; o < kBands; ++o) s.air_atten_db_per_m[o] = hs.atten[o];
@@ -391,11 +622,11 @@ void run_worker(pach_run *run) {
         s.broadband_ms = t_bb;
         s.sort_ms = t_sort;
         s.waves = (int64_t)h_ctl->waves;
-        s.kernel_launches = launches;
+        s.kernel_launches = timing ? launches : (long long)h_ctl->iters * (sorting ? 9 : 6);
         s.peak_live_rays = (int64_t)h_ctl->peak_live;
         s.bvh_nodes_visited = (int64_t)h_cnt->bvh_nodes;
         s.tri_tests = (int64_t)h_cnt->tri_tests;
-        s.accel[0] = hs.bvh_nodes;
+        s.accel[0] = (int32_t)(n_rooms > 1 ? run->bbvh.bytes / (kBvhNodeFloats * sizeof(float)) : hs.bvh_nodes);
         s.accel[1] = hs.bvh_leaves;
         s.accel[2] = hs.bvh_depth;
         run->rays_done = (long long)h_cnt->primaries;
@@ -405,6 +636,14 @@ void run_worker(pach_run *run) {
             status = PACH_ERR_BOUNDS;
             msg = "ring queue full: raise ring_log2";
             final_state = PACH_RUN_FAILED;
+        } else if (h_ctl->gave_up == 2) {
+            status = PACH_ERR_CANCELLED;
+            msg = "run cancelled; the loop stopped before every fed primary finished";
+            final_state = PACH_RUN_CANCELLED;
+        } else if (h_ctl->gave_up) {
+            status = PACH_ERR_GAVE_UP;
+            msg = "wavefront loop stopped without finishing (iteration cap or no progress)";
+            final_state = PACH_RUN_FAILED;
         } else if (cancelled) {
             status = PACH_ERR_CANCELLED;
             msg = "run cancelled after " + std::to_string(s.primaries) + " primaries";
@@ -413,20 +652,52 @@ void run_worker(pach_run *run) {
 #undef TRY
     } while (0);
     run->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
     for (cudaEvent_t ev : kev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : {ev0, ev1})
         if (ev) cudaEventDestroy(ev);
     if (h_ctl) cudaFreeHost(h_ctl);
     if (h_cnt) cudaFreeHost(h_cnt);
     if (stream) cudaStreamDestroy(stream);
-    // release the ring; histograms and counters stay until the run is destroyed
-    for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw, &run->sortbins}) m->release();
+    if (h_mirror) cudaFreeHost(h_mirror);
+    if (h_cancel) cudaFreeHost(h_cancel);
+    // release the ring and the batch scene; histograms and counters stay until the run is destroyed
+    for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw, &run->sortbins, &run->btri, &run->btri64,
+                      &run->bnorm, &run->bmat, &run->btrans, &run->bbvh})
+        m->release();
     if (e != cudaSuccess) return finish(PACH_ERR_CUDA, cuda_msg(e, where.c_str()), PACH_RUN_FAILED);
     finish(status, msg, final_state);
 }
 
 pach_status check_run(pach_run *run) {
     if (!run) return fail(PACH_ERR_INVALID_ARGUMENT, "null run handle");
+    return PACH_OK;
+}
+
+// Checks shared by pach_trace_begin and pach_batch_begin: the run-wide parameters and one room's
+// sources and receivers.
+pach_status check_common(const pach_trace_params &p) {
+    if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi) return fail(PACH_ERR_INVALID_ARGUMENT, "octave range must lie in 0..7");
+    if (p.sample_rate < 1) return fail(PACH_ERR_INVALID_ARGUMENT, "sample_rate must be positive");
+    if (p.traversal < 0 || p.traversal > 2) return fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
+    const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
+    if (T < 1 || T > (1ll << 24)) return fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");
+    return PACH_OK;
+}
+
+pach_status check_room(const pach_source_desc *sources, int32_t n_sources, const pach_receiver_desc *receivers,
+                       int32_t n_receivers, const std::string &who) {
+    if (!sources || n_sources < 1 || n_sources > kMaxSources)
+        return fail(PACH_ERR_INVALID_ARGUMENT, who + "need 1.." + std::to_string(kMaxSources) + " sources");
+    if (n_receivers < 0 || (n_receivers > 0 && !receivers)) return fail(PACH_ERR_INVALID_ARGUMENT, who + "bad receivers");
+    for (int i = 0; i < n_receivers; ++i)
+        if (!(receivers[i].radius > 0) || !std::isfinite(receivers[i].origin[0]) || !std::isfinite(receivers[i].origin[1]) ||
+            !std::isfinite(receivers[i].origin[2]))
+            return fail(PACH_ERR_INVALID_ARGUMENT,
+                        who + "receiver " + std::to_string(i) + ": radius must be positive, origin finite");
+    for (int s = 0; s < n_sources; ++s)
+        if (sources[s].kind < 0 || sources[s].kind > 2) return fail(PACH_ERR_INVALID_ARGUMENT, who + "unknown source kind");
     return PACH_OK;
 }
 
@@ -480,54 +751,13 @@ pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
         return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
     }
     cudaGetDevice(&sc->device);
-    const HostScene &hs = sc->hs;
-    std::vector<float4> tri((size_t)hs.ntri * 3);
-    for (int i = 0; i < hs.ntri; ++i) {
-        const double *t = &hs.tri64[9 * (size_t)i];
-        const double ax = t[4] * t[8] - t[5] * t[7], ay = t[5] * t[6] - t[3] * t[8], az = t[3] * t[7] - t[4] * t[6];
-        const double graze = 1e-4 * std::sqrt(ax * ax + ay * ay + az * az);  // |det| < 1e-4 |e1 x e2|: near grazing
-        int plane = hs.tri_plane[i], poly = hs.tri_poly[i];
-        float pw, qw;
-        std::memcpy(&pw, &plane, 4);
-        std::memcpy(&qw, &poly, 4);
-        tri[3 * i] = make_float4((float)t[0], (float)t[1], (float)t[2], pw);
-        tri[3 * i + 1] = make_float4((float)t[3], (float)t[4], (float)t[5], qw);
-        tri[3 * i + 2] = make_float4((float)t[6], (float)t[7], (float)t[8], (float)graze);
-    }
-    std::vector<float4> norm(hs.npoly), mat((size_t)hs.npoly * kBands);
-    std::vector<float> trans((size_t)hs.npoly * kBands);
-    for (int p = 0; p < hs.npoly; ++p) {
-        norm[p] = make_float4((float)hs.normal[3 * p], (float)hs.normal[3 * p + 1], (float)hs.normal[3 * p + 2], 0.f);
-        for (int o = 0; o < kBands; ++o) {
-            // Lambert_Scattering thresholds (Classes_Materials.cs:4466-4485)
-            const double s = hs.scat[p * 8 + o];
-            double lo, hi;
-            if (s < 0.25) { lo = 0.1; hi = 0.4; }
-            else { const double mod = std::fabs(1 - s) / 5; lo = s - mod; hi = s + mod; }
-            mat[p * kBands + o] = make_float4((float)(1.0 - hs.alpha[p * 8 + o]), (float)lo, (float)s, (float)hi);
-            trans[p * kBands + o] = (float)hs.trans[p * 8 + o];
-        }
-    }
-    cudaError_t e;
-    if ((e = upload(sc->tri, tri.data(), tri.size() * sizeof(float4))) ||
-        (e = upload(sc->tri64, hs.tri64.data(), hs.tri64.size() * sizeof(double))) ||
-        (e = upload(sc->norm, norm.data(), norm.size() * sizeof(float4))) ||
-        (e = upload(sc->mat, mat.data(), mat.size() * sizeof(float4))) ||
-        (e = upload(sc->trans, trans.data(), trans.size() * sizeof(float))) ||
-        (e = upload(sc->bvh, hs.bvh.data(), hs.bvh.size() * sizeof(float)))) {
+    SceneArrays A;
+    append_scene(sc->hs, A);
+    const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->dev);
+    if (e != cudaSuccess) {
         delete sc;
         return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
     }
-    DevScene &d = sc->dev;
-    d.tri = sc->tri.as<float4>();
-    d.tri64 = sc->tri64.as<double>();
-    d.pnormal = sc->norm.as<float4>();
-    d.mat = sc->mat.as<float4>();
-    d.trans = sc->trans.as<float>();
-    d.bvh = sc->bvh.as<float4>();
-    d.ntri = hs.ntri;
-    d.t_eps = (float)(2e-7 * hs.scale);
-    d.has_trans = hs.has_trans ? 1 : 0;
     *out = sc;
     return PACH_OK;
 }
@@ -553,26 +783,14 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
     if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
     *out = nullptr;
     if (!scene || !params) return fail(PACH_ERR_INVALID_ARGUMENT, "null scene or params");
-    if (!sources || n_sources < 1 || n_sources > kMaxSources)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "need 1.." + std::to_string(kMaxSources) + " sources");
-    if (n_receivers < 0 || (n_receivers > 0 && !receivers)) return fail(PACH_ERR_INVALID_ARGUMENT, "bad receivers");
+    if (pach_status st = check_room(sources, n_sources, receivers, n_receivers, "")) return st;
     if (n_receivers > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers per run");
     const pach_trace_params &p = *params;
     if (p.ray_count < 1 || p.ray_begin < 0 || p.ray_begin + p.ray_count > (1ll << 32))
         return fail(PACH_ERR_INVALID_ARGUMENT,
                     "ray_count must be >= 1 and ray_begin + ray_count <= 2^32 (convergence mode is not supported)");
-    if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi) return fail(PACH_ERR_INVALID_ARGUMENT, "octave range must lie in 0..7");
-    if (p.sample_rate < 1) return fail(PACH_ERR_INVALID_ARGUMENT, "sample_rate must be positive");
-    if (p.traversal < 0 || p.traversal > 2) return fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
+    if (pach_status st = check_common(p)) return st;
     if (!(p.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, "cutoff_length_m must be positive");
-    const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
-    if (T < 1 || T > (1ll << 24)) return fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");
-    for (int i = 0; i < n_receivers; ++i)
-        if (!(receivers[i].radius > 0) || !std::isfinite(receivers[i].origin[0]) || !std::isfinite(receivers[i].origin[1]) ||
-            !std::isfinite(receivers[i].origin[2]))
-            return fail(PACH_ERR_INVALID_ARGUMENT, "receiver " + std::to_string(i) + ": radius must be positive, origin finite");
-    for (int s = 0; s < n_sources; ++s)
-        if (sources[s].kind < 0 || sources[s].kind > 2) return fail(PACH_ERR_INVALID_ARGUMENT, "unknown source kind");
     if (p.proposal) {
         if (p.n_proposal < 1 || p.n_proposal > 256)
             return fail(PACH_ERR_INVALID_ARGUMENT, "n_proposal must be 1..256 when proposal is given");
@@ -585,50 +803,82 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
     }
     if (p.capture && (p.capture != 1 || n_receivers < 1))
         return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0 or 1 and needs receivers");
-    const HostScene &hs = scene->hs;
-    auto *run = new pach_run();
-    if (p.proposal) proposal_lobes(p.proposal, p.n_proposal, run->prop);
-    run->p.proposal = nullptr;
+    std::unique_ptr<pach_run> run(new pach_run());
     run->scene = scene;
     run->p = p;
-    run->src.assign(sources, sources + n_sources);
-    run->rec.assign(receivers, receivers + n_receivers);
+    if (p.proposal) proposal_lobes(p.proposal, p.n_proposal, run->prop);
     if (p.prim_dirs) run->prim_dirs.assign(p.prim_dirs, p.prim_dirs + 3 * p.ray_count);
     if (p.prim_weights) run->prim_weights.assign(p.prim_weights, p.prim_weights + p.ray_count);
+    run->p.proposal = nullptr;
     run->p.prim_dirs = nullptr;
     run->p.prim_weights = nullptr;
+    RoomSpec rm;
+    rm.scene = scene;
+    rm.src.assign(sources, sources + n_sources);
+    rm.rec.assign(receivers, receivers + n_receivers);
+    rm.rays = p.ray_count;
+    rm.prim_begin = p.ray_begin;
+    rm.cutoff_len = p.cutoff_length_m;  // TaskAll:83 -- the ctor's cutoff argument is a length
+    std::string err;
+    if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
+    run->rooms.push_back(std::move(rm));
     run->R = n_receivers;
-    run->T = (int)T;
     run->nsrc = n_sources;
-    // TaskAll:83 -- the ctor's cutoff argument is a length
-    run->cotime = p.cutoff_length_m / hs.c;
-    // TaskAll:88-109 -- h_oct: least total absorption among bands carrying >= 1e-6 of the peak power
-    // (SourceCluster power = per-band maximum over members, Classes_Sources.cs:680-688)
-    double total_abs[kBands] = {0}, power[kBands] = {0};
-    for (int s = 0; s < n_sources; ++s)
-        for (int o = 0; o < kBands; ++o) power[o] = std::max(power[o], 1e-12 * std::pow(10.0, .1 * sources[s].power_db[o]));
-    for (int q = 0; q < hs.npoly; ++q)
-        for (int o = p.oct_lo; o <= p.oct_hi; ++o) total_abs[o] += hs.area[q] * hs.alpha[q * 8 + o];
-    double mn = HUGE_VAL, octpower = 0;
-    for (int o = p.oct_lo; o <= p.oct_hi; ++o) octpower = std::max(octpower, power[o]);
-    run->h_oct = p.oct_lo;
-    for (int o = p.oct_lo; o <= p.oct_hi; ++o) {
-        if (power[o] < octpower * 1e-6) continue;
-        if (mn > total_abs[o]) { mn = total_abs[o]; run->h_oct = o; }
+    run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
+    run->worker = std::thread(run_worker, run.get());
+    *out = run.release();
+    return PACH_OK;
+}
+
+pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const pach_trace_params *params,
+                             pach_run **out) {
+    if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    if (!rooms || !params || n_rooms < 1 || n_rooms > kMaxRooms)
+        return fail(PACH_ERR_INVALID_ARGUMENT, "need 1.." + std::to_string(kMaxRooms) + " rooms and params");
+    const pach_trace_params &p = *params;
+    if (pach_status st = check_common(p)) return st;
+    if (p.proposal || p.prim_dirs || p.prim_weights)
+        return fail(PACH_ERR_INVALID_ARGUMENT, "a batch emits from its sources: no proposal or emission overrides");
+    if (p.ray_begin < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin must be >= 0");
+    std::unique_ptr<pach_run> run(new pach_run());
+    run->p = p;
+    long long prim = p.ray_begin;
+    int R = 0, nsrc = 0;
+    for (int i = 0; i < n_rooms; ++i) {
+        const pach_room_desc &d = rooms[i];
+        const std::string who = "room " + std::to_string(i) + ": ";
+        if (!d.scene) return fail(PACH_ERR_INVALID_ARGUMENT, who + "null scene");
+        if (d.scene->device != rooms[0].scene->device) return fail(PACH_ERR_INVALID_ARGUMENT, who + "scenes on different devices");
+        if (pach_status st = check_room(d.sources, d.n_sources, d.receivers, d.n_receivers, who)) return st;
+        if (d.ray_count < 1) return fail(PACH_ERR_INVALID_ARGUMENT, who + "ray_count must be >= 1");
+        if (!(d.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, who + "cutoff_length_m must be positive");
+        RoomSpec rm;
+        rm.scene = const_cast<pach_scene *>(d.scene);
+        rm.src.assign(d.sources, d.sources + d.n_sources);
+        rm.rec.assign(d.receivers, d.receivers + d.n_receivers);
+        rm.rays = d.ray_count;
+        rm.prim_begin = prim;
+        rm.cutoff_len = d.cutoff_length_m;
+        std::string err;
+        if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, who + err);
+        prim += d.ray_count;
+        R += d.n_receivers;
+        nsrc += d.n_sources;
+        run->rooms.push_back(std::move(rm));
     }
-    if (p.max_broadband_bounces > 0) {
-        run->max_broad = (unsigned long long)p.max_broadband_bounces;
-    } else {
-        run->max_broad = derived_broadband_bound(hs, run->h_oct, p.pure_specular != 0);
-        if (run->max_broad == 0) {
-            delete run;
-            return fail(PACH_ERR_INVALID_ARGUMENT,
-                        "a surface reflects band h_oct without loss: the broadband loop would not terminate; "
-                        "set max_broadband_bounces");
-        }
-    }
-    run->worker = std::thread(run_worker, run);
-    *out = run;
+    if (prim > (1ll << 32)) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin + the rooms' rays must be <= 2^32");
+    if (R > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers over the rooms of a batch");
+    if (p.capture && (p.capture != 1 || R < 1))
+        return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0 or 1 and needs receivers");
+    run->scene = run->rooms[0].scene;
+    run->p.ray_count = prim - p.ray_begin;
+    run->p.cutoff_length_m = run->rooms[0].cutoff_len;
+    run->R = R;
+    run->nsrc = nsrc;
+    run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
+    run->worker = std::thread(run_worker, run.get());
+    *out = run.release();
     return PACH_OK;
 }
 
@@ -678,19 +928,28 @@ pach_status pach_trace_get_histograms(pach_run *run, int32_t scaled, double *ene
     const size_t nE = (size_t)run->R * kBands * run->T, nD = nE * 3;
     if (cap_bins < nE) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < receivers * 8 * bins");
     cudaSetDevice(run->scene->device);
-    const double N = (double)std::max<long long>(1, run->rays_done.load());
-    const double ns = (double)run->nsrc;
-    // Receiver_Bank.Scale(N) then, for a cluster, Scale(1/n_sources) (TaskAll:770-771)
-    const double fE = ns / N, fP = std::sqrt(ns) / std::sqrt(N);
-    struct Item { double *dst; DevMem *src; size_t n; double f; };
-    const Item items[5] = {{energy, &run->hE, nE, fE}, {pressure, &run->hP, nE, fP}, {dir_pos, &run->hDp, nD, fE},
-                           {dir_neg, &run->hDn, nD, fE}, {analysis, &run->hAn, nD, fE}};
+    struct Item { double *dst; DevMem *src; size_t n; int lanes; bool pressure; };
+    const Item items[5] = {{energy, &run->hE, nE, 1, false}, {pressure, &run->hP, nE, 1, true},
+                           {dir_pos, &run->hDp, nD, 3, false}, {dir_neg, &run->hDn, nD, 3, false},
+                           {analysis, &run->hAn, nD, 3, false}};
+    const long long done = run->rays_done.load();
     for (const Item &it : items) {
         if (!it.dst || it.n == 0) continue;
         cudaError_t e = cudaMemcpy(it.dst, it.src->p, it.n * sizeof(double), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "histogram copy"));
-        if (scaled)
-            for (size_t i = 0; i < it.n; ++i) it.dst[i] *= it.f;
+        if (!scaled) continue;
+        // Receiver_Bank.Scale(N) then, for a cluster, Scale(1/n_sources) (TaskAll:770-771), with N the
+        // primaries the receiver's room completed (rooms are fed in order)
+        const size_t per_rec = (size_t)it.lanes * kBands * run->T;
+        double *dst = it.dst;
+        for (const RoomSpec &rm : run->rooms) {
+            const long long off = rm.prim_begin - run->rooms[0].prim_begin;
+            const double N = (double)std::max(1ll, std::min(rm.rays, done - off));
+            const double ns = (double)rm.src.size();
+            const double f = it.pressure ? std::sqrt(ns) / std::sqrt(N) : ns / N;
+            for (size_t i = 0; i < rm.rec.size() * per_rec; ++i) dst[i] *= f;
+            dst += rm.rec.size() * per_rec;
+        }
     }
     return PACH_OK;
 }
@@ -793,16 +1052,19 @@ pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, in
     geodesic_faces(gf);
     std::vector<float4> geo(kGeoFaces * 3);
     for (int i = 0; i < kGeoFaces * 3; ++i) geo[i] = make_float4((float)gf[3 * i], (float)gf[3 * i + 1], (float)gf[3 * i + 2], 0.f);
-    DevMem ds, dg, dout;
+    DevMem ds, dg, dout, droom;
     cudaError_t e;
     DevRun r{};
     r.seed = seed;
-    r.nsrc = n_sources;
+    RoomParams room{};
+    room.nsrc = n_sources;
     if ((e = upload(ds, src.data(), src.size() * sizeof(float4))) || (e = upload(dg, geo.data(), geo.size() * sizeof(float4))) ||
-        (e = dout.alloc(sizeof(double) * 3 * n)))
+        (e = upload(droom, &room, sizeof(room))) || (e = dout.alloc(sizeof(double) * 3 * n)))
         return fail(PACH_ERR_CUDA, cuda_msg(e, "emit setup"));
     r.src = ds.as<float4>();
     r.geo = dg.as<float4>();
+    r.rooms = droom.as<RoomParams>();
+    r.n_rooms = 1;
     if ((e = launch_emit(r, ray_begin, n, dout.as<double>(), 0)) ||
         (e = cudaMemcpy(dirs_out, dout.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost)))
         return fail(PACH_ERR_CUDA, cuda_msg(e, "emit"));
@@ -827,7 +1089,6 @@ pach_status pach_proposal_sample(const float *proposal, int32_t n_prop, double m
         return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample setup"));
     DevRun r{};
     r.seed = seed;
-    r.nsrc = 1;
     r.prop = dl.as<float4>();
     r.n_prop = n_prop;
     r.prop_mix = (float)(mix > 0 ? mix : 0.3);

@@ -111,8 +111,8 @@ struct TraceWork {
 };
 
 // One candidate triangle: FP32 Moller-Trumbore, FP64 re-test inside the epsilon band.
-__device__ __forceinline__ void test_tri(const DevScene &S, int i, float3 o, float3 d, int skip, float &best, int &bi,
-                                         TraceWork &w) {
+__device__ __forceinline__ void test_tri(const DevScene &S, float t_eps, int i, float3 o, float3 d, int skip,
+                                         float &best, int &bi, TraceWork &w) {
     const float4 A = __ldg(S.tri + 3 * i);
     if (__float_as_int(A.w) == skip) return;
     const float4 B = __ldg(S.tri + 3 * i + 1);
@@ -131,14 +131,14 @@ __device__ __forceinline__ void test_tri(const DevScene &S, int i, float3 o, flo
     if (grazing || !(fabsf(margin) > kBaryEps)) {
         // near grazing, near an edge, or not finite: decide in FP64.  Away from grazing the FP32
         // distance is accurate, so a candidate well outside (t_eps, best) needs no re-test.
-        if (!grazing && isfinite(t) && (t < 0.5f * S.t_eps || t > 1.0001f * best)) return;
+        if (!grazing && isfinite(t) && (t < 0.5f * t_eps || t > 1.0001f * best)) return;
         double td;
         ++w.retests;
         if (retest64(S, i, o, d, td)) {
             const float tf = (float)td;
-            if (tf > S.t_eps && tf < best) { best = tf; bi = i; }
+            if (tf > t_eps && tf < best) { best = tf; bi = i; }
         }
-    } else if (margin > 0.f && t > S.t_eps && t < best) {
+    } else if (margin > 0.f && t > t_eps && t < best) {
         best = t;
         bi = i;
     }
@@ -193,8 +193,8 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
 // Nearest hit along o + t d with t > t_eps, skipping triangles of plane `skip` (the surface the ray
 // leaves).  4-wide BVH, nearest-child-first walk with a per-thread stack of the other hit
 // children; a child box is entered only if the ray meets it before the best hit so far.
-__device__ __forceinline__ bool trace_ray(const DevScene &S, float3 o, float3 d, int skip, float &t_best,
-                                          int &tri_best, TraceWork &w) {
+__device__ __forceinline__ bool trace_ray(const DevScene &S, int root, float t_eps, float3 o, float3 d, int skip,
+                                          float &t_best, int &tri_best, TraceWork &w) {
     const float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
     const float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
     const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
@@ -202,7 +202,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, float3 o, float3 d,
     const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
     int stack[kBvhStack];
     int sp = 0;
-    int node = 0;
+    int node = root;
     float best = FLT_MAX;
     int bi = -1;
     for (;;) {
@@ -222,7 +222,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, float3 o, float3 d,
         const int code = ~node;
         const int f0 = code >> 4, cnt = (code & 15) + 1;
         w.tris += (unsigned)cnt;
-        for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+        for (int k = 0; k < cnt; ++k) test_tri(S, t_eps, f0 + k, o, d, skip, best, bi, w);
         if (sp == 0) break;
         node = stack[--sp];
     }
@@ -252,10 +252,11 @@ __device__ __forceinline__ bool sphere_hit(float4 c, float3 o, float3 d, float t
 }
 
 // Directional_Histogram.Add (Classes_Receivers.cs:1813-1825) + Reflection_Analysis_Data.
-__device__ __forceinline__ void hist_add(const DevRun &r, int k, int oct, long long bin, float e, float3 d, int kind) {
+__device__ __forceinline__ void hist_add(const DevRun &r, float rho_c, int k, int oct, long long bin, float e, float3 d,
+                                         int kind) {
     const size_t base = ((size_t)k * kBands + oct) * r.T + bin;
     atomicAdd(r.hE + base, (double)e);
-    atomicAdd(r.hP + base, (double)sqrtf(e * r.rho_c));
+    atomicAdd(r.hP + base, (double)sqrtf(e * rho_c));
     const float ca[3] = {-d.x, -d.y, -d.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -265,49 +266,51 @@ __device__ __forceinline__ void hist_add(const DevRun &r, int k, int oct, long l
     atomicAdd(r.hAn + (((size_t)k * 3 + kind) * kBands + oct) * r.T + bin, (double)e);
 }
 
-__device__ __forceinline__ void capture_add(const DevRun &r, const float4 *rec, int k, uint32_t prim, double time,
-                                            float e);
+__device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, const float4 *rec, int k,
+                                            uint32_t prim, double time, float e);
 
-// Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half.
-__device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
-                                                  double t_sum, float Iabs, int oct, int mask, uint32_t prim) {
+// Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half,
+// over the receivers of the ray's room (rec: the run's receiver table in shared memory).
+__device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomParams &P, const float4 *rec, float3 o,
+                                                  float3 d, float tseg, double t_sum, float Iabs, int oct, int mask,
+                                                  uint32_t prim) {
     uint32_t n = 0;
-    for (int k = 0; k < r.R; ++k) {
+    for (int k = P.rec_begin; k < P.rec_begin + P.R; ++k) {
         float t, half;
         if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
         ++n;
-        const double time = t_sum + (double)(t * r.inv_c);
+        const double time = t_sum + (double)(t * P.inv_c);
         const long long bin = (long long)(time * r.fs);
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
-        const float e = Iabs * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
-        hist_add(r, k, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
-        if (r.capture) capture_add(r, rec, k, prim, time, e);
+        const float e = Iabs * exp2f(P.atten_k[oct] * (float)time) * kInvPi * half;
+        hist_add(r, P.rho_c, k, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
+        if (r.capture) capture_add(r, P, rec, k, prim, time, e);
     }
     return n;
 }
 
 // Spherical_Receiver.CheckBroadbandRay (Classes_Receivers.cs:803-829): every band of the range,
 // analysis bin 0 (specular).
-__device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const float4 *rec, float3 o, float3 d, float tseg,
-                                                 double t_sum, const float (&E)[kBands], const float (&sc)[kBands],
-                                                 uint32_t prim) {
+__device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomParams &P, const float4 *rec, float3 o,
+                                                 float3 d, float tseg, double t_sum, const float (&E)[kBands],
+                                                 const float (&sc)[kBands], uint32_t prim) {
     uint32_t n = 0;
-    for (int k = 0; k < r.R; ++k) {
+    for (int k = P.rec_begin; k < P.rec_begin + P.R; ++k) {
         float t, half;
         if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
         ++n;
-        const double time = t_sum + (double)(t * r.inv_c);
+        const double time = t_sum + (double)(t * P.inv_c);
         const long long bin = (long long)(time * r.fs);
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
         float esum = 0.f;
 #pragma unroll
         for (int oct = 0; oct < kBands; ++oct) {
-            if (oct < r.oct_lo || oct > r.oct_hi) continue;
-            const float e = E[oct] * sc[oct] * exp2f(r.atten_k[oct] * (float)time) * kInvPi * half;
-            hist_add(r, k, oct, bin, e, d, 0);
+            if (oct < P.oct_lo || oct > P.oct_hi) continue;
+            const float e = E[oct] * sc[oct] * exp2f(P.atten_k[oct] * (float)time) * kInvPi * half;
+            hist_add(r, P.rho_c, k, oct, bin, e, d, 0);
             esum += e;
         }
-        if (r.capture) capture_add(r, rec, k, prim, time, esum);
+        if (r.capture) capture_add(r, P, rec, k, prim, time, esum);
     }
     return n;
 }
@@ -315,7 +318,7 @@ __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const float4 *
 // ------------------------------------------------------------------------------------------
 // emission
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ float3 emit_dir(const DevRun &r, long long prim, int kind) {
+__device__ __forceinline__ float3 emit_dir(const DevRun &r, int nsrc, long long prim, int kind) {
     const float4 U = draw(r.seed, (uint32_t)prim, 0ull, 0u);
     if (kind == PACH_SOURCE_RANDOM) {  // RandomSource (Classes_Sources.cs:256-265)
         float st, ct, sp, cp;
@@ -331,7 +334,7 @@ __device__ __forceinline__ float3 emit_dir(const DevRun &r, long long prim, int 
         return make_float3(rr * cp, rr * sp, z);
     }
     // GeodesicSource (Classes_Sources.cs:390-403): face (per-source ray count) mod 80, point on face
-    const long long j = prim / r.nsrc;
+    const long long j = prim / nsrc;
     const int f = (int)(j % kGeoFaces);
     float u = U.x, v = U.y;
     if (u + v > 1.f) { u = 1.f - u; v = 1.f - v; }
@@ -389,7 +392,7 @@ __device__ __forceinline__ float3 proposal_dir(const DevRun &r, uint32_t prim, f
 }
 
 // Emission direction of primary prim and its weight (1 unless importance sampled).
-__device__ __forceinline__ float3 primary_dir(const DevRun &r, uint32_t prim, int kind, float &w) {
+__device__ __forceinline__ float3 primary_dir(const DevRun &r, int nsrc, uint32_t prim, int kind, float &w) {
     w = 1.f;
     if (r.prim_dirs) {
         const double *pd = r.prim_dirs + 3 * ((long long)prim - r.prim_base);
@@ -398,20 +401,20 @@ __device__ __forceinline__ float3 primary_dir(const DevRun &r, uint32_t prim, in
     }
     if (r.prop) return proposal_dir(r, prim, w);
     if (r.prim_weights) w = (float)r.prim_weights[(long long)prim - r.prim_base];
-    return emit_dir(r, prim, kind);
+    return emit_dir(r, nsrc, prim, kind);
 }
 
 // Training capture: energy e detected at receiver k at time (s) from primary prim, added to the bin
 // of the primary's emission direction in the window of (time - direct arrival).
-__device__ __forceinline__ void capture_add(const DevRun &r, const float4 *rec, int k, uint32_t prim, double time,
-                                            float e) {
-    const int s = (int)((prim + 1ull) % (unsigned long long)r.nsrc);
+__device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, const float4 *rec, int k,
+                                            uint32_t prim, double time, float e) {
+    const int s = P.src_begin + (int)((prim + 1ull) % (unsigned long long)P.nsrc);
     const float4 src = r.src[s];
     float w;
-    const float3 d0 = primary_dir(r, prim, (int)src.w, w);
+    const float3 d0 = primary_dir(r, P.nsrc, prim, (int)src.w, w);
     const int b = dir_bin(d0.x, d0.y, d0.z);
     const double dx = rec[k].x - src.x, dy = rec[k].y - src.y, dz = rec[k].z - src.z;
-    const float ms = (float)((time - sqrt(dx * dx + dy * dy + dz * dz) * r.inv_c_d) * 1000.0);
+    const float ms = (float)((time - sqrt(dx * dx + dy * dy + dz * dz) * P.inv_c_d) * 1000.0);
     const int win = (ms >= r.cap_edge[0]) + (ms >= r.cap_edge[1]) + (ms >= r.cap_edge[2]);
     atomicAdd(r.capture + ((size_t)k * kCaptureWindows + win) * kDirBins + b, e);
 }
@@ -425,7 +428,7 @@ struct Ray {
     double t_sum;
     uint32_t prim, nb;
     unsigned long long sid;
-    int oct, mask, phase, plane;
+    int oct, mask, phase, plane, room;
 };
 
 __device__ __forceinline__ ORayItem to_item(const Ray &R) {
@@ -433,7 +436,7 @@ __device__ __forceinline__ ORayItem to_item(const Ray &R) {
     it.px = R.p.x; it.py = R.p.y; it.pz = R.p.z; it.I = R.I;
     it.dx = R.d.x; it.dy = R.d.y; it.dz = R.d.z; it.scale = R.scale;
     it.t_sum = R.t_sum; it.prim = R.prim; it.nb = R.nb; it.sid = R.sid;
-    it.meta = (uint32_t)R.oct | ((uint32_t)R.mask << 3) | ((uint32_t)R.phase << 5);
+    it.meta = (uint32_t)R.oct | ((uint32_t)R.mask << 3) | ((uint32_t)R.phase << 5) | ((uint32_t)R.room << 6);
     it.plane = R.plane;
     return it;
 }
@@ -444,16 +447,28 @@ __device__ __forceinline__ Ray to_ray(const ORayItem &it) {
     R.d = make_float3(it.dx, it.dy, it.dz);
     R.I = it.I; R.scale = it.scale; R.t_sum = it.t_sum; R.prim = it.prim; R.nb = it.nb; R.sid = it.sid;
     R.oct = (int)(it.meta & 7u); R.mask = (int)((it.meta >> 3) & 3u); R.phase = (int)((it.meta >> 5) & 1u);
+    R.room = (int)(it.meta >> 6);
     R.plane = it.plane;
     return R;
 }
 
 __device__ __forceinline__ Ray new_ray(float3 p, float3 d, float I, float scale, double t_sum, uint32_t prim,
-                                       unsigned long long sid, int oct, int mask, int plane) {
+                                       unsigned long long sid, int oct, int mask, int plane, int room) {
     Ray R;
     R.p = p; R.d = d; R.I = I; R.scale = scale; R.t_sum = t_sum; R.prim = prim; R.nb = 0; R.sid = sid;
-    R.oct = oct; R.mask = mask; R.phase = 0; R.plane = plane;
+    R.oct = oct; R.mask = mask; R.phase = 0; R.plane = plane; R.room = room;
     return R;
+}
+
+// Room of a primary: the last room whose first primary is <= prim (binary search of room_prim).
+__device__ __forceinline__ int room_of(const DevRun &r, long long prim) {
+    int lo = 0, hi = r.n_rooms - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(r.room_prim + mid) <= prim) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // Reserves n consecutive queue slots only if they all fit; bounded retries under contention.

@@ -63,7 +63,7 @@ struct __align__(16) ORayItem {
     uint32_t prim;              // primary ray index
     uint32_t nb;                // draw blocks used on this stream
     unsigned long long sid;     // stream identity in the split tree
-    uint32_t meta;              // bits 0-2 band, 3-4 Scatter_Mask, 5 phase (0 B, 1 C)
+    uint32_t meta;              // bits 0-2 band, 3-4 Scatter_Mask, 5 phase (0 B, 1 C), 6-31 room
     int32_t plane;              // coplanar group of the surface the ray leaves (-1 none)
 };
 
@@ -85,34 +85,58 @@ struct WaveCtl {
     unsigned long long per_prim;    // peak ring footprint per primary measured by the pilot batch (0 = not yet)
     unsigned long long trace_next;  // next wave item a trace thread takes (dynamic fetch)
     unsigned long long last_live;   // live count at the previous feed decision
-    int done, pad;
+    unsigned long long iters;       // loop iterations run (graph mode)
+    unsigned long long idle;        // consecutive iterations that neither traced nor fed
+    int done, gave_up;
 };
+
+// Progress mirror in mapped host memory, written by the device every iteration in graph mode.
+struct HostMirror {
+    long long next_prim;
+    unsigned long long iters, segments, end_traces;
+    int done, gave_up;
+};
+
+// One room of a run (a plain run is a batch of one room).  Rooms share the run's device scene (the
+// concatenation of their scenes), receiver, source and histogram tables; a room owns the ranges below.
+struct RoomParams {
+    long long prim_begin, prim_end;  // its primaries in the run's global primary numbering
+    double inv_c_d, cotime;          // 1 / c, COTime = cutoff length / c (s)
+    float inv_c, rho_c;
+    float atten_k[kBands];           // exp2 factor per second of travel: -0.1 log2(10) m c
+    float t_eps;                     // smallest hit distance (2e-7 x the room's scale)
+    int bvh_root;                    // root node of its BVH in the run's node array
+    int rec_begin, R;                // its receivers [rec_begin, rec_begin + R) (run-wide receiver index)
+    int src_begin, nsrc;             // its sources
+    int h_oct, oct_lo, oct_hi, is_order, pure_specular, max_broad;
+};
+constexpr int kMaxRooms = 4096;
 
 constexpr long long kPilotPrimaries = 256;
 
 // Launch-wide parameters (kernel argument).
 struct DevRun {
     DevScene S;
-    // receivers
+    // rooms: room i holds primaries [room_prim[i], room_prim[i + 1])
+    const RoomParams *rooms;    // [n_rooms]
+    const long long *room_prim; // [n_rooms + 1]
+    int n_rooms;
+    // receivers of every room
     const float4 *rec;          // [R] (x, y, z, r^2)
     int R, T;
     double fs;                  // histogram rate (Hz)
-    float inv_c;
-    double inv_c_d;
-    float atten_k[kBands];      // exp2 factor per second of travel: -0.1 log2(10) m c
-    float rho_c;
-    double cotime;
-    // sources
-    int nsrc;
-    const float4 *src;          // [nsrc] origin (w = kind)
-    const float *e0;            // [nsrc*8] band powers (W)
+    // sources of every room
+    const float4 *src;          // [sources] origin (w = kind)
+    const float *e0;            // [sources*8] band powers (W)
     const float4 *geo;          // [80*3] geodesic face vertices
     const double *prim_dirs;    // optional, indexed by prim - prim_base
     const double *prim_weights;
     long long prim_base;
-    int h_oct, oct_lo, oct_hi, is_order, pure_specular, max_broad;
     unsigned long long seed;
     long long max_seg;
+    volatile int *cancel;       // mapped host flag: stop feeding (graph mode; null otherwise)
+    HostMirror *mirror;         // mapped host progress (graph mode; null otherwise)
+    unsigned long long max_iters;  // graph mode: iteration cap
     // outputs
     double *hE, *hP, *hDp, *hDn, *hAn;
     DevCounters *cnt;
@@ -179,6 +203,7 @@ constexpr int kSortBins = 8 * kSortGrid * kSortGrid * kSortGrid;  // x 8 directi
 //   feed (1 thread) -> broadband (phase A of the fed primaries) -> wave (1 thread: size the wave)
 //   -> trace (BVH walk of every ray of the wave) -> shade (detect, absorb, scatter, append).
 cudaError_t launch_feed(const DevRun &r, cudaStream_t s);
+cudaError_t launch_cond(const DevRun &r, cudaGraphConditionalHandle h, cudaStream_t s);
 cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s);
 cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count -> scan -> scatter

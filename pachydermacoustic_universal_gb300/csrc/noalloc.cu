@@ -32,7 +32,9 @@ constexpr size_t kOffRec = align256(kOffCnt + sizeof(DevCounters));
 constexpr size_t kOffSrc = align256(kOffRec + kNaMaxReceivers * sizeof(float4));
 constexpr size_t kOffE0 = align256(kOffSrc + kNaMaxSources * sizeof(float4));
 constexpr size_t kOffGeo = align256(kOffE0 + kNaMaxSources * kBands * sizeof(float));
-constexpr size_t kScratchBytes = align256(kOffGeo + kGeoFaces * 3 * sizeof(float4));  // ~4.6 MB
+constexpr size_t kOffRoom = align256(kOffGeo + kGeoFaces * 3 * sizeof(float4));
+constexpr size_t kOffRoomPrim = align256(kOffRoom + sizeof(RoomParams));
+constexpr size_t kScratchBytes = align256(kOffRoomPrim + 2 * sizeof(long long));  // ~4.6 MB
 
 // The working memory of every pach_trace_run_noalloc call on this device.  It is resident on each
 // GPU that loads the library until the process exits.  In host code the name stands for a
@@ -160,6 +162,29 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         NA_TRY(cudaMemcpyAsync(base + kOffSrc, src, n_sources * sizeof(float4), cudaMemcpyHostToDevice, stream));
         NA_TRY(cudaMemcpyAsync(base + kOffE0, e0, n_sources * kBands * sizeof(float), cudaMemcpyHostToDevice, stream));
         NA_TRY(cudaMemcpyAsync(base + kOffGeo, geo, sizeof(geo), cudaMemcpyHostToDevice, stream));
+        RoomParams room{};
+        room.prim_begin = p.ray_begin;
+        room.prim_end = p.ray_begin + p.ray_count;
+        room.inv_c = (float)(1.0 / hs.c);
+        room.inv_c_d = 1.0 / hs.c;
+        for (int o = 0; o < kBands; ++o) room.atten_k[o] = (float)(-0.1 * std::log2(10.0) * hs.atten[o] * hs.c);
+        room.rho_c = (float)hs.rho_c;
+        room.cotime = p.cutoff_length_m / hs.c;
+        room.bvh_root = 0;
+        room.t_eps = (float)(2e-7 * hs.scale);
+        room.rec_begin = 0;
+        room.R = n_receivers;
+        room.src_begin = 0;
+        room.nsrc = n_sources;
+        room.h_oct = h_oct;
+        room.oct_lo = p.oct_lo;
+        room.oct_hi = p.oct_hi;
+        room.is_order = p.is_order;
+        room.pure_specular = p.pure_specular;
+        room.max_broad = (int)std::fmin((double)max_broad, (double)(1u << 30));
+        const long long room_prim[2] = {room.prim_begin, room.prim_end};
+        NA_TRY(cudaMemcpyAsync(base + kOffRoom, &room, sizeof(room), cudaMemcpyHostToDevice, stream));
+        NA_TRY(cudaMemcpyAsync(base + kOffRoomPrim, room_prim, sizeof(room_prim), cudaMemcpyHostToDevice, stream));
         NA_TRY(cudaMemcpyAsync(base + kOffCtl, &h_ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
         NA_TRY(cudaMemsetAsync(base + kOffCnt, 0, sizeof(DevCounters), stream));
         NA_TRY(cudaMemsetAsync(d_energy, 0, nE * sizeof(double), stream));
@@ -174,22 +199,13 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         r.R = n_receivers;
         r.T = (int)T;
         r.fs = (double)p.sample_rate;
-        r.inv_c = (float)(1.0 / hs.c);
-        r.inv_c_d = 1.0 / hs.c;
-        for (int o = 0; o < kBands; ++o) r.atten_k[o] = (float)(-0.1 * std::log2(10.0) * hs.atten[o] * hs.c);
-        r.rho_c = (float)hs.rho_c;
-        r.cotime = p.cutoff_length_m / hs.c;
-        r.nsrc = n_sources;
+        r.rooms = reinterpret_cast<const RoomParams *>(base + kOffRoom);
+        r.room_prim = reinterpret_cast<const long long *>(base + kOffRoomPrim);
+        r.n_rooms = 1;
         r.src = reinterpret_cast<const float4 *>(base + kOffSrc);
         r.e0 = reinterpret_cast<const float *>(base + kOffE0);
         r.geo = reinterpret_cast<const float4 *>(base + kOffGeo);
         r.prim_base = p.ray_begin;
-        r.h_oct = h_oct;
-        r.oct_lo = p.oct_lo;
-        r.oct_hi = p.oct_hi;
-        r.is_order = p.is_order;
-        r.pure_specular = p.pure_specular;
-        r.max_broad = (int)std::fmin((double)max_broad, (double)(1u << 30));
         r.seed = p.seed;
         r.max_seg = p.max_segments_per_ray > 0 ? p.max_segments_per_ray : (1ll << 22);
         r.hE = d_energy; r.hP = d_pressure; r.hDp = d_dir_pos; r.hDn = d_dir_neg; r.hAn = d_analysis;
@@ -249,7 +265,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
             stats->percent_lost = c.initial_energy > 0 ? 100.0 * c.lost_energy / c.initial_energy : 0.0;
             stats->h_oct = h_oct;
             stats->bins = (int32_t)T;
-            stats->cotime_s = r.cotime;
+            stats->cotime_s = room.cotime;
             stats->sound_speed = hs.c;
             stats->rho_c = hs.rho_c;
             for (int o = 0; o < kBands; ++o) stats->air_atten_db_per_m[o] = hs.atten[o];

@@ -64,6 +64,8 @@ __global__ void k_feed(DevRun r) {
     c->m = 0;
     c->pa_count = 0;
     if (c->done) return;
+    // cancellation (graph mode): stop feeding; the primaries already fed run to completion
+    if (r.cancel && *r.cancel && c->prim_end > c->next_prim) c->prim_end = c->next_prim;
     const unsigned long long live = c->tail - c->head;
     const long long fed = c->next_prim - c->prim_first;
     if (c->per_prim == 0 && fed >= kPilotPrimaries) {
@@ -113,6 +115,38 @@ __global__ void k_wave(DevRun r) {
     if (live > 0 && m == 0) { ++c->overflow; c->done = 1; }  // ring full: cannot make progress
 }
 
+// Last node of a graph-mode iteration: decides whether the while loop runs again.  The loop ends
+// when the run is done, and also -- as a failure -- after max_iters iterations or 4096 consecutive
+// iterations that neither traced nor fed, so it always terminates.  Progress goes to mapped host
+// memory for the polling host thread.
+__global__ void k_cond(DevRun r, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    WaveCtl *c = r.ctl;
+    ++c->iters;
+    if (c->m == 0 && c->pa_count == 0 && !c->done) ++c->idle;
+    else c->idle = 0;
+    bool stop = c->done != 0;
+    if (!stop && (c->iters >= r.max_iters || c->idle >= 4096)) {
+        c->gave_up = 1;
+        stop = true;
+    }
+    if (!stop && r.cancel && *r.cancel >= 2) {  // abort: the host stops waiting for fed primaries
+        c->gave_up = 2;
+        stop = true;
+    }
+    if (r.mirror) {
+        HostMirror *hm = r.mirror;
+        hm->next_prim = c->next_prim;
+        hm->iters = c->iters;
+        hm->segments = r.cnt->seg_broad + r.cnt->seg_b + r.cnt->seg_c;
+        hm->end_traces = r.cnt->end_traces;
+        hm->gave_up = c->gave_up;
+        __threadfence_system();
+        hm->done = stop ? 1 : 0;
+    }
+    cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
 // ------------------------------------------------------------------------------------------
 // phase A: broadband rays (cast_ray_distributed, TaskAll:347-424)
 // ------------------------------------------------------------------------------------------
@@ -126,10 +160,13 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += stride) {
         const long long prim = p0 + i;
-        const int s = (int)((prim + 1) % r.nsrc);  // SourceCluster round robin (Classes_Sources.cs:712-722)
+        const int room = room_of(r, prim);
+        const RoomParams &P = r.rooms[room];
+        // SourceCluster round robin (Classes_Sources.cs:712-722)
+        const int s = P.src_begin + (int)((prim + 1) % P.nsrc);
         const float4 src = r.src[s];
         float w;
-        float3 d = primary_dir(r, (uint32_t)prim, (int)src.w, w);
+        float3 d = primary_dir(r, P.nsrc, (uint32_t)prim, (int)src.w, w);
         float E[kBands], sc[kBands];
 #pragma unroll
         for (int o = 0; o < kBands; ++o) {
@@ -146,18 +183,18 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             float t;
             int tri;
             TraceWork tw;
-            const bool hit = trace_ray(S, pos, d, plane, t, tri, tw);
+            const bool hit = trace_ray(S, P.bvh_root, P.t_eps, pos, d, plane, t, tri, tw);
             L.v[C_RET] += tw.retests;
             ++L.v[C_SEGA];
             if (!hit) {
-                if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
+                if (order > P.is_order) L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
 #pragma unroll
                 for (int o = 0; o < kBands; ++o) L.lost += (double)(E[o] * sc[o]);
                 lost = true;
                 break;
             }
-            if (order > r.is_order) L.v[C_DET] += detect_broad(r, s_rec, pos, d, t, t_sum, E, sc, (uint32_t)prim);
-            t_sum += (double)t * r.inv_c_d;
+            if (order > P.is_order) L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, t, t_sum, E, sc, (uint32_t)prim);
+            t_sum += (double)t * P.inv_c_d;
             pos = pos + d * t;
             const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
             plane = __float_as_int(A.w);
@@ -170,8 +207,8 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             for (int o = 0; o < kBands; ++o) {
                 const float4 m = __ldg(S.mat + poly * kBands + o);
                 E[o] *= m.x;  // Basic_Material.Absorb
-                smid[o] = r.pure_specular ? 0.f : m.z;
-                tau[o] = (S.has_trans && !r.pure_specular) ? __ldg(S.trans + poly * kBands + o) : 0.f;
+                smid[o] = P.pure_specular ? 0.f : m.z;
+                tau[o] = (S.has_trans && !P.pure_specular) ? __ldg(S.trans + poly * kBands + o) : 0.f;
             }
             // Scatter_Early
             if (cos_t > 0.f) { n = n * -1.f; cos_t = -cos_t; }
@@ -182,12 +219,14 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
 #pragma unroll
             for (int o = 0; o < kBands; ++o) {
                 if (E[o] == 0.f) continue;
-                Ray ch = new_ray(pos, d, E[o] * smid[o], sc[o], t_sum, (uint32_t)prim, sid_early(k, o, 0), o, 3, plane);
+                Ray ch = new_ray(pos, d, E[o] * smid[o], sc[o], t_sum, (uint32_t)prim, sid_early(k, o, 0), o, 3, plane,
+                                 room);
                 E[o] *= (1.f - smid[o]);
                 const float4 U = draw(r.seed, (uint32_t)prim, ch.sid, 0u);
                 ch.d = lambert(n, U.x, U.y);
                 if (tau[o] > 0.f) {
-                    const Ray tr = new_ray(pos, d, E[o] * tau[o], sc[o], t_sum, (uint32_t)prim, sid_early(k, o, 1), o, 0, plane);
+                    const Ray tr = new_ray(pos, d, E[o] * tau[o], sc[o], t_sum, (uint32_t)prim, sid_early(k, o, 1), o, 0,
+                                           plane, room);
                     E[o] *= (1.f - tau[o]);
                     Ray td = ch;
                     td.I = ch.I * tau[o];
@@ -204,16 +243,16 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             d = d - n * (2.f * cos_t);
             eh = 0.f;
 #pragma unroll
-            for (int o = 0; o < kBands; ++o) eh = (o == r.h_oct) ? E[o] : eh;
-            if (order >= r.max_broad && eh > kTP1) { ++L.v[C_CAP]; break; }
+            for (int o = 0; o < kBands; ++o) eh = (o == P.h_oct) ? E[o] : eh;
+            if (order >= P.max_broad && eh > kTP1) { ++L.v[C_CAP]; break; }
         } while (eh > kTP1);
         if (!lost) {
-            const int nfin = r.oct_hi - r.oct_lo + 1;
+            const int nfin = P.oct_hi - P.oct_lo + 1;
             unsigned long long slot = atomicAdd(&c->tail, (unsigned long long)nfin);
 #pragma unroll
             for (int o = 0; o < kBands; ++o) {
-                if (o < r.oct_lo || o > r.oct_hi) continue;
-                const Ray it = new_ray(pos, d, E[o], sc[o], t_sum, (uint32_t)prim, sid_final(o), o, 0, plane);
+                if (o < P.oct_lo || o > P.oct_hi) continue;
+                const Ray it = new_ray(pos, d, E[o], sc[o], t_sum, (uint32_t)prim, sid_final(o), o, 0, plane, room);
                 ring_store(r, slot++, to_item(it));
                 ++L.v[C_OCT];
             }
@@ -333,6 +372,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     float3 o = make_float3(0.f, 0.f, 0.f), d = o;
     float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f, best = FLT_MAX;
     int skip = -1, node = 0, sp = 0, bi = -1, leaf = 0;
+    float teps = S.t_eps;
     int stack[kBvhStack];
     for (;;) {
         const unsigned need = __ballot_sync(FULL, !have && !exhausted);
@@ -349,12 +389,15 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                     o = f3(P);
                     d = f3(D);
                     skip = __float_as_int(X.w);
+                    const int room = (int)(__float_as_uint(X.z) >> 6);
                     const float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
                     const float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
                     const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
                     ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
                     ox = o.x * ix; oy = o.y * iy; oz = o.z * iz;
-                    node = 0; sp = 0; best = FLT_MAX; bi = -1;
+                    node = r.n_rooms > 1 ? __ldg(&r.rooms[room].bvh_root) : 0;
+                    teps = r.n_rooms > 1 ? __ldg(&r.rooms[room].t_eps) : S.t_eps;
+                    sp = 0; best = FLT_MAX; bi = -1;
                     have = true;
                 } else {
                     exhausted = true;
@@ -387,7 +430,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 const int code = ~leaf;
                 const int f0 = code >> 4, cnt = (code & 15) + 1;
                 w.tris += (unsigned)cnt;
-                for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+                for (int k = 0; k < cnt; ++k) test_tri(S, teps, f0 + k, o, d, skip, best, bi, w);
                 leaf = 0;
             }
             if (have && node == kEmptyChild) {
@@ -411,7 +454,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 const int code = ~node;
                 const int f0 = code >> 4, cnt = (code & 15) + 1;
                 w.tris += (unsigned)cnt;
-                for (int k = 0; k < cnt; ++k) test_tri(S, f0 + k, o, d, skip, best, bi, w);
+                for (int k = 0; k < cnt; ++k) test_tri(S, teps, f0 + k, o, d, skip, best, bi, w);
                 if (sp == 0) fin = true;
                 else node = stack[--sp];
             }
@@ -457,12 +500,14 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
             const bool hit = h.x >= 0;
             const float t = __int_as_float(h.y);
             ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
-            L.v[C_DET] += detect_octave(r, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask, R.prim);
+            const RoomParams &P = r.rooms[R.room];
+            L.v[C_DET] += detect_octave(r, P, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask,
+                                        R.prim);
             if (!hit) {
                 // lost: no End_Trace after a miss in phase B (TaskAll:437-443), loop exit in phase C (500-505)
                 L.lost += (double)(R.I * R.scale);
             } else {
-                R.t_sum += (double)t * r.inv_c_d;
+                R.t_sum += (double)t * P.inv_c_d;
                 R.p = R.p + R.d * t;
                 const float4 A = __ldg(S.tri + 3 * h.x), B = __ldg(S.tri + 3 * h.x + 1);
                 R.plane = __float_as_int(A.w);
@@ -473,14 +518,14 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
                 R.I *= mt.x;
                 const float4 U = draw(r.seed, R.prim, R.sid, 1u + R.nb);
                 const uint32_t nb = R.nb++;
-                const bool transmit = S.has_trans && !r.pure_specular && U.x < __ldg(S.trans + poly * kBands + R.oct);
+                const bool transmit = S.has_trans && !P.pure_specular && U.x < __ldg(S.trans + poly * kBands + R.oct);
                 const float3 spec = R.d - n * (2.f * cos_t);
                 const float3 nn = cos_t > 0.f ? n * -1.f : n;
                 bool alive = true;
                 bool split = false;
                 if (R.phase == 0) {
                     // Scatter_Late
-                    if (r.pure_specular || U.y > mt.w) {
+                    if (P.pure_specular || U.y > mt.w) {
                         R.d = transmit ? spec * -1.f : spec;
                         R.mask &= ~1;
                     } else {
@@ -502,10 +547,10 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
                     }
                     // phase-B loop test (TaskAll:473): failing it enters End_Trace, which always
                     // traces at least one more segment
-                    if (!(R.t_sum < r.cotime && R.I > kTP2)) { R.phase = 1; ++L.v[C_END]; }
+                    if (!(R.t_sum < P.cotime && R.I > kTP2)) { R.phase = 1; ++L.v[C_END]; }
                 } else {
                     // Scatter_VeryLate
-                    if (!r.pure_specular && U.y < mt.z) {
+                    if (!P.pure_specular && U.y < mt.z) {
                         R.d = lambert(nn, U.z, U.w);
                         R.mask |= 3;
                     } else {
@@ -513,7 +558,7 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
                         R.mask &= ~1;
                     }
                     if (transmit) R.d = R.d * -1.f;
-                    alive = R.t_sum < r.cotime && R.I > kTP3;  // TaskAll:534
+                    alive = R.t_sum < P.cotime && R.I > kTP3;  // TaskAll:534
                 }
                 if (alive && (long long)R.nb >= r.max_seg) { ++L.v[C_CAP]; alive = false; }
                 if (!alive && split) { R = C; split = false; alive = true; }
@@ -545,7 +590,7 @@ __global__ void k_paths(DevScene S, int n, const double *o, const double *dd, in
     for (int b = 0; b < maxb; ++b) {
         float t;
         int tri;
-        if (!trace_ray(S, p, d, plane, t, tri, rt)) break;
+        if (!trace_ray(S, 0, S.t_eps, p, d, plane, t, tri, rt)) break;
         const size_t k = (size_t)i * maxb + b;
         const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
         const int pl = __float_as_int(B.w);
@@ -563,8 +608,9 @@ __global__ void k_emit(DevRun r, long long p0, int n, double *out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const long long prim = p0 + i;
-    const int s = (int)((prim + 1) % r.nsrc);
-    const float3 d = emit_dir(r, prim, (int)r.src[s].w);
+    const RoomParams &P = r.rooms[0];
+    const int s = P.src_begin + (int)((prim + 1) % P.nsrc);
+    const float3 d = emit_dir(r, P.nsrc, prim, (int)r.src[s].w);
     out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
 }
 
@@ -596,6 +642,11 @@ cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStrea
 
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s) {
     k_wave<<<1, 32, 0, s>>>(r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cond(const DevRun &r, cudaGraphConditionalHandle h, cudaStream_t s) {
+    k_cond<<<1, 32, 0, s>>>(r, h);
     return cudaGetLastError();
 }
 

@@ -166,6 +166,57 @@ class Run:
             pass
 
 
+class BatchRun(Run):
+    """A batch run over several rooms traced as one wavefront (pach_batch_begin)."""
+
+    def __init__(self, dscenes, workloads, rays, params):
+        L = _capi.lib()
+        self._src = [source_array(w.sources) for w in workloads]
+        self._rec = [receiver_array(w.receivers) for w in workloads]
+        descs = (_capi.RoomDesc * len(workloads))()
+        for i, w in enumerate(workloads):
+            descs[i].scene = dscenes[i].handle.value
+            descs[i].sources = self._src[i]
+            descs[i].n_sources = len(w.sources)
+            descs[i].receivers = self._rec[i]
+            descs[i].n_receivers = len(w.receivers)
+            descs[i].ray_count = int(rays[i])
+            descs[i].cutoff_length_m = float(w.cutoff_length_m)
+        self._descs = descs
+        self._keep = dscenes
+        self.room_receivers = [len(w.receivers) for w in workloads]
+        self.R = sum(self.room_receivers)
+        self.params = params
+        self.T = int(params.sample_rate * params.hist_cotime_ms / 1000.0)
+        h = C.c_void_p()
+        check(L.pach_batch_begin(descs, len(workloads), C.byref(params), C.byref(h)))
+        self.handle = h
+
+    def room_histograms(self, scaled=False):
+        """Histograms split per room (the run's receiver rows in room order)."""
+        h = self.histograms(scaled=scaled)
+        out, k = [], 0
+        for n in self.room_receivers:
+            out.append({name: v[k:k + n] for name, v in h.items()})
+            k += n
+        return out
+
+
+def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, **kw):
+    """Trace several rooms.Workload as one batch run; returns (per-room histograms, stats)."""
+    ds = dscenes or [DeviceScene(w.scene) for w in workloads]
+    n = [w.rays for w in workloads] if rays is None else list(rays)
+    hist_ms = max(w.cutoff_s for w in workloads) * 1000.0
+    params = make_params(rays=sum(n), cutoff_length_m=workloads[0].cutoff_length_m, hist_cotime_ms=hist_ms, seed=seed,
+                         sample_rate=workloads[0].sample_rate, **kw)
+    run = BatchRun(ds, workloads, n, params)
+    try:
+        run.wait()
+        return run.room_histograms(scaled=scaled), run.stats()
+    finally:
+        run.close()
+
+
 def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, **kw):
     """Trace a rooms.Workload on the GPU; returns (histograms, stats)."""
     ds = dscene or DeviceScene(workload.scene)

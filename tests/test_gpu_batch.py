@@ -1,0 +1,71 @@
+"""GPU checks of batch runs (many rooms as one wavefront, pach_batch_begin) and of the graph-mode
+device loop: every room of a batch traces exactly as a single run with the same primary numbering."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+from pachydermacoustic_universal_gb300 import rooms, tracer  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _rooms():
+    hall = rooms.irregular_hall_c2(target_tris=2000)
+    return [rooms.shoebox_c1(), rooms.proposal_room_c4(3), hall]
+
+
+def test_batch_rooms_match_single_runs():
+    ws = _rooms()
+    ds = [tracer.DeviceScene(w.scene) for w in ws]
+    rays = [3000, 2000, 700]
+    seed = 11
+    hb, sb = tracer.trace_batch(ws, dscenes=ds, rays=rays, seed=seed)
+    off = 0
+    seg = 0
+    for i, w in enumerate(ws):
+        hs, ss = tracer.trace(w, dscene=ds[i], rays=rays[i], seed=seed, ray_begin=off)
+        T = hs["energy"].shape[-1]
+        for name in ("energy", "pressure", "dir_pos", "dir_neg", "analysis"):
+            a, b = hb[i][name][..., :T], hs[name]
+            assert np.allclose(a, b, rtol=1e-9, atol=1e-30), (i, name)
+        seg += ss["segments"]
+        off += rays[i]
+    assert sb["segments"] == seg
+    assert sb["primaries"] == sum(rays)
+
+
+def test_batch_scaling_is_per_room():
+    ws = _rooms()[:2]
+    ds = [tracer.DeviceScene(w.scene) for w in ws]
+    rays = [1500, 500]
+    raw, _ = tracer.trace_batch(ws, dscenes=ds, rays=rays, seed=3)
+    sc, _ = tracer.trace_batch(ws, dscenes=ds, rays=rays, seed=3, scaled=True)
+    for i in range(2):
+        ns = len(ws[i].sources)
+        assert np.allclose(sc[i]["energy"], raw[i]["energy"] * ns / rays[i], rtol=1e-9)
+
+
+def test_graph_loop_matches_host_loop():
+    w = rooms.shoebox_c1()
+    ds = tracer.DeviceScene(w.scene)
+    hg, sg = tracer.trace(w, dscene=ds, rays=4000, seed=9)
+    hh, sh = tracer.trace(w, dscene=ds, rays=4000, seed=9, kernel_timing=True)
+    assert sg["segments"] == sh["segments"]
+    assert np.allclose(hg["energy"], hh["energy"], rtol=1e-9, atol=1e-30)
+    assert sh["trace_ms"] > 0 and sg["trace_ms"] == 0
+
+
+def test_batch_of_c3_rooms_runs():
+    ws = rooms.batched_rooms_c3(n_rooms=16, max_rays=20_000)
+    h, s = tracer.trace_batch(ws, rays=[min(w.rays, 600) for w in ws], seed=5)
+    assert len(h) == 16
+    for i, w in enumerate(ws):
+        assert h[i]["energy"].shape[0] == len(w.receivers)
+        assert np.all(np.isfinite(h[i]["energy"]))
+        assert h[i]["energy"].sum() > 0
+    assert s["queue_overflows"] == 0
