@@ -1,9 +1,11 @@
-"""Benchmark: segment-bounces/s of the split ray tracer on the irregular-hall workload.
+"""Benchmark: segment-bounces/s of the split ray tracer.
 
-Workload (one GPU): the 40 x 25 x 15 m jittered hall with 200 diffusers (~20k triangles),
+Default workload (one GPU): the 40 x 25 x 15 m jittered hall with 200 diffusers (~20k triangles),
 2 sources, 16 receivers of radius 0.5 m, 3 s cutoff, 1 ms bins, 1M primary rays.  A step traces
 one batch of primaries (default 131072); the timed steps together cover the 1M-ray job, each step
 tracing its own primaries (ray_begin = step * batch), the warm-up steps trace primaries after them.
+--workload shoebox: the 12-triangle 10 x 8 x 4 m shoebox; --workload batched: the 64-room batch
+(each room's ray count x --ray-scale per step) as one batch run with autotuned knobs.
 
 Metric: segment-bounces/s = shoot calls (broadband + octave rays, hit or miss) per second.
   value  -- device time of the engine's kernels (CUDA events on the engine's stream), scene resident.
@@ -135,51 +137,75 @@ def sum_over_ranks(dist, x, device=None):
     return float(t.item())
 
 
-def reference_work(w, sample_rays, seed):
+def reference_work(ws, sample_rays, seed):
     """k_cell, k_tri: mean voxel cells stepped and polygon tests per segment of the reference
-    traversal (grid domain 7) on a sample of the same rays -- the SURVEY's algorithm-defined work."""
+    traversal (grid domain 7) on a sample of the same rays (shared among the rooms ws)."""
     from oracle import oracle as O
     t0 = time.time()
-    _, st = O.trace(w, rays=sample_rays, seed=seed, threads=0, grid_domain=7)
+    tot = {}
+    per = max(1, sample_rays // len(ws))
+    for w in ws:
+        _, st = O.trace(w, rays=per, seed=seed, threads=0, grid_domain=7)
+        for k, v in st.items():
+            if isinstance(v, (int, float)):
+                tot[k] = tot.get(k, 0) + v
     dt = time.time() - t0
-    return st, dt
+    return tot, dt
 
 
-def cpu_baseline(w, sample_rays, seed):
-    st, dt = reference_work(w, sample_rays, seed)
+def cpu_baseline(ws, sample_rays, seed):
+    st, dt = reference_work(ws, sample_rays, seed)
     cores = os.cpu_count() or 1
     return {"value": st["segments"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{sample_rays} primaries of the workload ({st['segments']} segments, {dt:.1f} s), "
-                      f"FP64 restatement, voxel grid domain 7, {cores} threads"}, st
+            "sample": f"{sample_rays} primaries of the workload ({len(ws)} room(s), {int(st['segments'])} segments, "
+                      f"{dt:.1f} s), FP64 restatement, voxel grid domain 7, {cores} threads"}, st
+
+
+def workload(name, ray_scale):
+    """The rooms of a bench workload: the irregular hall (default), the 12-triangle shoebox, or the
+    64-room batch (ray counts scaled by ray_scale)."""
+    from pachydermacoustic_universal_gb300 import rooms
+    if name == "hall":
+        return [rooms.irregular_hall_c2()]
+    if name == "shoebox":
+        return [rooms.shoebox_c1()]
+    ws = rooms.batched_rooms_c3()
+    for w in ws:
+        w.rays = max(100, int(round(w.rays * ray_scale)))
+    return ws
 
 
 def run_reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from pachydermacoustic_universal_gb300 import rooms
-    w = rooms.irregular_hall_c2()
+    from oracle import oracle as O
+    rooms_ = workload(args.workload, args.ray_scale)[:4]
     sample = args.ref_sample
+    per = max(1, sample // len(rooms_))
     tot_seg, tot_t = 0, 0.0
-    st = None
     for step in range(args.warmup + args.steps):
-        from oracle import oracle as O
         t0 = time.time()
-        _, st = O.trace(w, rays=sample, ray_begin=step * sample, seed=args.seed, threads=0, grid_domain=7)
+        seg = 0
+        for w in rooms_:
+            _, st = O.trace(w, rays=per, ray_begin=step * per, seed=args.seed, threads=0, grid_domain=7)
+            seg += st["segments"]
         dt = time.time() - t0
         if step >= args.warmup:
-            tot_seg += st["segments"]
+            tot_seg += seg
             tot_t += dt
     val = tot_seg / tot_t
     cores = os.cpu_count() or 1
+    w = rooms_[0]
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded room generator)",
             "impl": "reference",
-            "config": {"workload": w.name, "rays_per_step": sample, "cutoff_s": w.cutoff_s,
+            "config": {"workload": w.name if len(rooms_) == 1 else f"batched (first {len(rooms_)} rooms)",
+                       "rays_per_step": per * len(rooms_), "cutoff_s": w.cutoff_s,
                        "sources": len(w.sources), "receivers": len(w.receivers), "triangles": w.scene.n_triangles},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample} primaries per step, FP64 restatement of the reference "
+                             "sample": f"{per * len(rooms_)} primaries per step, FP64 restatement of the reference "
                                        f"algorithm (voxel grid domain 7), {cores} threads; the C# reference "
                                        f"cannot run here (no .NET runtime, Hare unvendored)"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -198,7 +224,9 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--batch", type=int, default=131072, help="primaries per step")
+    ap.add_argument("--workload", default="hall", choices=["hall", "shoebox", "batched"])
+    ap.add_argument("--batch", type=int, default=131072, help="primaries per step (single-room workloads)")
+    ap.add_argument("--ray-scale", type=float, default=0.004, help="batched: fraction of each room's rays per step")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-sample", type=int, default=400, help="primaries of the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=200, help="primaries per step of the reference arm")
@@ -213,26 +241,33 @@ def main():
     import torch
     torch.cuda.set_device(local)
     dist = init_dist(ws, "nccl")
-    from pachydermacoustic_universal_gb300 import rooms, tracer, _capi
+    from pachydermacoustic_universal_gb300 import tracer, _capi
     _capi.lib()
-    w = rooms.irregular_hall_c2()
-    dev_scene = tracer.DeviceScene(w.scene)
+    rooms_ = workload(args.workload, args.ray_scale)
+    batched = len(rooms_) > 1
+    scenes = [tracer.DeviceScene(w.scene) for w in rooms_]
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
-    B = args.batch
+    B = sum(w.rays for w in rooms_) if batched else args.batch
     # this rank's primaries: steps are consecutive batches; ranks own disjoint ranges
     base = rank * (args.warmup + args.steps) * B
+    tune = None
+    if batched:  # packet size and block shape from the autotuner (timed before the warm-up, cached)
+        tune = tracer.autotune(rooms_, dscenes=scenes, sample_rays=min(B, 20000), seed=args.seed)
 
     def step_trace(idx, e2e=False):
-        kw = dict(rays=B, seed=args.seed, ray_begin=base + idx * B, kernel_timing=not e2e)
+        kw = dict(seed=args.seed, ray_begin=base + idx * B, kernel_timing=not e2e)
+        t0 = time.perf_counter()
+        # e2e: the public API from host buffers -- upload the scenes, trace, download the histograms
+        ds = [tracer.DeviceScene(w.scene) for w in rooms_] if e2e else scenes
+        if batched:
+            h, s = tracer.trace_batch(rooms_, dscenes=ds, tune=tune, **kw)
+        else:
+            h, s = tracer.trace(rooms_[0], dscene=ds[0], rays=B, **kw)
+            h = [h]
         if e2e:
-            # public API from host buffers: upload the scene, trace, download the histograms
-            t0 = time.perf_counter()
-            ds = tracer.DeviceScene(w.scene)
-            h, s = tracer.trace(w, dscene=ds, **kw)
-            ds.close()
-            return h, s, time.perf_counter() - t0
-        h, s = tracer.trace(w, dscene=dev_scene, **kw)
-        return h, s, None
+            for d in ds:
+                d.close()
+        return h, s, time.perf_counter() - t0
 
     for i in range(args.warmup):
         flush.zero_()
@@ -270,8 +305,8 @@ def main():
             h, s, dt = step_trace(i, e2e=True)
             tt += dt
             es += s["segments"]
-            h2d = scene_bytes(w.scene) + 88 * len(w.sources) + 32 * len(w.receivers)
-            d2h = int(sum(v.nbytes for v in h.values()))
+            h2d = sum(scene_bytes(w.scene) + 88 * len(w.sources) + 32 * len(w.receivers) for w in rooms_)
+            d2h = int(sum(v.nbytes for hh in h for v in hh.values()))
         tt = max_over_ranks(dist, tt, device=f"cuda:{local}")
         es = sum_over_ranks(dist, es, device=f"cuda:{local}")
         e2e = {"value": es / tt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -280,7 +315,8 @@ def main():
     peaks, peak_kind = _peaks()
     agg = {k: sum(s[k] for s in stats) for k in ("segments", "detections", "fp64_retests", "octave_rays",
                                                    "segments_broadband", "segments_phase_b", "segments_phase_c",
-                                                   "trace_ms", "shade_ms", "broadband_ms", "waves")}
+                                                   "trace_ms", "shade_ms", "broadband_ms", "waves",
+                                                   "bvh_nodes_visited", "tri_tests")}
     # HBM roofline of the dominant wavefront kernel, algorithmic bytes per octave-ray segment:
     #   k_trace  reads the ray's position, direction and plane (48 B) and writes (triangle, t) (8 B);
     #   k_shade  reads the 64 B ray and its 8 B hit, writes the surviving ray and split children
@@ -294,14 +330,24 @@ def main():
     k_bytes = trace_bytes if kern == "k_trace" else shade_bytes
     achieved_gbs = k_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
     oct_launch = agg["waves"]
+    # the on-chip side of the walk: BVH node (128 B) and triangle (48 B) reads served by L1/L2
+    bvh_gbs = ((128.0 * agg["bvh_nodes_visited"] + 48.0 * agg["tri_tests"]) / (agg["trace_ms"] * 1e-3) / 1e9
+               if agg["trace_ms"] > 0 else None)
+    tris = sum(w.scene.n_triangles for w in rooms_)
+    cfg = {"workload": rooms_[0].name if not batched else f"batched_{len(rooms_)}_rooms",
+           "rays_per_step": B, "rays_total": B * args.steps * ws, "triangles": tris,
+           "sources": sum(len(w.sources) for w in rooms_), "receivers": sum(len(w.receivers) for w in rooms_),
+           "cutoff_s": max(w.cutoff_s for w in rooms_), "bins_ms": 1, "l2": "256 MiB buffer written between steps",
+           "bvh_nodes_leaves_depth": stats[0]["accel"]}
+    if batched:
+        cfg["rooms"] = len(rooms_)
+        cfg["ray_scale"] = args.ray_scale
+        cfg["autotune"] = {k: tune[k] for k in tracer.TUNE_KNOBS + ("from_cache",)}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 geometry, f64 histograms", "data": "synthetic (seeded room generator)",
-        "config": {"workload": w.name, "rays_per_step": B, "rays_total": B * args.steps * ws,
-                   "triangles": w.scene.n_triangles, "sources": len(w.sources), "receivers": len(w.receivers),
-                   "cutoff_s": w.cutoff_s, "bins_ms": 1, "l2": "256 MiB buffer written between steps",
-                   "bvh_nodes_leaves_depth": stats[0]["accel"]},
+        "config": cfg,
         "gpu_launches": launches,
         "clocks": clocks,
         "e2e": e2e,
@@ -310,15 +356,20 @@ def main():
                      "frac": (achieved_gbs / peaks["hbm_gbs"]) if achieved_gbs else None,
                      "traffic": None, "peak_source": peak_kind,
                      "per_unit": ("56 B per octave segment" if kern == "k_trace" else
-                                  "72 B in + 64 B per output ray per octave segment + 48 B per detection")},
+                                  "72 B in + 64 B per output ray per octave segment + 48 B per detection"),
+                     "bvh_reads_gbs": bvh_gbs,
+                     "bvh_reads_note": "BVH node (128 B) and triangle (48 B) reads of the walk per second of "
+                                       "k_trace, served by L1/L2 (the walk's binding resource is on-chip)"},
         "detail": {"trace_ms": agg["trace_ms"], "shade_ms": agg["shade_ms"], "broadband_ms": agg["broadband_ms"],
                    "waves": agg["waves"], "wall_s": wall, "segments": agg["segments"],
                    "detections": agg["detections"], "fp64_retests": agg["fp64_retests"],
                    "octave_rays": agg["octave_rays"], "peak_live_rays": max(s["peak_live_rays"] for s in stats),
+                   "bvh_nodes_per_segment": agg["bvh_nodes_visited"] / max(1, seg_oct),
+                   "tri_tests_per_segment": agg["tri_tests"] / max(1, seg_oct),
                    "segments_phase_c_frac": agg["segments_phase_c"] / max(1, agg["segments"])},
     }
     traffic_file = os.path.join(ROOT, "profiles", f"{kern}_traffic.json")
-    if os.path.exists(traffic_file):
+    if os.path.exists(traffic_file) and not batched:
         try:
             tr = json.load(open(traffic_file))
             line["roofline"]["traffic"] = tr.get("dram_bytes_per_segment", 0) * seg_oct / max(1, oct_launch)
@@ -326,12 +377,13 @@ def main():
         except Exception:
             pass
     if rank == 0 and ws >= 1 and not args.no_cpu_baseline:
-        cb, st = cpu_baseline(w, args.cpu_sample, args.seed)
+        sample_rooms = rooms_[:4]
+        cb, st = cpu_baseline(sample_rooms, args.cpu_sample, args.seed)
         line["cpu_baseline"] = cb
         k_cell = st["cells_visited"] / st["segments"]
         k_tri = st["tri_tests"] / st["segments"]
         det = st["detections"] / st["segments"]
-        R = len(w.receivers)
+        R = sum(len(w.receivers) for w in sample_rooms) / len(sample_rooms)
         flops_seg = 9 * k_cell + 27 * k_tri + 20 * R + 40
         bytes_seg = 8 * k_cell + 36 * k_tri + 2 * 48 + 12 * det
         line["reference_work"] = {"k_cell": k_cell, "k_tri": k_tri, "detections_per_segment": det,

@@ -114,7 +114,8 @@ typedef struct {
                                       2 = speculative (lanes holding a leaf keep descending until the
                                       whole warp holds one, then the warp tests its leaves together) */
     int32_t capture;               /* 1: record energy per receiver, time window and emission-direction
-                                      bin (pach_trace_get_capture, pach_proposal.h) */
+                                      bin; 2: per primary, receiver and time window
+                                      (pach_trace_get_capture, pach_proposal.h) */
     const double *prim_dirs;       /* optional [ray_count][3] emission directions (importance sampling) */
     const double *prim_weights;    /* optional [ray_count] emission weights (1/q) */
     const float *proposal;         /* optional [n_proposal][160] learned-proposal lobes (pach_proposal.h) */
@@ -210,6 +211,24 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
  * room by its own primaries. */
 pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const pach_trace_params *params,
                              pach_run **out);
+
+/* Autotuner (no counterpart in the reference): times sample runs of the rooms (sample_rays primaries
+ * shared among them in proportion to their ray counts) over candidate packet sizes and block shapes,
+ * and returns the fastest.  Results are cached in a text file (cache_path, or $PACH_TUNE_CACHE, or
+ * ~/.cache/pach_gb300_tune.txt) keyed by device and a coarse workload signature; force = 1 re-tunes.
+ * Copy the four knobs into pach_trace_params to use them. */
+typedef struct {
+    int32_t wave_kilo_items;
+    int32_t block_threads;
+    int32_t blocks_per_sm;
+    int32_t traversal;
+    double segments_per_s;         /* the chosen configuration's measured sample throughput */
+    double tune_seconds;           /* wall time spent timing (0 when taken from the cache) */
+    int32_t trials;                /* configurations timed */
+    int32_t from_cache;
+} pach_tune_result;
+pach_status pach_autotune(const pach_room_desc *rooms, int32_t n_rooms, const pach_trace_params *params,
+                          int64_t sample_rays, const char *cache_path, int32_t force, pach_tune_result *out);
 pach_status pach_trace_poll(pach_run *run, pach_progress *progress);
 pach_status pach_trace_cancel(pach_run *run);
 /* Blocks until the run stops or timeout_ms passes (timeout_ms < 0: no limit). */

@@ -78,8 +78,9 @@ int32_t pach_direction_bin(double x, double y, double z);
 pach_status pach_proposal_sample(const float *proposal, int32_t n_prop, double mix, uint64_t seed,
                                  int64_t ray_begin, int32_t n, float *dirs, float *weights);
 
-/* Capture of a finished run made with capture = 1: [n_receivers][PACH_CAPTURE_WINDOWS][PACH_DIR_BINS]
- * energy (W, unscaled), cap >= that many floats. */
+/* Capture of a finished run: capture = 1 gives [n_receivers][PACH_CAPTURE_WINDOWS][PACH_DIR_BINS],
+ * capture = 2 gives [ray_count][n_receivers][PACH_CAPTURE_WINDOWS] (energy in W, unscaled); cap >= that
+ * many floats. */
 pach_status pach_trace_get_capture(pach_run *run, float *out, size_t cap);
 
 #ifdef __cplusplus

@@ -64,6 +64,12 @@ class RoomDesc(C.Structure):
                 ("cutoff_length_m", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("wave_kilo_items", C.c_int32), ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("traversal", C.c_int32), ("segments_per_s", C.c_double), ("tune_seconds", C.c_double),
+                ("trials", C.c_int32), ("from_cache", C.c_int32)]
+
+
 class Progress(C.Structure):
     _fields_ = [("state", C.c_int32), ("last_status", C.c_int32), ("rays_done", C.c_int64),
                 ("rays_total", C.c_int64), ("end_traces", C.c_int64), ("segments", C.c_int64)]
@@ -93,7 +99,7 @@ class Stats(C.Structure):
 
 # Every symbol include/pach_gpu.h declares (checked by the CPU test suite).
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
-           "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
+           "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
@@ -122,6 +128,8 @@ def _declare(L):
         "pach_trace_begin": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
                                        C.POINTER(TraceParams), C.POINTER(vp)]),
         "pach_batch_begin": (C.c_int, [C.POINTER(RoomDesc), C.c_int32, C.POINTER(TraceParams), C.POINTER(vp)]),
+        "pach_autotune": (C.c_int, [C.POINTER(RoomDesc), C.c_int32, C.POINTER(TraceParams), C.c_int64, C.c_char_p,
+                                    C.c_int32, C.POINTER(TuneResult)]),
         "pach_trace_poll": (C.c_int, [vp, C.POINTER(Progress)]),
         "pach_trace_cancel": (C.c_int, [vp]),
         "pach_trace_wait": (C.c_int, [vp, C.c_int64]),

@@ -110,6 +110,13 @@ struct pach_run {
 
 namespace {
 
+// primaries of a run over all its rooms
+long long rprim_total(const pach_run *run) {
+    long long n = 0;
+    for (const RoomSpec &rm : run->rooms) n += rm.rays;
+    return n;
+}
+
 cudaError_t upload(DevMem &m, const void *src, size_t bytes) {
     cudaError_t e = m.alloc(bytes);
     if (e != cudaSuccess) return e;
@@ -363,7 +370,8 @@ void run_worker(pach_run *run) {
         if (!run->prim_weights.empty()) TRY(upload(run->dw, run->prim_weights.data(), run->prim_weights.size() * sizeof(double)));
         if (!run->prop.empty()) TRY(upload(run->dprop, run->prop.data(), run->prop.size() * sizeof(float)));
         if (run->p.capture) {
-            TRY(run->dcap.alloc((size_t)std::max(R, 1) * kCaptureWindows * kDirBins * sizeof(float)));
+            const size_t per = run->p.capture == 2 ? (size_t)(rprim_total(run)) : (size_t)kDirBins;
+            TRY(run->dcap.alloc((size_t)std::max(R, 1) * kCaptureWindows * per * sizeof(float)));
             TRY(cudaMemset(run->dcap.p, 0, run->dcap.bytes));
         }
 
@@ -374,7 +382,7 @@ void run_worker(pach_run *run) {
         int bps_tr = 0, bps_sh = 0;
         // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
         const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max);
-        TRY(wave_kernel_occupancy(tr_variant, threads, (int)sizeof(float4) * std::max(R, 1), &bps_tr, &bps_sh));
+        TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
         // ring and wave sizing
@@ -424,6 +432,7 @@ void run_worker(pach_run *run) {
         r.n_prop = run->prop.empty() ? 0 : run->p.n_proposal;
         r.prop_mix = (float)(run->p.proposal_mix > 0 ? run->p.proposal_mix : 0.3);
         r.capture = run->p.capture ? run->dcap.as<float>() : nullptr;
+        r.capture_mode = run->p.capture;
         {
             const bool given = run->p.capture_edges_ms[0] != 0 || run->p.capture_edges_ms[1] != 0 ||
                                run->p.capture_edges_ms[2] != 0;
@@ -801,8 +810,10 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
         for (long long i = 0; i < (long long)p.n_proposal * PACH_MLP_OUT; ++i)
             if (!std::isfinite(p.proposal[i])) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal holds a non-finite value");
     }
-    if (p.capture && (p.capture != 1 || n_receivers < 1))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0 or 1 and needs receivers");
+    if (p.capture && (p.capture < 0 || p.capture > 2 || n_receivers < 1))
+        return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0, 1 or 2 and needs receivers");
+    if (p.capture == 2 && (double)p.ray_count * n_receivers * kCaptureWindows * 4 > 16e9)
+        return fail(PACH_ERR_INVALID_ARGUMENT, "per-primary capture larger than 16 GB");
     std::unique_ptr<pach_run> run(new pach_run());
     run->scene = scene;
     run->p = p;
@@ -870,7 +881,7 @@ pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const
     if (prim > (1ll << 32)) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin + the rooms' rays must be <= 2^32");
     if (R > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers over the rooms of a batch");
     if (p.capture && (p.capture != 1 || R < 1))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0 or 1 and needs receivers");
+        return fail(PACH_ERR_INVALID_ARGUMENT, "a batch captures per direction bin only (capture 1) and needs receivers");
     run->scene = run->rooms[0].scene;
     run->p.ray_count = prim - p.ray_begin;
     run->p.cutoff_length_m = run->rooms[0].cutoff_len;
@@ -962,8 +973,9 @@ pach_status pach_trace_get_capture(pach_run *run, float *out, size_t cap) {
         if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
     }
     if (!run->p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "the run was made without capture");
-    const size_t n = (size_t)run->R * kCaptureWindows * kDirBins;
-    if (!out || cap < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap < receivers * 4 * 1536");
+    const size_t per = run->p.capture == 2 ? (size_t)rprim_total(run) : (size_t)kDirBins;
+    const size_t n = (size_t)run->R * kCaptureWindows * per;
+    if (!out || cap < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap < receivers * 4 * (1536 bins or primaries)");
     cudaSetDevice(run->scene->device);
     cudaError_t e = cudaMemcpy(out, run->dcap.p, n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "capture copy"));

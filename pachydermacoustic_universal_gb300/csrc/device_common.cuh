@@ -410,12 +410,16 @@ __device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P
                                             uint32_t prim, double time, float e) {
     const int s = P.src_begin + (int)((prim + 1ull) % (unsigned long long)P.nsrc);
     const float4 src = r.src[s];
-    float w;
-    const float3 d0 = primary_dir(r, P.nsrc, prim, (int)src.w, w);
-    const int b = dir_bin(d0.x, d0.y, d0.z);
     const double dx = rec[k].x - src.x, dy = rec[k].y - src.y, dz = rec[k].z - src.z;
     const float ms = (float)((time - sqrt(dx * dx + dy * dy + dz * dz) * P.inv_c_d) * 1000.0);
     const int win = (ms >= r.cap_edge[0]) + (ms >= r.cap_edge[1]) + (ms >= r.cap_edge[2]);
+    if (r.capture_mode == 2) {
+        atomicAdd(r.capture + (((size_t)((long long)prim - r.prim_base)) * r.R + k) * kCaptureWindows + win, e);
+        return;
+    }
+    float w;
+    const float3 d0 = primary_dir(r, P.nsrc, prim, (int)src.w, w);
+    const int b = dir_bin(d0.x, d0.y, d0.z);
     atomicAdd(r.capture + ((size_t)k * kCaptureWindows + win) * kDirBins + b, e);
 }
 
@@ -531,9 +535,13 @@ __device__ void flush_counters(const DevRun &r, const LocalCounters &L) {
     }
 }
 
-__device__ __forceinline__ void load_receivers(const DevRun &r, float4 *rec) {
-    for (int i = threadIdx.x; i < r.R; i += blockDim.x) rec[i] = r.rec[i];
+// Receiver table for detection: staged in shared memory when it is small (the common case), else read
+// through L1 (a batch of many rooms: each ray tests only its room's receivers).
+__device__ __forceinline__ const float4 *stage_receivers(const DevRun &r, float4 *smem) {
+    if (r.R > kSmemReceivers) return r.rec;
+    for (int i = threadIdx.x; i < r.R; i += blockDim.x) smem[i] = r.rec[i];
     __syncthreads();
+    return smem;
 }
 
 }  // namespace

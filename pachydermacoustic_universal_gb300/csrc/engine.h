@@ -111,6 +111,9 @@ struct RoomParams {
     int h_oct, oct_lo, oct_hi, is_order, pure_specular, max_broad;
 };
 constexpr int kMaxRooms = 4096;
+// Receiver tables up to this size are staged in shared memory by the detection kernels.
+constexpr int kSmemReceivers = 256;
+inline int receiver_smem_bytes(int R) { return 16 * (R > 0 && R <= kSmemReceivers ? R : 1); }
 
 constexpr long long kPilotPrimaries = 256;
 
@@ -158,8 +161,11 @@ struct DevRun {
     const float4 *prop;            // [n_prop][kLobes][2]: (mu xyz, kappa), (log pi + log norm, cdf, 0, 0)
     int n_prop;
     float prop_mix;                // probability of the uniform component
-    // training capture (null: off): energy per receiver, time window and emission-direction bin
-    float *capture;                // [R][kCaptureWindows][kDirBins]
+    // training capture (null: off).  Mode 1: energy per receiver, time window and emission-direction
+    // bin, [R][kCaptureWindows][kDirBins].  Mode 2: energy per primary, receiver and time window,
+    // [primaries][R][kCaptureWindows] (primary index - prim_base).
+    float *capture;
+    int capture_mode;
     float cap_edge[3];             // window edges, ms after the direct arrival
 };
 

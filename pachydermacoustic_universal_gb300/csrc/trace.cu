@@ -151,8 +151,8 @@ __global__ void k_cond(DevRun r, cudaGraphConditionalHandle h) {
 // phase A: broadband rays (cast_ray_distributed, TaskAll:347-424)
 // ------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
-    extern __shared__ float4 s_rec[];
-    load_receivers(r, s_rec);
+    extern __shared__ float4 s_rec_buf[];
+    const float4 *s_rec = stage_receivers(r, s_rec_buf);
     LocalCounters L;
     const DevScene &S = r.S;
     WaveCtl *c = r.ctl;
@@ -480,8 +480,8 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
 }
 
 __global__ void __launch_bounds__(256) k_shade(DevRun r) {
-    extern __shared__ float4 s_rec[];
-    load_receivers(r, s_rec);
+    extern __shared__ float4 s_rec_buf[];
+    const float4 *s_rec = stage_receivers(r, s_rec_buf);
     LocalCounters L;
     const DevScene &S = r.S;
     WaveCtl *c = r.ctl;
@@ -628,7 +628,7 @@ __global__ void k_prop_sample(DevRun r, long long p0, int n, float *dirs, float 
 // ------------------------------------------------------------------------------------------
 // host wrappers
 // ------------------------------------------------------------------------------------------
-static size_t rec_smem(const DevRun &r) { return sizeof(float4) * (size_t)(r.R > 0 ? r.R : 1); }
+static size_t rec_smem(const DevRun &r) { return (size_t)receiver_smem_bytes(r.R); }
 
 cudaError_t launch_feed(const DevRun &r, cudaStream_t s) {
     k_feed<<<1, 32, 0, s>>>(r);

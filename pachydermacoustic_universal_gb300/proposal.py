@@ -129,16 +129,69 @@ def capture_targets(capture) -> np.ndarray:
     return t.astype(np.float32)
 
 
-def collect(workloads, rays: int, seed: int = 1, **kw):
+def direction_bins_of(d) -> np.ndarray:
+    """Bins of directions d [n][3] (the rule of pach_direction_bin, vectorised)."""
+    d = np.asarray(d, dtype=np.float32).reshape(-1, 3)
+    a = np.abs(d)
+    major = np.where((a[:, 0] >= a[:, 1]) & (a[:, 0] >= a[:, 2]), 0, np.where(a[:, 1] >= a[:, 2], 1, 2))
+    m = a[np.arange(d.shape[0]), major]
+    sign = d[np.arange(d.shape[0]), major] > 0
+    face = 2 * major + np.where(sign, 0, 1)
+    ua = np.where(major == 0, 1, 0)          # u: the first of the two other axes (x, y, z order)
+    va = np.where(major == 2, 1, 2)          # v: the second
+    u = d[np.arange(d.shape[0]), ua] / m
+    v = d[np.arange(d.shape[0]), va] / m
+    i = np.clip(((u + np.float32(1)) * np.float32(8)).astype(np.int64), 0, 15)
+    j = np.clip(((v + np.float32(1)) * np.float32(8)).astype(np.int64), 0, 15)
+    return (face * 256 + j * 16 + i).astype(np.int64)
+
+
+def capture_targets_l2(per_prim, dirs) -> np.ndarray:
+    """[N][R][4] per-primary captured energy and the primaries' emission directions [N][3] ->
+    [R][1536] targets proportional to sqrt(E[sum_w (e_w / mean e_w)^2 | bin]) x bin solid angle: the
+    proposal that minimises the summed relative variance of the windows' energies (the optimal
+    importance density for several integrands sharing one sample is proportional to the root of their
+    summed squared relative contributions)."""
+    e = np.asarray(per_prim, dtype=np.float64)
+    mean = e.mean(axis=0)                                   # [R][W]
+    rel = np.divide(e, mean[None], out=np.zeros_like(e), where=mean[None] > 0)
+    q = (rel ** 2).sum(axis=2)                              # [N][R]
+    b = direction_bins_of(dirs)
+    cnt = np.bincount(b, minlength=N_BINS).astype(np.float64)
+    _, om = direction_bins()
+    out = np.zeros((e.shape[1], N_BINS))
+    for r in range(e.shape[1]):
+        s2 = np.bincount(b, weights=q[:, r], minlength=N_BINS)
+        m2 = np.divide(s2, cnt, out=np.zeros(N_BINS), where=cnt > 0)
+        t = np.sqrt(m2) * om
+        out[r] = t / t.sum() if t.sum() > 0 else 1.0 / N_BINS
+    return out.astype(np.float32)
+
+
+def emission_directions(seed: int, ray_begin: int, n: int, n_sources: int, kind: int) -> np.ndarray:
+    """The emission directions the tracer draws for primaries ray_begin .. ray_begin + n - 1."""
+    out = np.zeros((n, 3))
+    check(_capi.lib().pach_emit_directions(int(seed), int(ray_begin), int(n), int(n_sources), int(kind),
+                                           _capi.dptr(out)))
+    return out
+
+
+def collect(workloads, rays: int, seed: int = 1, target: str = "l2", **kw):
     """Trace each workload with uniform emission and capture on; returns (cond [n][12], target [n][1536],
-    wall seconds of the traces)."""
+    wall seconds of the traces).  target "l2": per-primary capture and capture_targets_l2; "linear":
+    per-bin capture and capture_targets."""
     import time
     conds, targets = [], []
     t0 = time.perf_counter()
     for i, w in enumerate(workloads):
-        h, _ = tracer.trace(w, rays=rays, seed=seed + i, capture=True, **kw)
+        if target == "l2":
+            h, _ = tracer.trace(w, rays=rays, seed=seed + i, capture=2, **kw)
+            d = emission_directions(seed + i, 0, rays, len(w.sources), w.sources[0].kind)
+            targets.append(capture_targets_l2(h["capture"], d))
+        else:
+            h, _ = tracer.trace(w, rays=rays, seed=seed + i, capture=1, **kw)
+            targets.append(capture_targets(h["capture"]))
         conds.append(conditions(w))
-        targets.append(capture_targets(h["capture"]))
     return np.concatenate(conds), np.concatenate(targets), time.perf_counter() - t0
 
 

@@ -5,7 +5,7 @@ Protocol (``python -m pachydermacoustic_universal_gb300.proposal_study``):
 
 1. Training data: ``train_rooms`` rooms, each traced with uniform emission and capture on
    (``train_rays`` primaries, ``train_receivers`` receivers per room); one target per receiver
-   (proposal.capture_targets).  A tenth of the rooms is held back for the validation loss.
+   (proposal.capture_targets_l2 from per-primary capture, or proposal.capture_targets).  A tenth of the rooms is held back for the validation loss.
 2. Training: full-batch Adam on the GPU (pach_mlp_train, a captured CUDA graph per step).
 3. Evaluation on ``eval_rooms`` further rooms: ``seeds`` independent runs of ``eval_rays`` primaries
    with uniform emission (source kind 2) and with the learned proposal (each mixture weight of
@@ -105,22 +105,22 @@ def bias_z(Pu, Pl):
 
 
 def study(train_rooms=200, train_rays=100_000, eval_rooms=50, eval_rays=10_000, seeds=8, steps=3000, lr=1e-3,
-          mixes=(0.3,), seed=7, train_receivers=12, log=print):
+          mixes=(0.3,), seed=7, train_receivers=12, target="l2", log=print):
     t0 = time.perf_counter()
     rooms_train = [rooms.proposal_room_c4(1000 + i, n_receivers=train_receivers) for i in range(train_rooms)]
-    cond, target, t_collect = proposal.collect(rooms_train, train_rays, seed=seed)
+    cond, tgt, t_collect = proposal.collect(rooms_train, train_rays, seed=seed, target=target)
     n_val = max(1, train_rooms // 10) * train_receivers
     net = proposal.ProposalNet(seed=seed, max_rows=max(cond.shape[0], 128))
-    net.set_data(cond[n_val:], target[n_val:])
+    net.set_data(cond[n_val:], tgt[n_val:])
     t1 = time.perf_counter()
     curve = np.concatenate([net.train(steps // 2, lr=lr), net.train(steps - steps // 2, lr=lr * 0.3)])
     train_loss = float(curve[-1])
     t_train = time.perf_counter() - t1
-    net.set_data(cond[:n_val], target[:n_val])
+    net.set_data(cond[:n_val], tgt[:n_val])
     val_loss, _ = net.loss_grad(with_grad=False)
     # entropy of the targets: the loss a perfect fit reaches (bin-centre rule, up to the bin solid angles)
     _, om = proposal.direction_bins()
-    tv = target[:n_val].astype(np.float64)
+    tv = tgt[:n_val].astype(np.float64)
     ent = float(-np.mean(np.sum(np.where(tv > 0, tv * np.log(np.maximum(tv, 1e-30) / om), 0.0), axis=1)))
     uni = float(math.log(4 * math.pi))
     log(f"collect {t_collect:.1f} s ({train_rooms} rooms x {train_rays} rays), train {t_train:.1f} s "
@@ -155,7 +155,8 @@ def study(train_rooms=200, train_rays=100_000, eval_rooms=50, eval_rays=10_000, 
         x = np.asarray([v for v in x if np.isfinite(v) and v > 0])
         return float(np.exp(np.mean(np.log(x)))) if x.size else float("nan")
 
-    summary = {"train_rooms": train_rooms, "train_receivers": train_receivers, "train_rays": train_rays,
+    summary = {"target": target, "train_rooms": train_rooms, "train_receivers": train_receivers,
+               "train_rays": train_rays,
                "eval_rooms": eval_rooms, "eval_rays": eval_rays, "seeds": seeds, "steps": steps, "mixes": list(mixes),
                "collect_s": t_collect, "train_s": t_train, "train_loss": train_loss, "val_loss": val_loss,
                "uniform_loss": uni, "target_entropy": ent}
@@ -189,9 +190,10 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--mix", type=float, nargs="+", default=[0.3])
     ap.add_argument("--train-receivers", type=int, default=12)
+    ap.add_argument("--target", default="l2", choices=["l2", "linear"])
     a = ap.parse_args()
     s = study(a.train_rooms, a.train_rays, a.eval_rooms, a.eval_rays, a.seeds, a.steps, a.lr, tuple(a.mix),
-              train_receivers=a.train_receivers)
+              train_receivers=a.train_receivers, target=a.target)
     print(json.dumps(s))
 
 

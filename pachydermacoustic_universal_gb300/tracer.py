@@ -95,7 +95,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.traversal = int(traversal)
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
-    p.capture = int(bool(capture))
+    p.capture = int(capture)
     if capture_edges_ms is not None:
         p.capture_edges_ms[:] = [float(x) for x in capture_edges_ms]
     if proposal is not None:
@@ -144,8 +144,12 @@ class Run:
         return {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}
 
     def capture(self):
-        """Energy per receiver, capture window and emission-direction bin, [R][4][1536] (W, unscaled)."""
-        out = np.zeros((self.R, _capi.CAPTURE_WINDOWS, _capi.DIR_BINS), dtype=np.float32)
+        """Captured energy (W, unscaled): capture 1 -> [R][4][1536] per emission-direction bin,
+        capture 2 -> [primaries][R][4] per primary."""
+        if self.params.capture == 2:
+            out = np.zeros((self.params.ray_count, self.R, _capi.CAPTURE_WINDOWS), dtype=np.float32)
+        else:
+            out = np.zeros((self.R, _capi.CAPTURE_WINDOWS, _capi.DIR_BINS), dtype=np.float32)
         check(_capi.lib().pach_trace_get_capture(self.handle, _capi.fptr(out), out.size))
         return out
 
@@ -202,13 +206,48 @@ class BatchRun(Run):
         return out
 
 
-def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, **kw):
-    """Trace several rooms.Workload as one batch run; returns (per-room histograms, stats)."""
+def _batch_params(workloads, n, seed, **kw):
+    hist_ms = max(w.cutoff_s for w in workloads) * 1000.0
+    return make_params(rays=sum(n), cutoff_length_m=workloads[0].cutoff_length_m, hist_cotime_ms=hist_ms, seed=seed,
+                       sample_rate=workloads[0].sample_rate, **kw)
+
+
+TUNE_KNOBS = ("wave_kilo_items", "block_threads", "blocks_per_sm", "traversal")
+
+
+def autotune(workloads, *, dscenes=None, rays=None, sample_rays=20_000, cache_path=None, force=False, seed=1, **kw):
+    """Packet size and block shape for these rooms (pach_autotune); returns a dict with the four knobs
+    (TUNE_KNOBS), the measured sample throughput and whether it came from the cache."""
     ds = dscenes or [DeviceScene(w.scene) for w in workloads]
     n = [w.rays for w in workloads] if rays is None else list(rays)
-    hist_ms = max(w.cutoff_s for w in workloads) * 1000.0
-    params = make_params(rays=sum(n), cutoff_length_m=workloads[0].cutoff_length_m, hist_cotime_ms=hist_ms, seed=seed,
-                         sample_rate=workloads[0].sample_rate, **kw)
+    params = _batch_params(workloads, n, seed, **kw)
+    src = [source_array(w.sources) for w in workloads]
+    rec = [receiver_array(w.receivers) for w in workloads]
+    descs = (_capi.RoomDesc * len(workloads))()
+    for i, w in enumerate(workloads):
+        descs[i].scene = ds[i].handle.value
+        descs[i].sources = src[i]
+        descs[i].n_sources = len(w.sources)
+        descs[i].receivers = rec[i]
+        descs[i].n_receivers = len(w.receivers)
+        descs[i].ray_count = int(n[i])
+        descs[i].cutoff_length_m = float(w.cutoff_length_m)
+    res = _capi.TuneResult()
+    path = cache_path.encode() if cache_path else None
+    check(_capi.lib().pach_autotune(descs, len(workloads), C.byref(params), int(sample_rays), path, int(bool(force)),
+                                    C.byref(res)))
+    return {k: getattr(res, k) for k, _ in res._fields_}
+
+
+def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, tune=None, **kw):
+    """Trace several rooms.Workload as one batch run; returns (per-room histograms, stats).
+    tune: a dict from autotune() whose knobs are applied."""
+    ds = dscenes or [DeviceScene(w.scene) for w in workloads]
+    n = [w.rays for w in workloads] if rays is None else list(rays)
+    if tune:
+        for k in TUNE_KNOBS:
+            kw.setdefault(k, tune[k])
+    params = _batch_params(workloads, n, seed, **kw)
     run = BatchRun(ds, workloads, n, params)
     try:
         run.wait()

@@ -69,3 +69,21 @@ def test_batch_of_c3_rooms_runs():
         assert np.all(np.isfinite(h[i]["energy"]))
         assert h[i]["energy"].sum() > 0
     assert s["queue_overflows"] == 0
+
+
+def test_autotune_picks_and_caches(tmp_path):
+    ws = _rooms()[:2]
+    ds = [tracer.DeviceScene(w.scene) for w in ws]
+    cache = str(tmp_path / "tune.txt")
+    t1 = tracer.autotune(ws, dscenes=ds, rays=[2000, 2000], sample_rays=600, cache_path=cache)
+    assert t1["from_cache"] == 0 and t1["trials"] >= 5 and t1["segments_per_s"] > 0
+    assert t1["wave_kilo_items"] in (512, 1024, 2048, 4096) and t1["block_threads"] in (128, 256)
+    assert t1["blocks_per_sm"] in (4, 6) and t1["traversal"] in (1, 2)
+    t2 = tracer.autotune(ws, dscenes=ds, rays=[2000, 2000], sample_rays=600, cache_path=cache)
+    assert t2["from_cache"] == 1
+    assert all(t2[k] == t1[k] for k in tracer.TUNE_KNOBS)
+    # the tuned knobs change scheduling only: same histograms as the defaults
+    ha, _ = tracer.trace_batch(ws, dscenes=ds, rays=[800, 400], seed=2, tune=t1)
+    hb, _ = tracer.trace_batch(ws, dscenes=ds, rays=[800, 400], seed=2)
+    for i in range(2):
+        assert np.allclose(ha[i]["energy"], hb[i]["energy"], rtol=1e-9, atol=1e-30)

@@ -141,3 +141,22 @@ def test_learned_emission_is_unbiased():
             mu, ml = tu[:, r, o].mean(), tl[:, r, o].mean()
             se = math.sqrt(tu[:, r, o].var(ddof=1) / 6 + tl[:, r, o].var(ddof=1) / 6)
             assert abs(mu - ml) < 4 * se + 1e-3 * mu, (r, o, mu, ml, se)
+
+
+def test_per_primary_capture_matches_bins():
+    w = rooms.shoebox_c1()
+    h1, _ = tracer.trace(w, rays=1500, seed=4, capture=1)
+    h2, _ = tracer.trace(w, rays=1500, seed=4, capture=2)
+    per = h2["capture"].astype(np.float64)            # [N][R][4]
+    assert per.shape == (1500, len(w.receivers), 4)
+    assert np.allclose(per.sum(axis=0), h1["capture"].astype(np.float64).sum(axis=2), rtol=1e-4)
+    # each primary's energy lands in its emission-direction bin
+    d = proposal.emission_directions(4, 0, 1500, len(w.sources), w.sources[0].kind)
+    b = proposal.direction_bins_of(d)
+    binned = np.zeros((len(w.receivers), 4, MO.N_BINS))
+    for r in range(len(w.receivers)):
+        for k in range(4):
+            binned[r, k] = np.bincount(b, weights=per[:, r, k], minlength=MO.N_BINS)
+    assert np.allclose(binned, h1["capture"], rtol=1e-3, atol=1e-9 * binned.max())
+    t = proposal.capture_targets_l2(h2["capture"], d)
+    assert t.shape == (len(w.receivers), MO.N_BINS) and np.allclose(t.sum(axis=1), 1.0, atol=1e-5)

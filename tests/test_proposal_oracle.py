@@ -115,3 +115,23 @@ def test_mixture_density_normalised():
     # bin-centre rule is accurate to ~1 % for kappa <= 55
     q = MO.mixture_density(out, d, 0.3)
     assert (q * om).sum() == pytest.approx(1.0, rel=2e-2)
+
+
+def test_vectorised_direction_bins_match_library():
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=(3000, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    v[:6] = [[1, 0, 0], [0, -1, 0], [0, 0, 1], [0.5, 0.5, 0.5], [-0.3, 0.3, -0.3], [0, 1e-9, -1]]
+    b = proposal.direction_bins_of(v)
+    assert all(int(b[i]) == proposal.direction_bin(v[i]) for i in range(len(v)))
+
+
+def test_second_moment_targets():
+    # two primaries in bin A each deliver the window-0 mean x 2 -> relative 2; bin B nothing
+    d, _ = MO.direction_bins()
+    dirs = np.stack([d[10], d[10], d[20], d[20]])
+    cap = np.zeros((4, 1, 4), dtype=np.float32)
+    cap[0, 0, 0] = cap[1, 0, 0] = 1.0
+    t = proposal.capture_targets_l2(cap, dirs)
+    assert t.shape == (1, MO.N_BINS)
+    assert t[0, 10] == pytest.approx(1.0) and t[0, 20] == 0.0
