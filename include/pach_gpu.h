@@ -120,7 +120,8 @@ typedef struct {
     const double *prim_weights;    /* optional [ray_count] emission weights (1/q) */
     const float *proposal;         /* optional [n_proposal][160] learned-proposal lobes (pach_proposal.h) */
     int32_t n_proposal;
-    int32_t reserved_q;            /* 0 */
+    int32_t bvh_format;            /* BVH nodes the trace kernel walks: 0 = default, 1 = 128-byte float
+                                      boxes, 2 = 64-byte nodes with 8-bit child boxes */
     double proposal_mix;           /* weight of uniform emission in the proposal, (0, 1]; 0 = 0.3 */
     double capture_edges_ms[3];    /* capture windows, ms after the direct arrival; zeros = 80, 400, 1200 */
 } pach_trace_params;
@@ -211,6 +212,16 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
  * room by its own primaries. */
 pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const pach_trace_params *params,
                              pach_run **out);
+
+/* Direct sound of point sources (Direct_Sound.Check_Validity and the unobstructed-path energy,
+ * Pachyderm_Acoustic_Universal/Classes_Direct.cs:654-685, 772-823; screen diffraction is not
+ * modelled): one visibility ray per (receiver, source) pair on the GPU.  Outputs, row-major by
+ * receiver then source: valid (1 = the receiver sees the source directly or through transmissive
+ * polygons), distance (m) and energy [..][8] = P 10^(-0.1 m L) prod(tau) / (4 pi L^2) -- the value the
+ * reference adds to Io at floor((L / c - Time_Pt) fs).  distance and energy may be NULL. */
+pach_status pach_direct_sound(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
+                              const pach_receiver_desc *receivers, int32_t n_receivers, int32_t *valid,
+                              double *distance, double *energy);
 
 /* Autotuner (no counterpart in the reference): times sample runs of the rooms (sample_rays primaries
  * shared among them in proportion to their ray counts) over candidate packet sizes and block shapes,

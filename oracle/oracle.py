@@ -241,3 +241,32 @@ def center_time(etc, fs=1000, direct=0.0, pressure=False):
 def strength(etc, swl, pressure=False):
     e = np.ascontiguousarray(etc, dtype=np.float64)
     return lib().orc_strength(_dp(e), e.size, swl, int(pressure))
+
+
+def direct_sound(workload, grid_domain=7):
+    """Direct_Sound validity and energy per (receiver, source) (orc_direct): valid [R][S], distance
+    [R][S], energy [R][S][8]."""
+    L = lib()
+    if not hasattr(L.orc_direct, "_declared"):
+        L.orc_direct.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.POINTER(OrcSource), C.c_int32,
+                                 C.POINTER(OrcReceiver), C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]
+        L.orc_direct.restype = C.c_int
+        L.orc_direct._declared = True
+    sh = _SceneHolder(workload.scene)
+    ns, nr = len(workload.sources), len(workload.receivers)
+    srcs = (OrcSource * ns)()
+    for i, s in enumerate(workload.sources):
+        srcs[i].origin[:] = list(s.origin)
+        srcs[i].power_db[:] = list(s.power_db)
+        srcs[i].kind = s.kind
+    recs = (OrcReceiver * max(nr, 1))()
+    for i, r in enumerate(workload.receivers):
+        recs[i].origin[:] = list(r.origin)
+        recs[i].radius = r.radius
+    valid = np.zeros((nr, ns), dtype=np.int32)
+    dist = np.zeros((nr, ns))
+    energy = np.zeros((nr, ns, 8))
+    L.orc_direct(C.byref(sh.desc), grid_domain, ns, srcs, nr, recs, valid.ctypes.data_as(C.POINTER(C.c_int32)),
+                 _dp(dist), _dp(energy))
+    return valid, dist, energy

@@ -735,6 +735,47 @@ int orc_shoot(const orc_scene_desc *scene, int32_t grid_domain, int32_t brute_fo
     return 1;
 }
 
+/* Direct_Sound.Check_Validity and the direct-path energy (Classes_Direct.cs:654-685, 772-823): shoot
+ * from the source towards the receiver; a hit before the full source-receiver distance through a
+ * polygon with any transmission multiplies the band transmissions and continues from the hit point
+ * (its next hit again compared with the full distance, as coded); energy
+ * P 10^(-0.1 m L) prod(tau) / (4 pi L^2). */
+int orc_direct(const orc_scene_desc *scene, int32_t grid_domain, int32_t n_src, const orc_source *src,
+               int32_t n_rec, const orc_receiver *rec, int32_t *valid, double *distance, double *energy) {
+    Scene S;
+    build_scene(scene, grid_domain, false, false, S);
+    Tracer tr(S);
+    for (int k = 0; k < n_rec; ++k)
+        for (int s = 0; s < n_src; ++s) {
+            const size_t p = (size_t)k * n_src + s;
+            const V3 so{src[s].origin[0], src[s].origin[1], src[s].origin[2]};
+            const V3 ro{rec[k].origin[0], rec[k].origin[1], rec[k].origin[2]};
+            V3 d = V3{ro.x - so.x, ro.y - so.y, ro.z - so.z};
+            const double L = std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+            d = normalized(d);
+            double tm[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+            V3 o = so;
+            int ok = 1;
+            for (int c = 0; c < 64; ++c) {
+                Hit h;
+                if (!tr.shoot(o, d, h)) { ok = 1; break; }
+                ok = h.t >= L ? 1 : 0;
+                bool transmissive = false;
+                for (int b = 0; b < 8; ++b) transmissive = transmissive || S.trans[h.poly * 8 + b] > 0;
+                if (ok || !transmissive) break;
+                for (int b = 0; b < 8; ++b) tm[b] *= S.trans[h.poly * 8 + b];
+                o = h.x;
+            }
+            valid[p] = ok;
+            distance[p] = L;
+            for (int b = 0; b < 8; ++b) {
+                const double P = 1e-12 * std::pow(10.0, 0.1 * src[s].power_db[b]);
+                energy[p * 8 + b] = P * std::pow(10.0, -0.1 * S.atten[b] * L) * tm[b] / (4 * M_PI * L * L);
+            }
+        }
+    return 0;
+}
+
 int orc_specular_paths(const orc_scene_desc *scene, int32_t grid_domain, int32_t brute_force,
                        int32_t n, const double *origins, const double *dirs, int32_t max_bounces,
                        int32_t *poly_out, double *t_out, double *pts_out) {

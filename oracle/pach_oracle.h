@@ -120,6 +120,8 @@ int orc_specular_paths(const orc_scene_desc *scene, int32_t grid_domain, int32_t
                        int32_t *poly_out, double *t_out, double *pts_out);
 
 /* Nearest hit of one ray (t > 1e-10) -- grid and brute force share this entry. */
+int orc_direct(const orc_scene_desc *scene, int32_t grid_domain, int32_t n_src, const orc_source *src,
+               int32_t n_rec, const orc_receiver *rec, int32_t *valid, double *distance, double *energy);
 int orc_shoot(const orc_scene_desc *scene, int32_t grid_domain, int32_t brute_force,
               const double o[3], const double d[3], int32_t *poly, double *t, double hit[3]);
 

@@ -54,7 +54,7 @@ class TraceParams(C.Structure):
                 ("kernel_timing", C.c_int32), ("ray_sort", C.c_int32),
                 ("traversal", C.c_int32), ("capture", C.c_int32),
                 ("prim_dirs", _dp), ("prim_weights", _dp),
-                ("proposal", C.POINTER(C.c_float)), ("n_proposal", C.c_int32), ("reserved_q", C.c_int32),
+                ("proposal", C.POINTER(C.c_float)), ("n_proposal", C.c_int32), ("bvh_format", C.c_int32),
                 ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3)]
 
 
@@ -99,7 +99,7 @@ class Stats(C.Structure):
 
 # Every symbol include/pach_gpu.h declares (checked by the CPU test suite).
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
-           "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
+           "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_direct_sound", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
@@ -130,6 +130,8 @@ def _declare(L):
         "pach_batch_begin": (C.c_int, [C.POINTER(RoomDesc), C.c_int32, C.POINTER(TraceParams), C.POINTER(vp)]),
         "pach_autotune": (C.c_int, [C.POINTER(RoomDesc), C.c_int32, C.POINTER(TraceParams), C.c_int64, C.c_char_p,
                                     C.c_int32, C.POINTER(TuneResult)]),
+        "pach_direct_sound": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
+                                        _ip, _dp, _dp]),
         "pach_trace_poll": (C.c_int, [vp, C.POINTER(Progress)]),
         "pach_trace_cancel": (C.c_int, [vp]),
         "pach_trace_wait": (C.c_int, [vp, C.c_int64]),

@@ -55,11 +55,11 @@ struct pach_scene {
     int device = 0;
     HostScene hs;
     DevScene dev{};
-    DevMem tri, tri64, norm, mat, trans, bvh;
+    DevMem tri, tri64, norm, mat, trans, bvh, bvhq;
     std::mutex mu;
     ~pach_scene() {
         cudaSetDevice(device);
-        for (DevMem *m : {&tri, &tri64, &norm, &mat, &trans, &bvh}) m->release();
+        for (DevMem *m : {&tri, &tri64, &norm, &mat, &trans, &bvh, &bvhq}) m->release();
     }
 };
 
@@ -84,7 +84,7 @@ struct pach_run {
     int R = 0, T = 0, nsrc = 0;   // receivers and sources over all rooms
     // device buffers
     DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw, sortbins, dprop, dcap;
-    DevMem droom, droomprim, btri, btri64, bnorm, bmat, btrans, bbvh;
+    DevMem droom, droomprim, btri, btri64, bnorm, bmat, btrans, bbvh, bbvhq;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -103,7 +103,7 @@ struct pach_run {
         }
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
-                          &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh})
+                          &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh, &bbvhq})
             m->release();
     }
 };
@@ -128,7 +128,7 @@ cudaError_t upload(DevMem &m, const void *src, size_t bytes) {
 // set of arrays: triangle, polygon, plane and node ids are offset, and each scene's root is kept.
 struct SceneArrays {
     std::vector<float4> tri, norm, mat;
-    std::vector<float> trans, bvh;
+    std::vector<float> trans, bvh, bvhq;
     std::vector<double> tri64;
     int planes = 0;
     float t_eps = 0.f;
@@ -182,21 +182,39 @@ int append_scene(const HostScene &hs, SceneArrays &A) {
                 }
                 std::memcpy(f, &code, 4);
             }
+    const size_t q0 = A.bvhq.size();
+    A.bvhq.insert(A.bvhq.end(), hs.bvhq.begin(), hs.bvhq.end());
+    if (tri_off || node_off)
+        for (size_t q = 0; q < hs.bvhq.size() / kBvhQNodeFloats; ++q)
+            for (int k = 0; k < 4; ++k) {
+                float *f = &A.bvhq[q0 + q * kBvhQNodeFloats + 12 + k];
+                int code;
+                std::memcpy(&code, f, 4);
+                if (code == (int)0x80000000) continue;
+                if (code >= 0) code += node_off;
+                else {
+                    const int c = ~code;
+                    code = ~(((c >> 4) + tri_off) * 16 + (c & 15));
+                }
+                std::memcpy(f, &code, 4);
+            }
     A.t_eps = std::max(A.t_eps, (float)(2e-7 * hs.scale));
     A.has_trans = A.has_trans || hs.has_trans;
     return node_off;
 }
 
 cudaError_t upload_scene(const SceneArrays &A, DevMem &tri, DevMem &tri64, DevMem &norm, DevMem &mat, DevMem &trans,
-                         DevMem &bvh, DevScene &d) {
+                         DevMem &bvh, DevMem &bvhq, DevScene &d) {
     cudaError_t e;
     if ((e = upload(tri, A.tri.data(), A.tri.size() * sizeof(float4))) ||
         (e = upload(tri64, A.tri64.data(), A.tri64.size() * sizeof(double))) ||
         (e = upload(norm, A.norm.data(), A.norm.size() * sizeof(float4))) ||
         (e = upload(mat, A.mat.data(), A.mat.size() * sizeof(float4))) ||
         (e = upload(trans, A.trans.data(), A.trans.size() * sizeof(float))) ||
-        (e = upload(bvh, A.bvh.data(), A.bvh.size() * sizeof(float))))
+        (e = upload(bvh, A.bvh.data(), A.bvh.size() * sizeof(float))) ||
+        (e = upload(bvhq, A.bvhq.data(), A.bvhq.size() * sizeof(float))))
         return e;
+    d.bvhq = bvhq.as<float4>();
     d.tri = tri.as<float4>();
     d.tri64 = tri64.as<double>();
     d.pnormal = norm.as<float4>();
@@ -303,7 +321,7 @@ void run_worker(pach_run *run) {
         if (n_rooms > 1) {
             SceneArrays A;
             for (int i = 0; i < n_rooms; ++i) roots[i] = append_scene(run->rooms[i].scene->hs, A);
-            TRY(upload_scene(A, run->btri, run->btri64, run->bnorm, run->bmat, run->btrans, run->bbvh, S));
+            TRY(upload_scene(A, run->btri, run->btri64, run->bnorm, run->bmat, run->btrans, run->bbvh, run->bbvhq, S));
         }
         // receivers, sources, powers and room table over all rooms
         std::vector<float4> rec(std::max(R, 1)), src;
@@ -381,7 +399,9 @@ void run_worker(pach_run *run) {
         const int threads = run->p.block_threads > 0 ? std::max(32, std::min(256, run->p.block_threads / 32 * 32)) : 256;
         int bps_tr = 0, bps_sh = 0;
         // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
-        const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max);
+        const bool quant = use_quantised_nodes(run->p.bvh_format);
+        if (!quant) S.bvhq = nullptr;  // trace_ray walks whichever node array is set
+        const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max, quant);
         TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
@@ -673,7 +693,7 @@ void run_worker(pach_run *run) {
     if (h_cancel) cudaFreeHost(h_cancel);
     // release the ring and the batch scene; histograms and counters stay until the run is destroyed
     for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw, &run->sortbins, &run->btri, &run->btri64,
-                      &run->bnorm, &run->bmat, &run->btrans, &run->bbvh})
+                      &run->bnorm, &run->bmat, &run->btrans, &run->bbvh, &run->bbvhq})
         m->release();
     if (e != cudaSuccess) return finish(PACH_ERR_CUDA, cuda_msg(e, where.c_str()), PACH_RUN_FAILED);
     finish(status, msg, final_state);
@@ -762,7 +782,7 @@ pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
     cudaGetDevice(&sc->device);
     SceneArrays A;
     append_scene(sc->hs, A);
-    const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->dev);
+    const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->bvhq, sc->dev);
     if (e != cudaSuccess) {
         delete sc;
         return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
@@ -1084,6 +1104,48 @@ pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, in
 }
 
 int32_t pach_direction_bin(double x, double y, double z) { return dir_bin((float)x, (float)y, (float)z); }
+
+pach_status pach_direct_sound(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
+                              const pach_receiver_desc *receivers, int32_t n_receivers, int32_t *valid,
+                              double *distance, double *energy) {
+    if (!scene || !sources || n_sources < 1 || n_receivers < 0 || (n_receivers > 0 && (!receivers || !valid)))
+        return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+    if ((long long)n_sources * n_receivers > (1ll << 30)) return fail(PACH_ERR_INVALID_ARGUMENT, "too many pairs");
+    if (n_receivers == 0) return PACH_OK;
+    cudaSetDevice(scene->device);
+    const HostScene &hs = scene->hs;
+    std::vector<double> s3(3 * (size_t)n_sources), r3(3 * (size_t)n_receivers);
+    for (int s = 0; s < n_sources; ++s)
+        for (int a = 0; a < 3; ++a) s3[3 * s + a] = sources[s].origin[a];
+    for (int k = 0; k < n_receivers; ++k)
+        for (int a = 0; a < 3; ++a) r3[3 * k + a] = receivers[k].origin[a];
+    const size_t npair = (size_t)n_sources * n_receivers;
+    DevMem ds, dr, dv, dt;
+    std::vector<int> v(npair);
+    std::vector<double> tm(npair * kBands);
+    cudaError_t e;
+    if ((e = upload(ds, s3.data(), s3.size() * sizeof(double))) || (e = upload(dr, r3.data(), r3.size() * sizeof(double))) ||
+        (e = dv.alloc(npair * sizeof(int))) || (e = dt.alloc(npair * kBands * sizeof(double))) ||
+        (e = launch_direct(scene->dev, ds.as<double>(), n_sources, dr.as<double>(), n_receivers, 64, dv.as<int>(),
+                           dt.as<double>(), 0)) ||
+        (e = cudaMemcpy(v.data(), dv.p, npair * sizeof(int), cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(tm.data(), dt.p, npair * kBands * sizeof(double), cudaMemcpyDeviceToHost)))
+        return fail(PACH_ERR_CUDA, cuda_msg(e, "direct sound"));
+    for (int k = 0; k < n_receivers; ++k)
+        for (int s = 0; s < n_sources; ++s) {
+            const size_t p = (size_t)k * n_sources + s;
+            const double dx = r3[3 * k] - s3[3 * s], dy = r3[3 * k + 1] - s3[3 * s + 1], dz = r3[3 * k + 2] - s3[3 * s + 2];
+            const double L = std::sqrt(dx * dx + dy * dy + dz * dz);
+            valid[p] = v[p];
+            if (distance) distance[p] = L;
+            if (energy)
+                for (int o = 0; o < kBands; ++o) {
+                    const double P = 1e-12 * std::pow(10.0, .1 * sources[s].power_db[o]);
+                    energy[p * kBands + o] = P * std::pow(10.0, -.1 * hs.atten[o] * L) * tm[p * kBands + o] / (4 * M_PI * L * L);
+                }
+        }
+    return PACH_OK;
+}
 
 pach_status pach_proposal_sample(const float *proposal, int32_t n_prop, double mix, uint64_t seed, int64_t ray_begin,
                                  int32_t n, float *dirs, float *weights) {

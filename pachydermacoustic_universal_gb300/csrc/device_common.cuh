@@ -190,6 +190,45 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
     return true;
 }
 
+// The same step on a 64-byte quantised node: child bounds are 8-bit steps from the node's origin,
+// a power-of-two step per axis, so the slab distance q (s / d) + (origin - o) / d is one FMA per
+// bound as with float nodes (s / d is exact: s is a power of two).
+__device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int node, float ix, float iy, float iz,
+                                           float ox, float oy, float oz, float best, int *stack, int &sp,
+                                           int &next) {
+    const float4 *N = bvhq + (kBvhQNodeFloats / 4) * node;
+    const float4 H = __ldg(N);
+    const uint4 A = __ldg(reinterpret_cast<const uint4 *>(N + 1));
+    const uint4 B = __ldg(reinterpret_cast<const uint4 *>(N + 2));
+    const int4 ch = __ldg(reinterpret_cast<const int4 *>(N + 3));
+    const uint32_t e = __float_as_uint(H.w);
+    const float sx = __uint_as_float((e & 255u) << 23) * ix, sy = __uint_as_float(((e >> 8) & 255u) << 23) * iy,
+                sz = __uint_as_float(((e >> 16) & 255u) << 23) * iz;
+    const float bx = fmaf(H.x, ix, -ox), by = fmaf(H.y, iy, -oy), bz = fmaf(H.z, iz, -oz);
+    int id[4] = {ch.x, ch.y, ch.z, ch.w};
+    float tk[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float t0x = fmaf((float)((A.x >> (8 * k)) & 255u), sx, bx), t1x = fmaf((float)((A.y >> (8 * k)) & 255u), sx, bx);
+        const float t0y = fmaf((float)((A.z >> (8 * k)) & 255u), sy, by), t1y = fmaf((float)((A.w >> (8 * k)) & 255u), sy, by);
+        const float t0z = fmaf((float)((B.x >> (8 * k)) & 255u), sz, bz), t1z = fmaf((float)((B.y >> (8 * k)) & 255u), sz, bz);
+        const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.f));
+        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), best));
+        tk[k] = (tn <= tf && id[k] != kEmptyChild) ? tn : FLT_MAX;
+    }
+    cswap(tk[0], id[0], tk[1], id[1]);
+    cswap(tk[2], id[2], tk[3], id[3]);
+    cswap(tk[0], id[0], tk[2], id[2]);
+    cswap(tk[1], id[1], tk[3], id[3]);
+    cswap(tk[1], id[1], tk[2], id[2]);
+    if (tk[0] == FLT_MAX) return false;
+#pragma unroll
+    for (int k = 3; k >= 1; --k)
+        if (tk[k] != FLT_MAX && sp < kBvhStack) stack[sp++] = id[k];
+    next = id[0];
+    return true;
+}
+
 // Nearest hit along o + t d with t > t_eps, skipping triangles of plane `skip` (the surface the ray
 // leaves).  4-wide BVH, nearest-child-first walk with a per-thread stack of the other hit
 // children; a child box is entered only if the ray meets it before the best hit so far.
@@ -210,7 +249,8 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, int root, float t_e
         while (node >= 0) {
             ++w.nodes;
             int next;
-            if (!bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) {
+            if (!(S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                        : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))) {
                 if (sp == 0) { done = true; break; }
                 node = stack[--sp];
                 continue;

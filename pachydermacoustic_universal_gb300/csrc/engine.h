@@ -32,6 +32,7 @@ struct HostScene {
     // bits), unused; a child >= 0 is an inner node, < 0 the leaf ~(first * 16 + count - 1); an
     // empty slot has an inverted box.
     std::vector<float> bvh;          // [nodes*32]
+    std::vector<float> bvhq;         // [nodes*16]: the same tree with 8-bit child boxes (64-byte nodes)
     int bvh_nodes = 0, bvh_leaves = 0, bvh_depth = 0;
     double c = 343, rho = 1.2, rho_c = 411.6, atten[kBands] = {0};
     double scale = 1;                // largest box extent
@@ -39,6 +40,7 @@ struct HostScene {
 
 constexpr int kBvhStack = 64;
 constexpr int kBvhNodeFloats = 32;
+constexpr int kBvhQNodeFloats = 16;
 constexpr int kLeafMax = 8;      // largest leaf the node encoding holds
 constexpr int kLeafDefault = 4;  // leaf size used when the scene does not ask for one
 
@@ -49,7 +51,8 @@ struct DevScene {
     const float4 *pnormal;      // [npoly]
     const float4 *mat;          // [npoly*8]: (1-alpha, s_lo, s_mid, s_hi)
     const float *trans;         // [npoly*8]
-    const float4 *bvh;          // [nodes*4]
+    const float4 *bvh;          // [nodes*8] 128-byte nodes
+    const float4 *bvhq;         // [nodes*4] 64-byte quantised nodes (null: walk the 128-byte ones)
     int ntri;
     float t_eps;
     int has_trans;
@@ -218,12 +221,16 @@ cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count 
 // scenes of more than kSpecMinTris triangles: measured on a 20k-triangle hall it walks 1.5x faster than
 // one leaf at a time, while on a 12-triangle shoebox (a two-level tree) it is 10 % slower.
 constexpr int kSpecMinTris = 64;
-inline int trace_variant(int blocks_per_sm, int traversal, int ntri) {
+// quantised: walk the 64-byte nodes (variants for 4 and 6 blocks per SM), + 32.
+inline int trace_variant(int blocks_per_sm, int traversal, int ntri, bool quantised = false) {
     const int minb = blocks_per_sm > 0 ? blocks_per_sm : 4;
     const bool spec = traversal == 2 || (traversal == 0 && ntri > kSpecMinTris);
+    if (quantised) return 32 + (spec ? 16 : 0) + (minb >= 6 ? 6 : 4);
     if (spec) return 16 + (minb >= 6 ? 6 : 4);
     return minb;
 }
+// bvh_format of pach_trace_params: 0 default, 1 128-byte float nodes, 2 64-byte quantised nodes.
+inline bool use_quantised_nodes(int bvh_format) { return bvh_format == 2; }
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s);
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);
@@ -231,6 +238,8 @@ cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double
                          double *t, double *pts, cudaStream_t s);
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s);
 cudaError_t launch_prop_sample(const DevRun &r, long long p0, int n, float *dirs, float *weights, cudaStream_t s);
+cudaError_t launch_direct(const DevScene &S, const double *src, int nsrc, const double *rec, int nrec, int max_cross,
+                          int *valid, double *transmod, cudaStream_t s);
 
 // capi.cpp: read access to a scene handle (for entry points in other translation units)
 const HostScene *scene_host(const pach_scene *s);

@@ -239,6 +239,78 @@ void build_bvh(HostScene &hs, int leaf_max) {
     hs.tri_plane.swap(tl);
 }
 
+// 64-byte copy of the 4-wide BVH: per node a frame (origin of the children's union box and a
+// power-of-two step per axis, 255 steps spanning it) and each child's box as 8-bit steps, the lower
+// bound rounded down and the upper rounded up, so a decoded box always contains the float box.
+//   float4 (origin x, y, z, biased exponents ex | ey << 8 | ez << 16 as bits)
+//   uint4  (lo.x of children 0-3 as bytes, hi.x, lo.y, hi.y)
+//   uint4  (lo.z, hi.z, 0, 0)
+//   int4   child codes (as the 128-byte nodes)
+void quantize_bvh(HostScene &hs) {
+    const size_t nodes = hs.bvh.size() / kBvhNodeFloats;
+    hs.bvhq.assign(nodes * kBvhQNodeFloats, 0.f);
+    for (size_t q = 0; q < nodes; ++q) {
+        const float *f = &hs.bvh[q * kBvhNodeFloats];
+        int code[4];
+        for (int k = 0; k < 4; ++k) std::memcpy(&code[k], &f[24 + k], 4);
+        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        bool valid[4];
+        for (int k = 0; k < 4; ++k) {
+            valid[k] = code[k] != (int)0x80000000;
+            for (int a = 0; a < 3; ++a) valid[k] = valid[k] && std::isfinite(f[8 * a + k]) && std::isfinite(f[8 * a + 4 + k]);
+            if (!valid[k]) continue;
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], (double)f[8 * a + k]);
+                hi[a] = std::max(hi[a], (double)f[8 * a + 4 + k]);
+            }
+        }
+        float origin[3] = {0.f, 0.f, 0.f};
+        int ebias[3] = {127, 127, 127};
+        uint32_t qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0};  // 4 children x 8 bits each
+        for (int a = 0; a < 3; ++a) {
+            if (lo[a] > hi[a]) continue;  // no valid child: the node is never entered
+            origin[a] = (float)lo[a];
+            if ((double)origin[a] > lo[a]) origin[a] = std::nextafter(origin[a], -INFINITY);
+            const double ext = hi[a] - (double)origin[a];
+            int e = ext > 0 ? (int)std::ceil(std::log2(ext / 255.0)) : -126;
+            e = std::max(-126, std::min(127, e));
+            for (;;) {  // the decoded float boxes must contain every child box
+                const float s = std::ldexp(1.0f, e);
+                bool ok = true;
+                uint32_t L = 0, H = 0;
+                for (int k = 0; k < 4 && ok; ++k) {
+                    int ql = 255, qh = 0;  // invalid children: an inverted box (never tested: code check)
+                    if (valid[k]) {
+                        ql = (int)std::floor(((double)f[8 * a + k] - origin[a]) / s);
+                        qh = (int)std::ceil(((double)f[8 * a + 4 + k] - origin[a]) / s);
+                        ql = std::max(0, ql);
+                        while (ql > 0 && origin[a] + (float)ql * s > f[8 * a + k]) --ql;
+                        while (qh <= 255 && origin[a] + (float)qh * s < f[8 * a + 4 + k]) ++qh;
+                        if (qh > 255 || origin[a] + (float)ql * s > f[8 * a + k]) ok = false;
+                    }
+                    L |= (uint32_t)ql << (8 * k);
+                    H |= (uint32_t)std::min(qh, 255) << (8 * k);
+                }
+                if (ok || e >= 127) {
+                    qlo[a] = L;
+                    qhi[a] = H;
+                    ebias[a] = e + 127;
+                    break;
+                }
+                ++e;
+            }
+        }
+        float *g = &hs.bvhq[q * kBvhQNodeFloats];
+        g[0] = origin[0];
+        g[1] = origin[1];
+        g[2] = origin[2];
+        const uint32_t ex = (uint32_t)ebias[0] | ((uint32_t)ebias[1] << 8) | ((uint32_t)ebias[2] << 16);
+        std::memcpy(&g[3], &ex, 4);
+        const uint32_t words[8] = {qlo[0], qhi[0], qlo[1], qhi[1], qlo[2], qhi[2], 0u, 0u};
+        std::memcpy(&g[4], words, sizeof(words));
+        std::memcpy(&g[12], code, sizeof(code));
+    }
+}
 
 }  // namespace
 
@@ -510,6 +582,7 @@ bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err)
     }
 
     build_bvh(hs, d->bvh_leaf_max);
+    quantize_bvh(hs);
 
     medium_properties(d->temp_c, d->rel_humidity, d->pressure_hpa, d->air_choice, d->edge_correction, hs.atten,
                       &hs.c, &hs.rho);

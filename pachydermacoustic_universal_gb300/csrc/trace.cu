@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(DevRun r) {
 // Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
 // its next leaf and tests it; a lane whose walk has ended writes its hit and takes the next wave
 // item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
-template <int MINB, bool SPEC>
+template <int MINB, bool SPEC, bool QUANT>
 __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     WaveCtl *c = r.ctl;
     const unsigned long long m = c->m, head = c->head;
@@ -418,7 +418,9 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 if (have && node >= 0) {
                     ++w.nodes;
                     int next;
-                    if (bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) node = next;
+                    if (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                              : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
+                        node = next;
                     else node = sp ? stack[--sp] : kEmptyChild;
                     if (node < 0 && node != kEmptyChild && leaf == 0) {
                         leaf = node;
@@ -443,7 +445,8 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             while (node >= 0) {
                 ++w.nodes;
                 int next;
-                if (!bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)) {
+                if (!(QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                            : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))) {
                     if (sp == 0) { fin = true; break; }
                     node = stack[--sp];
                     continue;
@@ -614,6 +617,44 @@ __global__ void k_emit(DevRun r, long long p0, int n, double *out) {
     out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
 }
 
+// Direct-sound visibility (Direct_Sound.Check_Validity, Classes_Direct.cs:654-685): from each
+// source towards each receiver, shoot; a hit before the receiver distance through a transmissive
+// polygon multiplies the band transmission and the ray continues from the hit point, comparing its
+// next hit with the full source-receiver distance again (as coded); any other hit decides.
+__global__ void k_direct(DevScene S, const double *src, int nsrc, const double *rec, int nrec, int max_cross,
+                         int *valid, double *transmod) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nsrc * nrec) return;
+    const int k = p / nsrc, s = p % nsrc;
+    const double dx = rec[3 * k] - src[3 * s], dy = rec[3 * k + 1] - src[3 * s + 1], dz = rec[3 * k + 2] - src[3 * s + 2];
+    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    float3 o = make_float3((float)src[3 * s], (float)src[3 * s + 1], (float)src[3 * s + 2]);
+    const float3 d = make_float3((float)(dx / dist), (float)(dy / dist), (float)(dz / dist));
+    double tm[kBands];
+#pragma unroll
+    for (int b = 0; b < kBands; ++b) tm[b] = 1.0;
+    int plane = -1, ok = 1;
+    for (int c = 0; c < max_cross; ++c) {
+        float t;
+        int tri;
+        TraceWork w;
+        if (!trace_ray(S, 0, S.t_eps, o, d, plane, t, tri, w)) { ok = 1; break; }
+        ok = (double)t >= dist ? 1 : 0;
+        const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
+        const int poly = __float_as_int(B.w);
+        bool transmissive = false;
+        if (S.has_trans)
+            for (int b = 0; b < kBands; ++b) transmissive = transmissive || __ldg(S.trans + poly * kBands + b) > 0.f;
+        if (ok || !transmissive) break;
+        for (int b = 0; b < kBands; ++b) tm[b] *= (double)__ldg(S.trans + poly * kBands + b);
+        o = o + d * t;
+        plane = __float_as_int(A.w);
+    }
+    valid[p] = ok;
+#pragma unroll
+    for (int b = 0; b < kBands; ++b) transmod[(size_t)p * kBands + b] = tm[b];
+}
+
 __global__ void k_prop_sample(DevRun r, long long p0, int n, float *dirs, float *weights) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -657,14 +698,18 @@ cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// variant = blocks per SM (3..6) + 16 x speculative + 32 x quantised nodes
+#define PACH_TRACE_VARIANTS(X)                                                                         \
+    X(3, false, false) X(4, false, false) X(5, false, false) X(6, false, false) X(4, true, false)    \
+    X(6, true, false) X(4, false, true) X(6, false, true) X(4, true, true) X(6, true, true)
+
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s) {
     switch (variant) {
-        case 3: k_trace<3, false><<<blocks, threads, 0, s>>>(r); break;
-        case 5: k_trace<5, false><<<blocks, threads, 0, s>>>(r); break;
-        case 6: k_trace<6, false><<<blocks, threads, 0, s>>>(r); break;
-        case 16 + 4: k_trace<4, true><<<blocks, threads, 0, s>>>(r); break;
-        case 16 + 6: k_trace<6, true><<<blocks, threads, 0, s>>>(r); break;
-        default: k_trace<4, false><<<blocks, threads, 0, s>>>(r); break;
+#define PACH_LAUNCH(M, SP, Q) \
+    case M + (SP ? 16 : 0) + (Q ? 32 : 0): k_trace<M, SP, Q><<<blocks, threads, 0, s>>>(r); break;
+        PACH_TRACE_VARIANTS(PACH_LAUNCH)
+#undef PACH_LAUNCH
+        default: k_trace<4, false, false><<<blocks, threads, 0, s>>>(r); break;
     }
     return cudaGetLastError();
 }
@@ -677,12 +722,13 @@ cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t 
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade) {
     cudaError_t e;
     switch (variant) {
-        case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<3, false>, threads, 0); break;
-        case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<5, false>, threads, 0); break;
-        case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<6, false>, threads, 0); break;
-        case 16 + 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, true>, threads, 0); break;
-        case 16 + 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<6, true>, threads, 0); break;
-        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false>, threads, 0); break;
+#define PACH_OCC(M, SP, Q)                                                                           \
+    case M + (SP ? 16 : 0) + (Q ? 32 : 0):                                                           \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<M, SP, Q>, threads, 0); \
+        break;
+        PACH_TRACE_VARIANTS(PACH_OCC)
+#undef PACH_OCC
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false, false>, threads, 0); break;
     }
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade, threads, smem_shade);
@@ -696,6 +742,13 @@ cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double
 
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s) {
     k_emit<<<(n + 127) / 128, 128, 0, s>>>(r, p0, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_direct(const DevScene &S, const double *src, int nsrc, const double *rec, int nrec, int max_cross,
+                          int *valid, double *transmod, cudaStream_t s) {
+    const int n = nsrc * nrec;
+    k_direct<<<(n + 127) / 128, 128, 0, s>>>(S, src, nsrc, rec, nrec, max_cross, valid, transmod);
     return cudaGetLastError();
 }
 

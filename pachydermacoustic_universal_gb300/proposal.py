@@ -176,7 +176,7 @@ def emission_directions(seed: int, ray_begin: int, n: int, n_sources: int, kind:
     return out
 
 
-def collect(workloads, rays: int, seed: int = 1, target: str = "l2", **kw):
+def collect(workloads, rays: int, seed: int = 1, target: str = "linear", **kw):
     """Trace each workload with uniform emission and capture on; returns (cond [n][12], target [n][1536],
     wall seconds of the traces).  target "l2": per-primary capture and capture_targets_l2; "linear":
     per-bin capture and capture_targets."""

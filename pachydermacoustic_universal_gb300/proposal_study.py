@@ -105,7 +105,7 @@ def bias_z(Pu, Pl):
 
 
 def study(train_rooms=200, train_rays=100_000, eval_rooms=50, eval_rays=10_000, seeds=8, steps=3000, lr=1e-3,
-          mixes=(0.3,), seed=7, train_receivers=12, target="l2", log=print):
+          mixes=(0.3,), seed=7, train_receivers=12, target="linear", log=print):
     t0 = time.perf_counter()
     rooms_train = [rooms.proposal_room_c4(1000 + i, n_receivers=train_receivers) for i in range(train_rooms)]
     cond, tgt, t_collect = proposal.collect(rooms_train, train_rays, seed=seed, target=target)
@@ -190,7 +190,7 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--mix", type=float, nargs="+", default=[0.3])
     ap.add_argument("--train-receivers", type=int, default=12)
-    ap.add_argument("--target", default="l2", choices=["l2", "linear"])
+    ap.add_argument("--target", default="linear", choices=["linear", "l2"])
     a = ap.parse_args()
     s = study(a.train_rooms, a.train_rays, a.eval_rooms, a.eval_rays, a.seeds, a.steps, a.lr, tuple(a.mix),
               train_receivers=a.train_receivers, target=a.target)

@@ -322,6 +322,121 @@ class SplitRayTracer:
             self._run = None
 
 
+class Direct_Sound:
+    """Direct sound of point sources (Classes_Direct.cs:232-262, 654-835), visibility rays on the GPU
+    (pach_direct_sound).  Io, Time_Pt, Validity and the direction arrays are filled as the reference
+    fills them, quirks included: Time_Pt adds Delay_ms to seconds; with ScreenCalc off the direct energy
+    enters Io even when the path is blocked (ETCurve adds it only where IsOccluded, i.e. Validity, is
+    true); a cluster's Validity is the last member's; negative direction components land in sample 0.
+    Screen diffraction (ScreenCalc) and line / surface sources are not modelled."""
+
+    def __init__(self, Src_in, Rec_in, Room_in, Octaves, ScreenCalc=False, SPL_Only=False):
+        if ScreenCalc:
+            raise NotImplementedError("screen diffraction is not part of the GPU engine")
+        self.SPL_Only = bool(SPL_Only)
+        self.Delay_ms = 0.0
+        self.Src = Src_in
+        self.Room = Room_in
+        self.Oct_choice = list(Octaves)
+        self.C_Sound = Room_in.Sound_speed(0)
+        self.SampleFreq = Rec_in.SampleRate
+        self.CO_Time = Rec_in.CutOffTime
+        self.Receiver = Rec_in.Origins()
+        R = len(self.Receiver)
+        self.Validity = [False] * R
+        self.Io = [None] * R
+        self.Time_Pt = np.zeros(R)
+        self.Dir_Rec_Pos = [None] * R
+        self.Dir_Rec_Neg = [None] * R
+        self.Rho_C = [Room_in.Rho_C(0)] * R
+
+    def Begin(self):
+        self.Calculate()
+
+    def Calculate(self):
+        srcs = self.Src.Sources if isinstance(self.Src, SourceCluster) else [self.Src]
+        R, S = len(self.Receiver), len(srcs)
+        sa = (_capi.SourceDesc * S)()
+        for i, s in enumerate(srcs):
+            sa[i].origin[:] = list(s.Center)
+            sa[i].power_db[:] = [float(x) for x in s.SPL]
+            sa[i].kind = s.kind
+        ra = (_capi.ReceiverDesc * max(R, 1))()
+        for i, p in enumerate(self.Receiver):
+            ra[i].origin[:] = list(p)
+            ra[i].radius = 1.0
+        valid = np.zeros((R, S), dtype=np.int32)
+        dist = np.zeros((R, S))
+        energy = np.zeros((R, S, 8))
+        self.Room._need()
+        _capi.check(_capi.lib().pach_direct_sound(self.Room._dev.handle, sa, S, ra, R,
+                                                  valid.ctypes.data_as(C.POINTER(C.c_int32)), dptr(dist), dptr(energy)))
+        fs, c = self.SampleFreq, self.C_Sound
+        for i in range(R):
+            lo, hi = dist[i].min(), dist[i].max()
+            self.Time_Pt[i] = lo / c + self.Delay_ms
+            samples = 1 if self.SPL_Only else max(int(np.ceil((hi - lo) * fs / c)) + 100, 1)
+            Io = np.zeros((8, samples))
+            dp = np.zeros((8, samples, 3), dtype=np.float32)
+            dn = np.zeros((8, samples, 3), dtype=np.float32)
+            for s in range(S):
+                self.Validity[i] = bool(valid[i, s])
+                L = dist[i, s]
+                t = 0 if self.SPL_Only else int(np.floor((L / c - self.Time_Pt[i]) * fs))
+                t = min(max(t, 0), samples - 1)
+                Io[:, t] += energy[i, s]
+                d = (np.asarray(self.Receiver[i]) - np.asarray(srcs[s].Center)) / L
+                for oct in range(8):
+                    V = d * Io[oct, t]
+                    for a in range(3):
+                        if -V[a] > 0:
+                            dp[oct, t, a] -= np.float32(V[a])
+                        else:
+                            dn[oct, 0, a] -= np.float32(V[a])
+            self.Io[i], self.Dir_Rec_Pos[i], self.Dir_Rec_Neg[i] = Io, dp, dn
+
+    def IsOccluded(self, id):
+        return self.Validity[id]
+
+    def Time(self, Rec_ID):
+        return float(self.Time_Pt[Rec_ID])
+
+    def Min_Time(self, Rec_ID):
+        return float(self.Time_Pt[Rec_ID])
+
+    def EnergyValue(self, octave, Rec_ID):
+        return self.Io[Rec_ID].sum(axis=0) if octave > 7 else self.Io[Rec_ID][octave].copy()
+
+    def EnergySum(self, Rec_ID, t):
+        return float(self.Io[Rec_ID][:, t].sum()) if t < self.Io[Rec_ID].shape[1] else 0.0
+
+
+class IR_Construction:
+    """IR_Construction.ETCurve (Classes_Math.cs:1351-1475) for one source: the ray histogram delayed by
+    the direct sound's Delay_ms, plus the direct sound where it is unobstructed, placed from
+    ceil((Delay_ms / 1000 + Time_Pt) fs) (or sample 0 with StartAtZero).  Image-source paths (ISData)
+    are not part of this engine and must be None."""
+
+    @staticmethod
+    def ETCurve(Direct, ISData, RTData, CO_Time_ms, Sampling_Frequency, Octave, Rec_ID, StartAtZero):
+        if ISData is not None:
+            raise NotImplementedError("image sources are not part of the GPU engine")
+        delay = Direct.Delay_ms if Direct is not None else 0.0
+        if RTData is not None:
+            h = RTData.Rec_List[Rec_ID].GetEnergyHistogram(Octave)
+            pad = int(np.floor(delay / 1000.0 * RTData.SampleRate))
+            Histogram = np.zeros(pad + h.size)
+            Histogram[pad:] = h
+        else:
+            Histogram = np.zeros(int((CO_Time_ms + int(delay)) * 0.001 * Sampling_Frequency))
+        if Direct is not None and Direct.IsOccluded(Rec_ID):
+            start = 0 if StartAtZero else int(np.ceil((delay * 0.001 + Direct.Time(Rec_ID)) * Sampling_Frequency))
+            D = Direct.EnergyValue(Octave, Rec_ID)
+            n = max(0, min(D.size, Histogram.size - start))
+            Histogram[start:start + n] += D[:n]
+        return Histogram
+
+
 class AcousticalMath:
     """Room-acoustic parameters (Classes_Math.cs) computed by the library."""
 

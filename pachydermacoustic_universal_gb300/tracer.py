@@ -72,7 +72,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
                 pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
                 block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
                 ring_log2=0, kernel_timing=False, ray_sort=0, traversal=0, capture=False, capture_edges_ms=None,
-                proposal=None, proposal_mix=0.0):
+                proposal=None, proposal_mix=0.0, bvh_format=0):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -93,6 +93,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.kernel_timing = int(bool(kernel_timing))
     p.ray_sort = int(ray_sort)
     p.traversal = int(traversal)
+    p.bvh_format = int(bvh_format)
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
     p.capture = int(capture)

@@ -87,3 +87,14 @@ def test_autotune_picks_and_caches(tmp_path):
     hb, _ = tracer.trace_batch(ws, dscenes=ds, rays=[800, 400], seed=2)
     for i in range(2):
         assert np.allclose(ha[i]["energy"], hb[i]["energy"], rtol=1e-9, atol=1e-30)
+
+
+def test_quantised_nodes_trace_the_same_rays():
+    """64-byte nodes hold conservative boxes of the 128-byte ones: the nearest hits, and so every
+    histogram, are the same."""
+    for w in (rooms.shoebox_c1(), rooms.irregular_hall_c2(target_tris=4000)):
+        ds = tracer.DeviceScene(w.scene)
+        ha, sa = tracer.trace(w, dscene=ds, rays=1500, seed=21, bvh_format=1)
+        hb, sb = tracer.trace(w, dscene=ds, rays=1500, seed=21, bvh_format=2)
+        assert sa["segments"] == sb["segments"]
+        assert np.allclose(ha["energy"], hb["energy"], rtol=1e-9, atol=1e-30)

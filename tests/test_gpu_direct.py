@@ -1,0 +1,97 @@
+"""GPU checks of the direct sound (pach_direct_sound, Direct_Sound) against the FP64 oracle, and of
+the ETC assembly (IR_Construction.ETCurve) with the split tracer's histograms."""
+import math
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from pachydermacoustic_universal_gb300 import rooms, tracer  # noqa: E402
+from pachydermacoustic_universal_gb300.simulation import (Direct_Sound, GeodesicSource, IR_Construction,  # noqa: E402
+                                                          Polygon_Scene, Receiver_Bank, SplitRayTracer)
+
+pytestmark = pytest.mark.gpu
+
+
+def _partitioned_room(tau):
+    """10 x 8 x 4 m shoebox with a partition at x = 5 up to z = 3 m (open above), transmission tau."""
+    b = rooms._Builder()
+    rooms._box_faces(b, (0, 0, 0), (10, 8, 4))
+    p = [b.vertex(q) for q in [(5, 0, 0), (5, 8, 0), (5, 8, 3), (5, 0, 3)]]
+    b.quad_tris(p[0], p[1], p[2], p[3])
+    v, offs, idx = b.arrays()
+    P = offs.size - 1
+    trans = np.zeros((P, 8))
+    trans[-2:] = tau
+    scene = rooms.SceneArrays(v, offs, idx, np.full((P, 8), 0.2), np.full((P, 8), 0.2), trans)
+    srcs = [rooms.SourceSpec((2.0, 4.0, 1.5)), rooms.SourceSpec((2.5, 2.0, 2.0), (100.0,) * 8)]
+    recs = [rooms.ReceiverSpec(q) for q in [(8.0, 4.0, 1.5), (8.0, 6.0, 3.9), (3.0, 6.0, 1.0), (9.0, 1.0, 0.5)]]
+    return rooms.Workload("partitioned", scene, srcs, recs, 1000, 2.0)
+
+
+def _gpu_direct(w):
+    ds = tracer.DeviceScene(w.scene)
+    import ctypes as C
+    from pachydermacoustic_universal_gb300 import _capi
+    sa = tracer.source_array(w.sources)
+    ra = tracer.receiver_array(w.receivers)
+    R, S = len(w.receivers), len(w.sources)
+    valid = np.zeros((R, S), dtype=np.int32)
+    dist = np.zeros((R, S))
+    energy = np.zeros((R, S, 8))
+    _capi.check(_capi.lib().pach_direct_sound(ds.handle, sa, S, ra, R, valid.ctypes.data_as(C.POINTER(C.c_int32)),
+                                              _capi.dptr(dist), _capi.dptr(energy)))
+    return valid, dist, energy
+
+
+@pytest.mark.parametrize("tau", [0.0, 0.25])
+def test_direct_sound_matches_oracle(tau):
+    for w in (_partitioned_room(tau), rooms.irregular_hall_c2(target_tris=3000)):
+        vg, dg, eg = _gpu_direct(w)
+        vo, do, eo = O.direct_sound(w)
+        assert np.array_equal(vg, vo)
+        assert np.allclose(dg, do, rtol=1e-12)
+        assert np.allclose(eg, eo, rtol=1e-6)
+    w = _partitioned_room(tau)
+    vg, _, eg = _gpu_direct(w)
+    # receiver 0 is behind the partition from both sources: visible only through it
+    assert vg[0, 0] == (1 if tau > 0 else 0) and vg[2, 0] == 1
+    L = math.dist(w.sources[0].origin, w.receivers[0].origin)
+    att, _, _ = tracer.medium_properties()
+    expect = 1.0 * 10 ** (-0.1 * att[3] * L) * tau / (4 * math.pi * L * L)
+    assert eg[0, 0, 3] == pytest.approx(expect, rel=1e-6)
+
+
+def test_etc_assembly_places_the_direct_sound():
+    w = rooms.shoebox_c1()
+    room = Polygon_Scene.from_arrays(w.scene)
+    room.partition()
+    src = GeodesicSource(list(w.sources[0].power_db), w.sources[0].origin)
+    bank = Receiver_Bank([r.origin for r in w.receivers], src, room, 1000, 2000.0)
+    for r in bank.Rec_List:
+        r.Radius = 0.5
+    rt = SplitRayTracer(src, bank, room, 2.0 * room.Sound_speed(0), [0, 7], 0, 5000)
+    rt.Begin()
+    rt.Combine_ThreadLocal_Results()
+    direct = Direct_Sound(src, bank, room, list(range(8)))
+    direct.Begin()
+    c = room.Sound_speed(0)
+    for k, rec in enumerate(bank.Rec_List):
+        L = math.dist(rec.Origin, src.Origin)
+        assert direct.IsOccluded(k)
+        assert direct.Time(k) == pytest.approx(L / c, rel=1e-12)
+        etc = IR_Construction.ETCurve(direct, None, bank, 2000.0, 1000, 4, k, False)
+        raw = rec.GetEnergyHistogram(4)
+        start = int(math.ceil(L / c * 1000))
+        dE = etc - np.concatenate([raw, np.zeros(etc.size - raw.size)])
+        assert np.argmax(dE) == start
+        assert dE.sum() == pytest.approx(direct.Io[k][4].sum(), rel=1e-12)
+        P = 1e-12 * 10 ** (0.1 * src.SPL[4])
+        assert direct.Io[k][4].sum() == pytest.approx(P * 10 ** (-0.1 * room.Attenuation(0)[4] * L) /
+                                                      (4 * math.pi * L * L), rel=1e-9)
+    rt.close()
