@@ -399,7 +399,7 @@ void run_worker(pach_run *run) {
         const int threads = run->p.block_threads > 0 ? std::max(32, std::min(256, run->p.block_threads / 32 * 32)) : 256;
         int bps_tr = 0, bps_sh = 0;
         // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
-        const bool quant = use_quantised_nodes(run->p.bvh_format);
+        const bool quant = use_quantised_nodes(run->p.bvh_format, ntri_max);
         if (!quant) S.bvhq = nullptr;  // trace_ray walks whichever node array is set
         const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max, quant);
         TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh));
