@@ -186,8 +186,9 @@ class SourceCluster(Source):
 
 
 class Spherical_Receiver:
-    def __init__(self, Center, SampleRate, CO_Time_ms, rho_c):
+    def __init__(self, Center, SampleRate, CO_Time_ms, rho_c, Sound_Speed=343.0):
         self.Origin = tuple(float(x) for x in Center)
+        self.Sound_Speed = float(Sound_Speed)
         self.Radius = 1.0          # Classes_Receivers.cs:751
         self.SampleRate = SampleRate
         self.CO_Time = CO_Time_ms
@@ -222,7 +223,8 @@ class Receiver_Bank:
         self.SampleCT = int(np.floor(COTime_in * SampleRate_in / 1000))
         self.SWL = SrcPT.SWL()
         rho_c = Sc.Rho_C(0)
-        self.Rec_List = [Spherical_Receiver(p, self.SampleRate, self.CutOffTime, rho_c) for p in Pt]
+        c = Sc.Sound_speed(0)
+        self.Rec_List = [Spherical_Receiver(p, self.SampleRate, self.CutOffTime, rho_c, c) for p in Pt]
 
     def Origins(self):
         return [r.Origin for r in self.Rec_List]
