@@ -331,14 +331,15 @@ def main():
     achieved_gbs = k_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
     oct_launch = agg["waves"]
     # the on-chip side of the walk: BVH node (128 B) and triangle (48 B) reads served by L1/L2
-    bvh_gbs = ((128.0 * agg["bvh_nodes_visited"] + 48.0 * agg["tri_tests"]) / (agg["trace_ms"] * 1e-3) / 1e9
+    node_bytes = float(stats[0]["walk"] % 1000) or 128.0
+    bvh_gbs = ((node_bytes * agg["bvh_nodes_visited"] + 48.0 * agg["tri_tests"]) / (agg["trace_ms"] * 1e-3) / 1e9
                if agg["trace_ms"] > 0 else None)
     tris = sum(w.scene.n_triangles for w in rooms_)
     cfg = {"workload": rooms_[0].name if not batched else f"batched_{len(rooms_)}_rooms",
            "rays_per_step": B, "rays_total": B * args.steps * ws, "triangles": tris,
            "sources": sum(len(w.sources) for w in rooms_), "receivers": sum(len(w.receivers) for w in rooms_),
            "cutoff_s": max(w.cutoff_s for w in rooms_), "bins_ms": 1, "l2": "256 MiB buffer written between steps",
-           "bvh_nodes_leaves_depth": stats[0]["accel"]}
+           "bvh_nodes_leaves_depth": stats[0]["accel"], "walk": stats[0]["walk"]}
     if batched:
         cfg["rooms"] = len(rooms_)
         cfg["ray_scale"] = args.ray_scale
@@ -358,8 +359,8 @@ def main():
                      "per_unit": ("56 B per octave segment" if kern == "k_trace" else
                                   "72 B in + 64 B per output ray per octave segment + 48 B per detection"),
                      "bvh_reads_gbs": bvh_gbs,
-                     "bvh_reads_note": "BVH node (128 B) and triangle (48 B) reads of the walk per second of "
-                                       "k_trace, served by L1/L2 (the walk's binding resource is on-chip)"},
+                     "bvh_reads_note": f"BVH node ({node_bytes:.0f} B) and triangle (48 B) reads of the walk per "
+                                       "second of k_trace, served by L1/L2 (the walk's binding resource is on-chip)"},
         "detail": {"trace_ms": agg["trace_ms"], "shade_ms": agg["shade_ms"], "broadband_ms": agg["broadband_ms"],
                    "waves": agg["waves"], "wall_s": wall, "segments": agg["segments"],
                    "detections": agg["detections"], "fp64_retests": agg["fp64_retests"],

@@ -110,9 +110,10 @@ typedef struct {
     int32_t ray_sort;              /* 1: order each wave by (direction octant, origin cell) before tracing;
                                       0 = default (off: measured +6 % walk rate in the 20k-triangle
                                       hall, less than the sort costs) */
-    int32_t traversal;             /* BVH walk of the trace kernel: 0 = default, 1 = one leaf at a time,
-                                      2 = speculative (lanes holding a leaf keep descending until the
-                                      whole warp holds one, then the warp tests its leaves together) */
+    int32_t traversal;             /* BVH walk: 0 = default, 1 = one leaf at a time, 2 = speculative
+                                      (lanes holding a leaf keep descending until the whole warp holds
+                                      one, then the warp tests its leaves together), 3 = in the shading
+                                      kernel (no separate walk pass; the default up to 64 triangles) */
     int32_t capture;               /* 1: record energy per receiver, time window and emission-direction
                                       bin; 2: per primary, receiver and time window
                                       (pach_trace_get_capture, pach_proposal.h) */
@@ -180,7 +181,7 @@ typedef struct {
     int64_t tri_tests;             /* octave-ray traversal work: triangles tested */
     double wall_ms;
     int32_t accel[3];              /* BVH inner nodes, leaves, depth */
-    int32_t reserved;
+    int32_t walk;                  /* the walk used: BVH node bytes (64 or 128) + 1000 x traversal (1-3) */
 } pach_stats;
 
 typedef struct pach_scene pach_scene;

@@ -87,7 +87,7 @@ class Stats(C.Structure):
                 ("sort_ms", C.c_double),
                 ("waves", C.c_int64), ("kernel_launches", C.c_int64), ("peak_live_rays", C.c_int64),
                 ("bvh_nodes_visited", C.c_int64), ("tri_tests", C.c_int64),
-                ("wall_ms", C.c_double), ("accel", C.c_int32 * 3), ("reserved", C.c_int32)]
+                ("wall_ms", C.c_double), ("accel", C.c_int32 * 3), ("walk", C.c_int32)]
 
     def to_dict(self):
         out = {}

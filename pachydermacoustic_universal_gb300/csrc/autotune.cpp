@@ -2,8 +2,9 @@
 // timing short sample runs, and remembers the choice in a small text cache.
 //
 // Knobs (pach_trace_params): wave_kilo_items (octave rays per wave, the packet), block_threads and
-// blocks_per_sm (block shape and the trace kernel's register variant), traversal (one leaf at a time
-// or speculative).  Search: coordinate descent from the defaults -- traversal x register variant,
+// blocks_per_sm (block shape and the trace kernel's register variant), traversal (one leaf at a time,
+// speculative, or inside the shading kernel).  Search: coordinate descent from the defaults --
+// traversal x register variant,
 // then the wave size, then the block size -- each candidate timed on a sample of the rooms' primaries
 // (device time per segment of the whole run, the stats' device_ms).  No counterpart in the reference.
 #include <algorithm>
@@ -153,6 +154,7 @@ extern "C" pach_status pach_autotune(const pach_room_desc *rooms, int32_t n_room
     };
     for (int trav : {1, 2})
         for (int bps : {4, 6}) consider(Knobs{cur.wave_kilo, cur.threads, bps, trav});
+    consider(Knobs{cur.wave_kilo, cur.threads, 4, 3});  // the walk inside the shading kernel
     const Knobs stage1 = best;
     for (int w : {512, 1024, 4096}) consider(Knobs{w, stage1.threads, stage1.bps, stage1.traversal});
     const Knobs stage2 = best;

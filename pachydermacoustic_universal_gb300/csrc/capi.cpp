@@ -402,6 +402,7 @@ void run_worker(pach_run *run) {
         const bool quant = use_quantised_nodes(run->p.bvh_format, ntri_max);
         if (!quant) S.bvhq = nullptr;  // trace_ray walks whichever node array is set
         const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max, quant);
+        const bool fused = fused_walk(run->p.traversal, ntri_max) && run->p.ray_sort <= 0;
         TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
@@ -511,9 +512,9 @@ void run_worker(pach_run *run) {
             if (timing && (x = cudaEventRecord(kev[6 * k + 2], stream))) return x;
             if (sorting && (x = launch_sort(r, sort_blocks, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 3], stream))) return x;
-            if ((x = launch_trace(r, tr_variant, tr_blocks, threads, stream))) return x;
+            if (!fused && (x = launch_trace(r, tr_variant, tr_blocks, threads, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 4], stream))) return x;
-            if ((x = launch_shade(r, sh_blocks, threads, stream))) return x;
+            if ((x = launch_shade(r, sh_blocks, threads, stream, fused))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 5], stream))) return x;
             return cudaSuccess;
         };
@@ -574,7 +575,7 @@ void run_worker(pach_run *run) {
                 if (e) break;
                 for (int k = 0; k < batch && !e; ++k, ++it) {
                     TRY(one_iteration(k));
-                    launches += sorting ? 8 : 5;
+                    launches += (sorting ? 8 : 5) - (fused ? 1 : 0);
                 }
                 if (e) break;
                 TRY(cudaMemcpyAsync(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
@@ -651,13 +652,14 @@ void run_worker(pach_run *run) {
         s.broadband_ms = t_bb;
         s.sort_ms = t_sort;
         s.waves = (int64_t)h_ctl->waves;
-        s.kernel_launches = timing ? launches : (long long)h_ctl->iters * (sorting ? 9 : 6);
+        s.kernel_launches = timing ? launches : (long long)h_ctl->iters * ((sorting ? 9 : 6) - (fused ? 1 : 0));
         s.peak_live_rays = (int64_t)h_ctl->peak_live;
         s.bvh_nodes_visited = (int64_t)h_cnt->bvh_nodes;
         s.tri_tests = (int64_t)h_cnt->tri_tests;
         s.accel[0] = (int32_t)(n_rooms > 1 ? run->bbvh.bytes / (kBvhNodeFloats * sizeof(float)) : hs.bvh_nodes);
         s.accel[1] = hs.bvh_leaves;
         s.accel[2] = hs.bvh_depth;
+        s.walk = (quant ? 64 : 128) + 1000 * (fused ? 3 : ((tr_variant & 16) ? 2 : 1));
         run->rays_done = (long long)h_cnt->primaries;
         run->segments = s.segments;
         run->end_traces = s.end_traces;
@@ -709,7 +711,7 @@ pach_status check_run(pach_run *run) {
 pach_status check_common(const pach_trace_params &p) {
     if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi) return fail(PACH_ERR_INVALID_ARGUMENT, "octave range must lie in 0..7");
     if (p.sample_rate < 1) return fail(PACH_ERR_INVALID_ARGUMENT, "sample_rate must be positive");
-    if (p.traversal < 0 || p.traversal > 2) return fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
+    if (p.traversal < 0 || p.traversal > 3) return fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0..3");
     const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
     if (T < 1 || T > (1ll << 24)) return fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");
     return PACH_OK;

@@ -207,11 +207,15 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
     const float bx = fmaf(H.x, ix, -ox), by = fmaf(H.y, iy, -oy), bz = fmaf(H.z, iz, -oz);
     int id[4] = {ch.x, ch.y, ch.z, ch.w};
     float tk[4];
+    // byte k of w as a float: one byte permute builds 2^23 + byte (bits 0x4B0000bb), one add removes 2^23
+    auto q = [](uint32_t w, int k) {
+        return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)) - 8388608.0f;
+    };
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const float t0x = fmaf((float)((A.x >> (8 * k)) & 255u), sx, bx), t1x = fmaf((float)((A.y >> (8 * k)) & 255u), sx, bx);
-        const float t0y = fmaf((float)((A.z >> (8 * k)) & 255u), sy, by), t1y = fmaf((float)((A.w >> (8 * k)) & 255u), sy, by);
-        const float t0z = fmaf((float)((B.x >> (8 * k)) & 255u), sz, bz), t1z = fmaf((float)((B.y >> (8 * k)) & 255u), sz, bz);
+        const float t0x = fmaf(q(A.x, k), sx, bx), t1x = fmaf(q(A.y, k), sx, bx);
+        const float t0y = fmaf(q(A.z, k), sy, by), t1y = fmaf(q(A.w, k), sy, by);
+        const float t0z = fmaf(q(B.x, k), sz, bz), t1z = fmaf(q(B.y, k), sz, bz);
         const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.f));
         const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), best));
         tk[k] = (tn <= tf && id[k] != kEmptyChild) ? tn : FLT_MAX;

@@ -223,7 +223,9 @@ cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count 
 constexpr int kSpecMinTris = 64;
 // quantised: walk the 64-byte nodes (variants for 4 and 6 blocks per SM), + 32.
 inline int trace_variant(int blocks_per_sm, int traversal, int ntri, bool quantised = false) {
-    const int minb = blocks_per_sm > 0 ? blocks_per_sm : 4;
+    // default: 6 blocks of 256 (40 registers) on the smaller quantised nodes (+2.5 % on a 20k-triangle
+    // hall), 4 (64 registers) on 128-byte nodes (+23 %)
+    const int minb = blocks_per_sm > 0 ? blocks_per_sm : (quantised ? 6 : 4);
     const bool spec = traversal == 2 || (traversal == 0 && ntri > kSpecMinTris);
     if (quantised) return 32 + (spec ? 16 : 0) + (minb >= 6 ? 6 : 4);
     if (spec) return 16 + (minb >= 6 ? 6 : 4);
@@ -238,7 +240,11 @@ inline bool use_quantised_nodes(int bvh_format, int ntri) {
     return bvh_format == 2 || (bvh_format == 0 && ntri > kQuantMinTris);
 }
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s);
-cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s);
+// fused: k_shade walks the rays itself (no k_trace launch) -- the default for scenes of at most
+// kFuseMaxTris triangles, or traversal = 3
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused = false);
+constexpr int kFuseMaxTris = 64;
+inline bool fused_walk(int traversal, int ntri) { return traversal == 3 || (traversal == 0 && ntri <= kFuseMaxTris); }
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
                          double *t, double *pts, cudaStream_t s);

@@ -75,7 +75,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "bad octave range, sample rate or cutoff");
     const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
     if (T < 1 || T > (1ll << 24)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");
-    if (p.traversal < 0 || p.traversal > 2) return na_fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
+    if (p.traversal < 0 || p.traversal > 3) return na_fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0..3");
     for (int i = 0; i < n_receivers; ++i)
         if (!(receivers[i].radius > 0)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "receiver radius must be positive");
     for (int s = 0; s < n_sources; ++s)
@@ -235,8 +235,9 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
                 NA_TRY(launch_feed(r, stream));
                 NA_TRY(launch_broadband(r, sms * 2, 128, stream));
                 NA_TRY(launch_wave(r, stream));
-                NA_TRY(launch_trace(r, variant, tr_blocks, 256, stream));
-                NA_TRY(launch_shade(r, sh_blocks, 256, stream));
+                const bool fused = fused_walk(p.traversal, (int)hs.tri_poly.size());
+                if (!fused) NA_TRY(launch_trace(r, variant, tr_blocks, 256, stream));
+                NA_TRY(launch_shade(r, sh_blocks, 256, stream, fused));
                 launches += 5;
             }
             NA_TRY(cudaMemcpyAsync(&h_ctl, base + kOffCtl, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));

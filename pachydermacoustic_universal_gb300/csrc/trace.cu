@@ -482,6 +482,9 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     }
 }
 
+// FUSED: walk the ray here instead of reading k_trace's hit (small scenes, whose walk is a few
+// cached nodes: the separate trace pass would only re-read the ray and round-trip its hit via HBM).
+template <bool FUSED>
 __global__ void __launch_bounds__(256) k_shade(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
     const float4 *s_rec = stage_receivers(r, s_rec_buf);
@@ -499,7 +502,19 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
         Ray R, C;
         if (j < m) {
             R = to_ray(load_item(wave_item(r, head, j), 0));
-            const int2 h = r.hits[j];
+            int2 h;
+            if constexpr (FUSED) {
+                float tt;
+                int tri;
+                TraceWork tw;
+                const int root = r.n_rooms > 1 ? __ldg(&r.rooms[R.room].bvh_root) : 0;
+                const float teps = r.n_rooms > 1 ? __ldg(&r.rooms[R.room].t_eps) : S.t_eps;
+                h = trace_ray(S, root, teps, R.p, R.d, R.plane, tt, tri, tw) ? make_int2(tri, __float_as_int(tt))
+                                                                              : make_int2(-1, 0);
+                L.v[C_RET] += tw.retests;
+            } else {
+                h = r.hits[j];
+            }
             const bool hit = h.x >= 0;
             const float t = __int_as_float(h.y);
             ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
@@ -714,8 +729,9 @@ cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s) {
-    k_shade<<<blocks, threads, rec_smem(r), s>>>(r);
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused) {
+    if (fused) k_shade<true><<<blocks, threads, rec_smem(r), s>>>(r);
+    else k_shade<false><<<blocks, threads, rec_smem(r), s>>>(r);
     return cudaGetLastError();
 }
 
@@ -731,7 +747,7 @@ cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int 
         default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false, false>, threads, 0); break;
     }
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade, threads, smem_shade);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false>, threads, smem_shade);
 }
 
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,

@@ -78,7 +78,7 @@ def test_autotune_picks_and_caches(tmp_path):
     t1 = tracer.autotune(ws, dscenes=ds, rays=[2000, 2000], sample_rays=600, cache_path=cache)
     assert t1["from_cache"] == 0 and t1["trials"] >= 5 and t1["segments_per_s"] > 0
     assert t1["wave_kilo_items"] in (512, 1024, 2048, 4096) and t1["block_threads"] in (128, 256)
-    assert t1["blocks_per_sm"] in (4, 6) and t1["traversal"] in (1, 2)
+    assert t1["blocks_per_sm"] in (4, 6) and t1["traversal"] in (1, 2, 3)
     t2 = tracer.autotune(ws, dscenes=ds, rays=[2000, 2000], sample_rays=600, cache_path=cache)
     assert t2["from_cache"] == 1
     assert all(t2[k] == t1[k] for k in tracer.TUNE_KNOBS)
@@ -99,3 +99,14 @@ def test_quantised_nodes_trace_the_same_rays():
         hb, sb = tracer.trace(w, dscene=ds, rays=1500, seed=21, bvh_format=2)
         assert abs(sa["segments"] - sb["segments"]) <= 1e-4 * sa["segments"]
         assert hb["energy"].sum() == pytest.approx(ha["energy"].sum(), rel=1e-3)
+
+
+def test_fused_walk_traces_the_same_rays():
+    """traversal 3 walks the rays inside the shading kernel with the same walk as the trace kernel's
+    one-leaf-at-a-time variant: identical hits, identical histograms."""
+    for w in (rooms.shoebox_c1(), rooms.irregular_hall_c2(target_tris=3000)):
+        ds = tracer.DeviceScene(w.scene)
+        ha, sa = tracer.trace(w, dscene=ds, rays=1500, seed=8, traversal=1)
+        hb, sb = tracer.trace(w, dscene=ds, rays=1500, seed=8, traversal=3)
+        assert sa["segments"] == sb["segments"]
+        assert np.allclose(ha["energy"], hb["energy"], rtol=1e-9, atol=1e-30)
