@@ -125,7 +125,29 @@ typedef struct {
                                       boxes, 2 = 64-byte nodes with 8-bit child boxes */
     double proposal_mix;           /* weight of uniform emission in the proposal, (0, 1]; 0 = 0.3 */
     double capture_edges_ms[3];    /* capture windows, ms after the direct arrival; zeros = 80, 400, 1200 */
+    const struct pach_map_desc *map; /* optional mapping receivers (single-room runs), else NULL */
 } pach_trace_params;
+
+/* Mapping receivers (PachMapReceiver, Pach_Map_Receiver.cs:34-1834): many small spheres, typically one
+ * per face or vertex of an audience mesh, found along each segment by a walk over a uniform grid of
+ * cells 4 x 4 x 2.5 increments.  Detection as Map_Receiver.CheckRay / CheckBroadbandRay
+ * (Pach_Map_Receiver.cs:1780-1826): energy I 10^(-0.1 m t) / (pi r^2) with t the arrival time in
+ * seconds AFTER the receiver's direct arrival (the reference's exponent takes that time, not a
+ * distance), no chord-length weight, 1 ms bins counted from the direct arrival, every band of a
+ * broadband ray.  The direct arrival is |source - receiver| / c for a single source and 0 for a
+ * cluster (Map_Receiver ctor, Pach_Map_Receiver.cs:1737-1751). */
+typedef struct pach_map_desc {
+    int32_t n_receivers;
+    int32_t time_1pt;              /* 1: one bin per band holding every arrival (Histogram_1Pt) */
+    const double *origins;         /* [3*n_receivers] sphere centres (PachMapReceiver.Partition places them) */
+    double increment;              /* sphere DIAMETER, m (radius = increment / 2) */
+    double cutoff_ms;              /* histogram length: (int)(cutoff_ms / 1000 * 1000) bins of 1 ms */
+    int32_t walk;                  /* 0: the grid walks as the reference writes them (the broadband walk steps
+                                      by the sign of the ray's POSITION and stops when any cell index reaches
+                                      the end cell's; the octave walk never visits the end cell);
+                                      1: every cell the segment crosses, end cell included */
+    int32_t reserved;
+} pach_map_desc;
 
 /* One room of a batch run (pach_batch_begin). */
 typedef struct {
@@ -253,6 +275,20 @@ pach_status pach_trace_wait(pach_run *run, int64_t timeout_ms);
 pach_status pach_trace_get_histograms(pach_run *run, int32_t scaled, double *energy, double *pressure,
                                       double *dir_pos, double *dir_neg, double *analysis, size_t cap_bins);
 pach_status pach_trace_get_stats(pach_run *run, pach_stats *stats);
+/* Map histograms of a run with mapping receivers, energy/pressure [M][8][T] (T = 1 with time_1pt),
+ * time 0 = each receiver's direct arrival.  scaled = 1: Histogram.Scale (energy and pressure / N,
+ * Classes_Receivers.cs:1211-1218), then x n_sources (Combine_ThreadLocal_Results, TaskAll:768-774).
+ * direct_time [M] seconds, sizes [2] = (M, T).  Any pointer may be NULL; cap_bins = capacity of
+ * energy and pressure in doubles. */
+pach_status pach_trace_get_map(pach_run *run, int32_t scaled, double *energy, double *pressure, double *direct_time,
+                               int32_t *sizes, size_t cap_bins);
+/* Room-acoustic parameters of every map receiver and band, computed on the device from the map
+ * histograms (Get_RT_Map, Get_EDT_Map, Get_Clarity_Map, Get_Definition_Map without coherent
+ * superposition, Pach_Map_Receiver.cs:925-1270: AcousticalMath.T_X / EarlyDecayTime of the Schroeder
+ * integral, Clarity / Definition with the start at bin 0).  Outputs [M][8] (NaN where the decay never
+ * reaches the fit limits, as T_X); any may be NULL.  energy_sum = the band's total scaled energy. */
+pach_status pach_map_parameters(pach_run *run, int32_t decay_depth, int32_t clarity_ms, double *t_x, double *edt,
+                                double *clarity, double *definition, double *energy_sum);
 void pach_run_destroy(pach_run *run);
 
 /* Synchronous convenience: begin + wait + histograms + stats. */

@@ -51,6 +51,11 @@ class OrcStats(C.Structure):
                 ("air_atten_db_per_m", C.c_double * 8)]
 
 
+class OrcMap(C.Structure):
+    _fields_ = [("n_receivers", C.c_int32), ("time_1pt", C.c_int32), ("origins", C.POINTER(C.c_double)),
+                ("increment", C.c_double), ("cutoff_ms", C.c_double), ("walk", C.c_int32), ("pad", C.c_int32)]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++ only)."""
     if force or not os.path.exists(_LIB_PATH) or \
@@ -69,6 +74,11 @@ def lib():
         L.orc_trace_ex.argtypes = [C.POINTER(OrcScene), C.c_int32, C.POINTER(OrcSource), C.c_int32,
                                    C.POINTER(OrcReceiver), C.POINTER(OrcParams), C.c_int64, C.c_int64,
                                    C.c_int32, dp, dp, dp, dp, dp, dp, dp, C.POINTER(OrcStats)]
+        L.orc_trace_map.restype = C.c_int
+        L.orc_trace_map.argtypes = [C.POINTER(OrcScene), C.c_int32, C.POINTER(OrcSource), C.c_int32,
+                                    C.POINTER(OrcReceiver), C.POINTER(OrcMap), C.POINTER(OrcParams), C.c_int64,
+                                    C.c_int64, C.c_int32, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp,
+                                    C.POINTER(OrcStats)]
         L.orc_specular_paths.restype = C.c_int
         L.orc_specular_paths.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, dp, dp, C.c_int32,
                                          C.POINTER(C.c_int32), dp, dp]
@@ -141,9 +151,11 @@ def emit_direction(seed, ray, n_src, kind):
 
 def trace(workload, *, seed=1, rays=None, ray_begin=0, threads=0, pure_specular=False, is_order=-1,
           grid_domain=7, brute_force=False, oct_range=(0, 7), prim_dirs=None, prim_weights=None,
-          max_broadband_bounces=0, max_segments_per_ray=0):
+          max_broadband_bounces=0, max_segments_per_ray=0, map_receivers=None):
     """Trace primaries [ray_begin, ray_begin+rays) of a rooms.Workload.  Returns RAW histogram sums
-    (energy, pressure, dir_pos, dir_neg, analysis) and a stats dict."""
+    (energy, pressure, dir_pos, dir_neg, analysis) and a stats dict.  map_receivers (an object with
+    origins [M][3], increment, cutoff_ms, time_1pt, walk) adds map_energy / map_pressure [M][8][Tm] and
+    map_direct [M] (PachMapReceiver)."""
     L = lib()
     sh = _SceneHolder(workload.scene)
     ns = len(workload.sources)
@@ -170,13 +182,24 @@ def trace(workload, *, seed=1, rays=None, ray_begin=0, threads=0, pure_specular=
     st = OrcStats()
     pd = np.ascontiguousarray(prim_dirs, dtype=np.float64) if prim_dirs is not None else None
     pw = np.ascontiguousarray(prim_weights, dtype=np.float64) if prim_weights is not None else None
-    rc = L.orc_trace_ex(C.byref(sh.desc), ns, srcs, nr, recs, C.byref(p), ray_begin, ray_begin + n, threads,
-                        _dp(pd), _dp(pw), _dp(E), _dp(P), _dp(Dp), _dp(Dn), _dp(An), C.byref(st))
+    out = {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}
+    mdesc, mE, mP, mD = None, None, None, None
+    if map_receivers is not None:
+        m = map_receivers
+        morg = np.ascontiguousarray(m.origins, dtype=np.float64).reshape(-1)
+        M = morg.size // 3
+        Tm = 1 if m.time_1pt else int(float(m.cutoff_ms) / 1000.0 * 1000.0)
+        mdesc = OrcMap(M, int(bool(m.time_1pt)), _dp(morg), float(m.increment), float(m.cutoff_ms), int(m.walk), 0)
+        mE, mP, mD = np.zeros((M, 8, Tm)), np.zeros((M, 8, Tm)), np.zeros(M)
+        out.update(map_energy=mE, map_pressure=mP, map_direct=mD)
+    rc = L.orc_trace_map(C.byref(sh.desc), ns, srcs, nr, recs, C.byref(mdesc) if mdesc is not None else None,
+                         C.byref(p), ray_begin, ray_begin + n, threads, _dp(pd), _dp(pw), _dp(E), _dp(P), _dp(Dp),
+                         _dp(Dn), _dp(An), _dp(mE), _dp(mP), _dp(mD), C.byref(st))
     if rc != 0:
         raise RuntimeError(f"orc_trace failed ({rc})")
     stats = {k: getattr(st, k) for k, _ in OrcStats._fields_}
     stats["air_atten_db_per_m"] = list(st.air_atten_db_per_m)
-    return {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}, stats
+    return out, stats
 
 
 def specular_paths(scene, origins, dirs, max_bounces, grid_domain=7, brute_force=False):

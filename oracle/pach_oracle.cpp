@@ -416,8 +416,115 @@ struct Hist {
 
 struct Rec { V3 o; double r2; };
 
+/* ----------------------------------------------------------------------------------------
+ * Mapping receivers (PachMapReceiver, Pach_Map_Receiver.cs).
+ * -------------------------------------------------------------------------------------- */
+struct MapBank {
+    int M = 0, T = 1, walk = 0;
+    bool one_pt = false;
+    double r = 0, r2 = 0, sizemod = 0, c = 343;
+    double atten[8] = {0};
+    std::vector<V3> org;
+    std::vector<double> direct;
+    double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0}, vd[3] = {1, 1, 1};
+    int n[3] = {1, 1, 1};
+    std::vector<std::vector<int>> inv;   /* Voxel_Inv, cell (x * ny + y) * nz + z */
+    const std::vector<int> &cell(int x, int y, int z) const { return inv[((size_t)x * n[1] + y) * n[2] + z]; }
+    double cmin(int a, int i) const { return (i * vd[a]) + mn[a]; }        /* Voxels[].Min_PT */
+    double cmax(int a, int i) const { return ((i + 1) * vd[a]) + mn[a]; }  /* Voxels[].Max_PT */
+};
+
+/* Fill_in + Partition (Pach_Map_Receiver.cs:78-263) and the Map_Receiver ctor (1721-1768) for
+ * receivers already placed. */
+bool build_map(const orc_map_desc *d, V3 src, int nsrc, double c, const double atten[8], MapBank &B) {
+    if (!d || d->n_receivers < 1 || !d->origins || !(d->increment > 0)) return false;
+    B.M = d->n_receivers;
+    B.one_pt = d->time_1pt != 0;
+    B.walk = d->walk;
+    B.T = B.one_pt ? 1 : (int)(d->cutoff_ms / 1000.0 * 1000.0);  /* Histogram(1000, COTime_in) */
+    if (B.T < 1) return false;
+    B.r = d->increment * 0.5;                                       /* Radius = Diameter * 0.5 */
+    B.r2 = B.r * B.r;
+    B.sizemod = 1 / (kPi * B.r2);
+    B.c = c;
+    for (int o = 0; o < 8; ++o) B.atten[o] = atten[o];
+    B.org.resize(B.M);
+    B.direct.assign(B.M, 0.0);
+    for (int k = 0; k < B.M; ++k) {
+        B.org[k] = {d->origins[3 * k], d->origins[3 * k + 1], d->origins[3 * k + 2]};
+        if (nsrc == 1) {  /* a SourceCluster leaves Direct_Time = min(0, ...) = 0 */
+            double lx = src.x - B.org[k].x, ly = src.y - B.org[k].y, lz = src.z - B.org[k].z;
+            B.direct[k] = std::sqrt(lx * lx + ly * ly + lz * lz) / c;
+        }
+    }
+    for (int a = 0; a < 3; ++a) { B.mn[a] = INFINITY; B.mx[a] = -INFINITY; }
+    for (int k = 0; k < B.M; ++k) {
+        const double o[3] = {B.org[k].x, B.org[k].y, B.org[k].z};
+        for (int a = 0; a < 3; ++a) {
+            if (o[a] + d->increment * .5 > B.mx[a]) B.mx[a] = o[a] + d->increment * .5;
+            if (o[a] - d->increment * .5 < B.mn[a]) B.mn[a] = o[a] - d->increment * .5;
+        }
+    }
+    const double per[3] = {d->increment * 4, d->increment * 4, d->increment * 2.5};
+    double inv_vd[3];
+    for (int a = 0; a < 3; ++a) {
+        B.n[a] = (int)std::ceil((B.mx[a] - B.mn[a]) / per[a]);
+        B.vd[a] = (B.mx[a] - B.mn[a]) / B.n[a];
+        inv_vd[a] = 1 / B.vd[a];
+    }
+    B.inv.assign((size_t)B.n[0] * B.n[1] * B.n[2], {});
+    for (int k = 0; k < B.M; ++k) {
+        const double o[3] = {B.org[k].x, B.org[k].y, B.org[k].z};
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::max(0, (int)std::floor((o[a] - B.r - B.mn[a]) * inv_vd[a]));
+            hi[a] = std::min(B.n[a] - 1, (int)std::floor((o[a] + B.r - B.mn[a]) * inv_vd[a]));
+        }
+        for (int x = lo[0]; x <= hi[0]; ++x)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int z = lo[2]; z <= hi[2]; ++z) {
+                    const int ix[3] = {x, y, z};
+                    double q[3];
+                    for (int a = 0; a < 3; ++a) q[a] = std::max(B.cmin(a, ix[a]) - o[a], std::max(0.0, o[a] - B.cmax(a, ix[a])));
+                    if (q[0] * q[0] + q[1] * q[1] + q[2] * q[2] < B.r2) B.inv[((size_t)x * B.n[1] + y) * B.n[2] + z].push_back(k);
+                }
+    }
+    return true;
+}
+
+/* OBox.IsPointInBox and OBox.Intersect of Hare's AABB (not in the reference tree), restated as
+ * inclusive bounds and the slab test of the half-line; the entry point is o + t_near d. */
+inline bool map_inside(const MapBank &B, V3 p) {
+    return p.x >= B.mn[0] && p.x <= B.mx[0] && p.y >= B.mn[1] && p.y <= B.mx[1] && p.z >= B.mn[2] && p.z <= B.mx[2];
+}
+inline bool map_entry(const MapBank &B, V3 o, V3 d, V3 &pt) {
+    const double oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    double tn = 0, tf = INFINITY;
+    for (int a = 0; a < 3; ++a) {
+        if (dd[a] == 0) {
+            if (oo[a] < B.mn[a] || oo[a] > B.mx[a]) return false;
+            continue;
+        }
+        double t1 = (B.mn[a] - oo[a]) / dd[a], t2 = (B.mx[a] - oo[a]) / dd[a];
+        if (t1 > t2) std::swap(t1, t2);
+        tn = std::max(tn, t1);
+        tf = std::min(tf, t2);
+    }
+    if (tn > tf) return false;
+    pt = o + d * tn;
+    return true;
+}
+/* (int)Math.Floor(x) for the cell indices, kept inside int range */
+inline int floor_int(double x) {
+    double f = std::floor(x);
+    if (!(f > -2147483648.0)) return INT32_MIN;
+    if (f > 2147483647.0) return INT32_MAX;
+    return (int)f;
+}
+
 struct Ctx {
     const Scene &S;
+    MapBank map;
     const orc_params &p;
     std::vector<Rec> recs;
     std::vector<V3> src_org;
@@ -455,7 +562,114 @@ struct Worker {
     Hist H;
     orc_stats st{};
     std::vector<ORay> queue;
-    Worker(Ctx &c) : C(c), tr(c.S) { H.init((int)c.recs.size(), c.T); }
+    std::vector<double> mE, mP;       /* map histograms [M][8][T] */
+    std::vector<uint32_t> stamp;      /* Map_Receiver.Ray_ID: the walk that last tested the receiver */
+    uint32_t walk_id = 0;
+    Worker(Ctx &c) : C(c), tr(c.S) {
+        H.init((int)c.recs.size(), c.T);
+        if (c.map.M) {
+            mE.assign((size_t)c.map.M * 8 * c.map.T, 0);
+            mP.assign((size_t)c.map.M * 8 * c.map.T, 0);
+            stamp.assign(c.map.M, 0);
+        }
+    }
+
+    /* CheckBroadbandRay (broadband) / CheckRay (Pach_Map_Receiver.cs:1359-1631) with the
+     * Ray_ID mailbox of CheckReceivers_* (349-408): test(k) once for every receiver listed in a
+     * visited cell.  walk 0 is the reference's code: the broadband walk indexes from the ray's
+     * origin (unclipped), steers by the sign of the POSITION (R.x where R.dx is meant) and stops
+     * when any index reaches the end cell's; the octave walk starts at the entry point and stops on
+     * reaching the end cell, unvisited.  walk 1 visits every crossed cell, the end cell included. */
+    template <class F> void map_walk(V3 o, V3 d, V3 end, bool broadband, F test) {
+        const MapBank &B = C.map;
+        const bool quirk = broadband && B.walk == 0;
+        V3 s = o;
+        if (!map_inside(B, o)) {
+            V3 pt = o;
+            if (!map_entry(B, o, d, pt)) return;
+            if (!quirk) s = pt;
+        }
+        const double sp[3] = {s.x, s.y, s.z}, ep[3] = {end.x, end.y, end.z};
+        const double g[3] = {quirk ? o.x : d.x, quirk ? o.y : d.y, quirk ? o.z : d.z};
+        int c[3], ce[3], step[3];
+        double tmax[3], tdel[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = floor_int((sp[a] - B.mn[a]) / B.vd[a]);
+            ce[a] = floor_int((ep[a] - B.mn[a]) / B.vd[a]);
+        }
+        for (int a = 0; a < 3; ++a) c[a] = c[a] < 0 ? 0 : (c[a] >= B.n[a] ? B.n[a] - 1 : c[a]);
+        for (int a = 0; a < 3; ++a)
+            if ((g[a] < 0 && c[a] < ce[a]) || (g[a] >= 0 && c[a] > ce[a])) return;
+        for (int a = 0; a < 3; ++a) {
+            step[a] = g[a] < 0 ? -1 : 1;
+            tmax[a] = ((g[a] < 0 ? B.cmin(a, c[a]) : B.cmax(a, c[a])) - sp[a]) / g[a];
+            tdel[a] = B.vd[a] / g[a] * step[a];
+        }
+        if (++walk_id == 0) { std::fill(stamp.begin(), stamp.end(), 0u); walk_id = 1; }
+        for (;;) {
+            for (int k : B.cell(c[0], c[1], c[2])) {
+                if (stamp[k] == walk_id) continue;
+                stamp[k] = walk_id;
+                test(k);
+            }
+            if (B.walk && c[0] == ce[0] && c[1] == ce[1] && c[2] == ce[2]) return;
+            int a;
+            if (tmax[0] < tmax[1]) a = tmax[0] < tmax[2] ? 0 : 2;
+            else a = tmax[1] < tmax[2] ? 1 : 2;
+            c[a] += step[a];
+            if (c[a] < 0 || c[a] >= B.n[a]) return;  /* outside grid */
+            tmax[a] = tmax[a] + tdel[a];
+            if (quirk) { if (!(c[0] != ce[0] && c[1] != ce[1] && c[2] != ce[2])) return; }
+            else if (B.walk == 0) { if (!(c[0] != ce[0] || c[1] != ce[1] || c[2] != ce[2])) return; }
+        }
+    }
+
+    /* Histogram.Add / Histogram_1Pt.Add (Classes_Receivers.cs:1159-1166, 1393-1396), 1000 Hz */
+    void map_add(int k, int oct, double time, double e) {
+        const MapBank &B = C.map;
+        size_t i = ((size_t)k * 8 + oct) * B.T;
+        if (B.one_pt) { mE[i] += e; return; }
+        const double x = time * 1000;
+        if (!(x > -1) || x >= B.T) return;   /* (int) truncates: (-1, 0) is sample 0 */
+        const int sample = (int)x;
+        mE[i + sample] += e;
+        mP[i + sample] += std::sqrt(e);
+    }
+
+    /* Map_Receiver.CheckRay / CheckBroadbandRay geometry (Pach_Map_Receiver.cs:1780-1826) */
+    bool map_hit(int k, V3 o, V3 d, V3 end, double &t) const {
+        const MapBank &B = C.map;
+        double mx = o.x - B.org[k].x, my = o.y - B.org[k].y, mz = o.z - B.org[k].z;
+        double b = mx * d.x + my * d.y + mz * d.z;
+        double c = mx * mx + my * my + mz * mz - B.r2;
+        if (c > 0 && b > 0) return false;
+        double discr = b * b - c;
+        if (discr < 0) return false;
+        double t1 = -b - std::sqrt(discr), t2 = -b + std::sqrt(discr);
+        t = (t1 + t2) / 2;
+        double ex = end.x - o.x, ey = end.y - o.y, ez = end.z - o.z;
+        return t > 0 && t * t < ex * ex + ey * ey + ez * ez;
+    }
+    void map_octave(const ORay &R, V3 end, double scale) {
+        const MapBank &B = C.map;
+        map_walk(R.p, R.d, end, false, [&](int k) {
+            double t;
+            if (!map_hit(k, R.p, R.d, end, t)) return;
+            st.detections++;
+            double raydist = t / B.c + R.t_sum - B.direct[k];
+            map_add(k, R.oct, raydist, R.I * scale * std::pow(10, -.1 * B.atten[R.oct] * raydist) * B.sizemod);
+        });
+    }
+    void map_broad(V3 o, V3 d, double t_sum, const double E[8], V3 end) {
+        const MapBank &B = C.map;
+        map_walk(o, d, end, true, [&](int k) {
+            double t;
+            if (!map_hit(k, o, d, end, t)) return;
+            st.detections++;
+            double raydist = t / B.c + t_sum - B.direct[k];
+            for (int oct = 0; oct < 8; ++oct) map_add(k, oct, raydist, E[oct] * std::pow(10, -.1 * B.atten[oct] * raydist) * B.sizemod);
+        });
+    }
 
     /* Receiver_Bank.CheckRay -> Spherical_Receiver.CheckRay (Classes_Receivers.cs:197-200, 837-877). */
     void check_ray(const ORay &R, V3 end, double scale) {
@@ -516,12 +730,18 @@ struct Worker {
             Hit h;
             st.segments++; st.segments_broadband++;
             if (!tr.shoot(pos, d, h)) {
-                if (order > C.p.is_order) check_broad(pos, d, t_sum, E, pos + d * 1000000);
+                if (order > C.p.is_order) {
+                    check_broad(pos, d, t_sum, E, pos + d * 1000000);
+                    if (C.map.M) map_broad(pos, d, t_sum, E, pos + d * 1000000);
+                }
                 for (int j = 0; j < 8; ++j) st.lost_energy += E[j];
                 lost = true;
                 break;
             }
-            if (order > C.p.is_order) check_broad(pos, d, t_sum, E, h.x);
+            if (order > C.p.is_order) {
+                check_broad(pos, d, t_sum, E, h.x);
+                if (C.map.M) map_broad(pos, d, t_sum, E, h.x);
+            }
             t_sum += h.t / S.c;
             pos = h.x;
             int k = order;  /* index of this broadband bounce */
@@ -578,11 +798,13 @@ struct Worker {
                 st.segments++; st.segments_phase_b++; nseg++;
                 if (!tr.shoot(R.p, R.d, h)) {
                     check_ray(R, R.p + R.d * 1000000, scale);
+                    if (C.map.M) map_octave(R, R.p + R.d * 1000000, scale);
                     st.lost_energy += R.I;
                     dead = true;
                     break;
                 }
                 check_ray(R, h.x, scale);
+                if (C.map.M) map_octave(R, h.x, scale);
                 R.t_sum += h.t / S.c;
                 R.p = h.x;
                 V3 n = S.normal[h.poly];
@@ -627,10 +849,12 @@ struct Worker {
                 st.segments++; st.segments_phase_c++; nseg++;
                 if (!tr.shoot(R.p, R.d, h)) {
                     check_ray(R, R.p + R.d * 1000000, scale);
+                    if (C.map.M) map_octave(R, R.p + R.d * 1000000, scale);
                     st.lost_energy += R.I;
                     break;
                 }
                 check_ray(R, h.x, scale);
+                if (C.map.M) map_octave(R, h.x, scale);
                 R.t_sum += h.t / S.c;
                 R.p = h.x;
                 V3 n = S.normal[h.poly];
@@ -810,6 +1034,16 @@ int orc_trace_ex(const orc_scene_desc *scene, int32_t n_src, const orc_source *s
                  const double *prim_dirs, const double *prim_weights,
                  double *energy, double *pressure, double *dir_pos, double *dir_neg, double *analysis,
                  orc_stats *stats) {
+    return orc_trace_map(scene, n_src, src, n_rec, rec, nullptr, pp, ray_begin, ray_end, n_threads, prim_dirs,
+                         prim_weights, energy, pressure, dir_pos, dir_neg, analysis, nullptr, nullptr, nullptr, stats);
+}
+
+int orc_trace_map(const orc_scene_desc *scene, int32_t n_src, const orc_source *src,
+                  int32_t n_rec, const orc_receiver *rec, const orc_map_desc *map, const orc_params *pp,
+                  int64_t ray_begin, int64_t ray_end, int32_t n_threads,
+                  const double *prim_dirs, const double *prim_weights,
+                  double *energy, double *pressure, double *dir_pos, double *dir_neg, double *analysis,
+                  double *map_energy, double *map_pressure, double *map_direct, orc_stats *stats) {
     if (!scene || !src || n_src < 1 || !pp || ray_end < ray_begin) return -1;
     if (pp->oct_lo < 0 || pp->oct_hi > 7 || pp->oct_lo > pp->oct_hi) return -1;
     Scene S;
@@ -841,6 +1075,7 @@ int orc_trace_ex(const orc_scene_desc *scene, int32_t n_src, const orc_source *s
     C.rate = p.sample_rate;
     C.T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
     if (C.T < 1) return -1;
+    if (map && !build_map(map, C.src_org[0], n_src, S.c, S.atten, C.map)) return -1;
     /* Derived phase-A bound: E[h] shrinks at least by fmax per bounce. */
     if (p.max_broadband_bounces <= 0) {
         double fmax = 0;
@@ -882,8 +1117,14 @@ int orc_trace_ex(const orc_scene_desc *scene, int32_t n_src, const orc_source *s
         out.end_traces += w.st.end_traces; out.detections += w.st.detections; out.capped += w.st.capped;
         out.cells_visited += w.tr.cells_visited; out.tri_tests += w.tr.tri_tests;
         out.lost_energy += w.st.lost_energy; out.initial_energy += w.st.initial_energy;
+        const size_t nm = w.mE.size();
+        for (size_t i = 0; i < nm; ++i) {
+            if (map_energy) map_energy[i] = (t ? map_energy[i] : 0) + w.mE[i];
+            if (map_pressure) map_pressure[i] = (t ? map_pressure[i] : 0) + w.mP[i];
+        }
         delete W[t];
     }
+    if (map_direct) for (int k = 0; k < C.map.M; ++k) map_direct[k] = C.map.direct[k];
     out.h_oct = C.h_oct; out.bins = C.T; out.cotime_s = C.COTime; out.sound_speed = S.c; out.rho_c = S.rho_c;
     for (int o = 0; o < 8; ++o) out.air_atten_db_per_m[o] = S.atten[o];
     if (stats) *stats = out;

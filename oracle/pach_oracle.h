@@ -113,6 +113,30 @@ int orc_trace_ex(const orc_scene_desc *scene, int32_t n_src, const orc_source *s
                  double *energy, double *pressure, double *dir_pos, double *dir_neg, double *analysis,
                  orc_stats *stats);
 
+/* Mapping receivers (PachMapReceiver, Pach_Map_Receiver.cs): spheres of diameter `increment` at
+ * the given centres, the reference's receiver grid and walks (walk 0) or every crossed cell
+ * (walk 1), Map_Receiver detection, 1000 Hz histograms counted from each receiver's direct
+ * arrival; time_1pt = Histogram_1Pt. */
+typedef struct {
+    int32_t n_receivers;
+    int32_t time_1pt;
+    const double *origins;         /* [3*n_receivers] */
+    double increment;
+    double cutoff_ms;
+    int32_t walk;
+    int32_t pad;
+} orc_map_desc;
+
+/* As orc_trace_ex with mapping receivers as well (map may be NULL): map_energy / map_pressure
+ * [M][8][Tm] RAW sums, Tm = (int)(cutoff_ms / 1000 * 1000) or 1; map_direct [M] seconds.  Any
+ * output pointer may be NULL. */
+int orc_trace_map(const orc_scene_desc *scene, int32_t n_src, const orc_source *src,
+                  int32_t n_rec, const orc_receiver *rec, const orc_map_desc *map, const orc_params *p,
+                  int64_t ray_begin, int64_t ray_end, int32_t n_threads,
+                  const double *prim_dirs, const double *prim_weights,
+                  double *energy, double *pressure, double *dir_pos, double *dir_neg, double *analysis,
+                  double *map_energy, double *map_pressure, double *map_direct, orc_stats *stats);
+
 /* Pure specular path of each ray: per bounce the hit polygon (-1 = miss, then stop), the leg
  * length and the hit point.  Used for the image-lattice known answers. */
 int orc_specular_paths(const orc_scene_desc *scene, int32_t grid_domain, int32_t brute_force,

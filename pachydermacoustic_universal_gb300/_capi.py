@@ -44,6 +44,11 @@ class ReceiverDesc(C.Structure):
     _fields_ = [("origin", C.c_double * 3), ("radius", C.c_double)]
 
 
+class MapDesc(C.Structure):
+    _fields_ = [("n_receivers", C.c_int32), ("time_1pt", C.c_int32), ("origins", _dp), ("increment", C.c_double),
+                ("cutoff_ms", C.c_double), ("walk", C.c_int32), ("reserved", C.c_int32)]
+
+
 class TraceParams(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("ray_count", C.c_int64), ("ray_begin", C.c_int64), ("cutoff_length_m", C.c_double),
                 ("oct_lo", C.c_int32), ("oct_hi", C.c_int32), ("is_order", C.c_int32), ("sample_rate", C.c_int32),
@@ -55,7 +60,7 @@ class TraceParams(C.Structure):
                 ("traversal", C.c_int32), ("capture", C.c_int32),
                 ("prim_dirs", _dp), ("prim_weights", _dp),
                 ("proposal", C.POINTER(C.c_float)), ("n_proposal", C.c_int32), ("bvh_format", C.c_int32),
-                ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3)]
+                ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3), ("map", C.POINTER(MapDesc))]
 
 
 class RoomDesc(C.Structure):
@@ -100,7 +105,8 @@ class Stats(C.Structure):
 # Every symbol include/pach_gpu.h declares (checked by the CPU test suite).
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
            "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_direct_sound", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
-           "pach_trace_get_histograms", "pach_trace_get_stats", "pach_run_destroy", "pach_trace_run",
+           "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_map_parameters",
+           "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
            "pach_math_strength", "pach_math_sound_speed",
@@ -137,6 +143,8 @@ def _declare(L):
         "pach_trace_wait": (C.c_int, [vp, C.c_int64]),
         "pach_trace_get_histograms": (C.c_int, [vp, C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_size_t]),
         "pach_trace_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
+        "pach_trace_get_map": (C.c_int, [vp, C.c_int32, _dp, _dp, _dp, _ip, C.c_size_t]),
+        "pach_map_parameters": (C.c_int, [vp, C.c_int32, C.c_int32, _dp, _dp, _dp, _dp, _dp]),
         "pach_run_destroy": (None, [vp]),
         "pach_trace_run": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
                                      C.POINTER(TraceParams), C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_size_t,

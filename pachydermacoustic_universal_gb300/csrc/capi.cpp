@@ -85,6 +85,11 @@ struct pach_run {
     // device buffers
     DevMem hE, hP, hDp, hDn, hAn, cnt, qa, qs0, qs1, qctl, drec, dsrc, de0, dgeo, ddirs, dw, sortbins, dprop, dcap;
     DevMem droom, droomprim, btri, btri64, bnorm, bmat, btrans, bbvh, bbvhq;
+    // mapping receivers (has_map): the host grid and its device copy, histograms [M][8][Tm]
+    bool has_map = false;
+    MapGrid mg;
+    std::vector<double> map_org;
+    DevMem mrec, mdir, mcell, mentry, mE, mP;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -103,7 +108,8 @@ struct pach_run {
         }
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
-                          &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh, &bbvhq})
+                          &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh, &bbvhq,
+                          &mrec, &mdir, &mcell, &mentry, &mE, &mP})
             m->release();
     }
 };
@@ -393,6 +399,24 @@ void run_worker(pach_run *run) {
             TRY(cudaMemset(run->dcap.p, 0, run->dcap.bytes));
         }
 
+        const bool map = run->has_map;
+        if (map) {
+            const MapGrid &g = run->mg;
+            std::vector<float4> mr((size_t)g.M);
+            for (int k = 0; k < g.M; ++k)
+                mr[(size_t)k] = make_float4((float)run->map_org[3 * (size_t)k], (float)run->map_org[3 * (size_t)k + 1],
+                                            (float)run->map_org[3 * (size_t)k + 2], (float)g.r2);
+            TRY(upload(run->mrec, mr.data(), mr.size() * sizeof(float4)));
+            TRY(upload(run->mdir, g.direct.data(), g.direct.size() * sizeof(double)));
+            TRY(upload(run->mcell, g.cell_off.data(), g.cell_off.size() * sizeof(int)));
+            TRY(upload(run->mentry, g.entry.data(), std::max<size_t>(g.entry.size(), 1) * sizeof(uint2)));
+            const size_t nm = (size_t)g.M * kBands * g.T;
+            TRY(run->mE.alloc(nm * sizeof(double)));
+            TRY(run->mP.alloc(nm * sizeof(double)));
+            TRY(cudaMemsetAsync(run->mE.p, 0, run->mE.bytes, stream));
+            TRY(cudaMemsetAsync(run->mP.p, 0, run->mP.bytes, stream));
+        }
+
         // launch shapes: one resident wave of blocks for the trace and shade kernels
         int dev_sms = 0;
         TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, sc->device));
@@ -460,6 +484,29 @@ void run_worker(pach_run *run) {
             const double def[3] = {80.0, 400.0, 1200.0};
             for (int i = 0; i < 3; ++i) r.cap_edge[i] = (float)(given ? run->p.capture_edges_ms[i] : def[i]);
         }
+        if (map) {
+            const MapGrid &g = run->mg;
+            MapDev &m = r.map;
+            m.rec = run->mrec.as<float4>();
+            m.direct = run->mdir.as<double>();
+            m.cell = run->mcell.as<int>();
+            m.entry = run->mentry.as<uint2>();
+            m.E = run->mE.as<double>();
+            m.P = run->mP.as<double>();
+            for (int a = 0; a < 3; ++a) {
+                m.lo[a] = (float)g.mn[a];
+                m.hi[a] = (float)g.mx[a];
+                m.vd[a] = (float)g.vd[a];
+                m.n[a] = g.n[a];
+            }
+            m.M = g.M;
+            m.T = g.T;
+            m.one_pt = g.one_pt ? 1 : 0;
+            m.walk = g.walk;
+            m.size_mod = (float)(1.0 / (M_PI * g.r2));
+            const HostScene &hs0 = run->rooms[0].scene->hs;
+            for (int o = 0; o < kBands; ++o) m.atten_k[o] = (float)(-0.1 * std::log2(10.0) * hs0.atten[o]);
+        }
         r.seed = run->p.seed;
         r.max_seg = run->p.max_segments_per_ray > 0 ? run->p.max_segments_per_ray : (1ll << 22);
         if (!timing) {
@@ -506,7 +553,7 @@ void run_worker(pach_run *run) {
             cudaError_t x;
             if ((x = launch_feed(r, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k], stream))) return x;
-            if ((x = launch_broadband(r, bb_blocks, bb_threads, stream))) return x;
+            if ((x = launch_broadband(r, bb_blocks, bb_threads, stream, map))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 1], stream))) return x;
             if ((x = launch_wave(r, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 2], stream))) return x;
@@ -514,7 +561,7 @@ void run_worker(pach_run *run) {
             if (timing && (x = cudaEventRecord(kev[6 * k + 3], stream))) return x;
             if (!fused && (x = launch_trace(r, tr_variant, tr_blocks, threads, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 4], stream))) return x;
-            if ((x = launch_shade(r, sh_blocks, threads, stream, fused))) return x;
+            if ((x = launch_shade(r, sh_blocks, threads, stream, fused, map))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 5], stream))) return x;
             return cudaSuccess;
         };
@@ -839,6 +886,16 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
     std::unique_ptr<pach_run> run(new pach_run());
     run->scene = scene;
     run->p = p;
+    if (p.map) {
+        std::string err;
+        if (!build_map_grid(*p.map, sources[0].origin, n_sources, scene->hs.c, run->mg, err))
+            return fail(PACH_ERR_INVALID_ARGUMENT, err);
+        if ((double)run->mg.M * kBands * run->mg.T * 16 > 200e9)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "map histograms larger than 200 GB");
+        run->map_org.assign(p.map->origins, p.map->origins + 3 * (size_t)p.map->n_receivers);
+        run->has_map = true;
+    }
+    run->p.map = nullptr;
     if (p.proposal) proposal_lobes(p.proposal, p.n_proposal, run->prop);
     if (p.prim_dirs) run->prim_dirs.assign(p.prim_dirs, p.prim_dirs + 3 * p.ray_count);
     if (p.prim_weights) run->prim_weights.assign(p.prim_weights, p.prim_weights + p.ray_count);
@@ -873,9 +930,11 @@ pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const
     if (pach_status st = check_common(p)) return st;
     if (p.proposal || p.prim_dirs || p.prim_weights)
         return fail(PACH_ERR_INVALID_ARGUMENT, "a batch emits from its sources: no proposal or emission overrides");
+    if (p.map) return fail(PACH_ERR_INVALID_ARGUMENT, "mapping receivers need a single-room run (pach_trace_begin)");
     if (p.ray_begin < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin must be >= 0");
     std::unique_ptr<pach_run> run(new pach_run());
     run->p = p;
+    run->p.map = nullptr;
     long long prim = p.ray_begin;
     int R = 0, nsrc = 0;
     for (int i = 0; i < n_rooms; ++i) {
@@ -1001,6 +1060,69 @@ pach_status pach_trace_get_capture(pach_run *run, float *out, size_t cap) {
     cudaSetDevice(run->scene->device);
     cudaError_t e = cudaMemcpy(out, run->dcap.p, n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "capture copy"));
+    return PACH_OK;
+}
+
+pach_status pach_trace_get_map(pach_run *run, int32_t scaled, double *energy, double *pressure, double *direct_time,
+                               int32_t *sizes, size_t cap_bins) {
+    if (pach_status s = check_run(run)) return s;
+    if (!run->has_map) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no mapping receivers");
+    const MapGrid &g = run->mg;
+    if (sizes) { sizes[0] = g.M; sizes[1] = g.T; }
+    if (direct_time) std::memcpy(direct_time, g.direct.data(), g.direct.size() * sizeof(double));
+    if (!energy && !pressure) return PACH_OK;
+    {
+        std::lock_guard<std::mutex> lk(run->mu);
+        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+    }
+    const size_t n = (size_t)g.M * kBands * g.T;
+    if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 8 * bins");
+    cudaSetDevice(run->scene->device);
+    // Histogram.Scale(N) divides energy and pressure by N; a cluster's Scale(1 / n_sources) multiplies back
+    const double N = (double)std::max(1ll, run->rays_done.load());
+    const double f = (double)run->nsrc / N;
+    for (auto [dst, src] : {std::pair<double *, DevMem *>{energy, &run->mE}, {pressure, &run->mP}}) {
+        if (!dst) continue;
+        cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map copy"));
+        if (scaled)
+            for (size_t i = 0; i < n; ++i) dst[i] *= f;
+    }
+    return PACH_OK;
+}
+
+pach_status pach_map_parameters(pach_run *run, int32_t decay_depth, int32_t clarity_ms, double *t_x, double *edt,
+                                double *clarity, double *definition, double *energy_sum) {
+    if (pach_status s = check_run(run)) return s;
+    if (!run->has_map) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no mapping receivers");
+    {
+        std::lock_guard<std::mutex> lk(run->mu);
+        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+    }
+    const MapGrid &g = run->mg;
+    const int n = g.M * kBands;
+    cudaSetDevice(run->scene->device);
+    DevMem out;
+    struct Release {
+        DevMem &m;
+        ~Release() { m.release(); }
+    } release_out{out};
+    cudaError_t e = out.alloc((size_t)5 * n * sizeof(double));
+    if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "parameter map buffers"));
+    double *d = out.as<double>();
+    const double scale = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
+    e = launch_map_params(run->mE.as<double>(), n, g.T, scale, decay_depth, clarity_ms / 1000.0, d, d + n, d + 2 * (size_t)n,
+                          d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map kernel"));
+    double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
+    for (int i = 0; i < 5; ++i) {
+        if (!dst[i]) continue;
+        e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map copy"));
+    }
     return PACH_OK;
 }
 

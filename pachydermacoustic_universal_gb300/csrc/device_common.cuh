@@ -360,6 +360,165 @@ __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomPara
 }
 
 // ------------------------------------------------------------------------------------------
+// mapping receivers (PachMapReceiver, Pach_Map_Receiver.cs)
+// ------------------------------------------------------------------------------------------
+// Histogram.Add / Histogram_1Pt.Add (Classes_Receivers.cs:1159-1166, 1393-1396) at 1000 Hz: the
+// sample is (int)(time * 1000), a truncation, so arrivals up to 1 ms before the direct arrival
+// land in bin 0; samples outside [0, T) are dropped.  Histogram_1Pt keeps every arrival in bin 0
+// and no pressure.
+__device__ __forceinline__ void map_add(const MapDev &M, int k, int oct, double time, float e) {
+    long long s = 0;
+    if (!M.one_pt) {
+        const double x = time * 1000.0;
+        if (!(x > -1.0) || x >= (double)M.T) return;
+        s = (long long)x;
+    }
+    const size_t i = ((size_t)k * kBands + oct) * M.T + s;
+    atomicAdd(M.E + i, (double)e);
+    if (!M.one_pt) atomicAdd(M.P + i, (double)sqrtf(e));
+}
+
+// OBox.IsPointInBox and OBox.Intersect (Hare AABB, not in the reference tree), restated as
+// inclusive bounds and the slab test of the half-line o + t d, t >= 0.
+__device__ __forceinline__ bool map_box_entry(const MapDev &M, float3 o, float3 d, float &t0) {
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    float tn = 0.f, tf = 3.0e38f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (dd[a] == 0.f) {
+            if (oo[a] < M.lo[a] || oo[a] > M.hi[a]) return false;
+            continue;
+        }
+        const float inv = 1.f / dd[a];
+        float ta = (M.lo[a] - oo[a]) * inv, tb = (M.hi[a] - oo[a]) * inv;
+        if (ta > tb) { const float x = ta; ta = tb; tb = x; }
+        tn = fmaxf(tn, ta);
+        tf = fminf(tf, tb);
+    }
+    t0 = tn;
+    return tn <= tf;
+}
+
+__device__ __forceinline__ int map_cell_index(float p, float lo, float vd) {
+    return (int)floorf(fminf(fmaxf((p - lo) / vd, -1.0e9f), 1.0e9f));
+}
+
+// The receiver-grid walk of one segment [o, end] (CheckBroadbandRay / CheckRay,
+// Pach_Map_Receiver.cs:1359-1631), calling visit(k) once for every receiver listed in a visited
+// cell.  walk 0 keeps the reference's two walks as written: the broadband walk starts from the
+// ray's origin even when it lies outside the grid, takes its step signs, first crossings and
+// increments from the ray's POSITION (R.x where R.dx is meant) and stops as soon as ANY cell index
+// equals the end cell's; the octave walk starts at the grid entry point and stops on reaching the
+// end cell without visiting it (after a segment that starts and ends in one cell it runs on to the
+// grid's edge).  walk 1 visits every cell the segment crosses, the end cell included.
+template <typename Visit>
+__device__ __forceinline__ void map_walk(const MapDev &M, float3 o, float3 d, float3 end, bool broadband, Visit visit) {
+    const bool quirk = broadband && M.walk == 0;
+    float3 s = o;
+    const bool inside = o.x >= M.lo[0] && o.x <= M.hi[0] && o.y >= M.lo[1] && o.y <= M.hi[1] && o.z >= M.lo[2] &&
+                        o.z <= M.hi[2];
+    if (!inside) {
+        float t0;
+        if (!map_box_entry(M, o, d, t0)) return;
+        if (!quirk) s = o + d * t0;
+    }
+    const float sp[3] = {s.x, s.y, s.z}, ep[3] = {end.x, end.y, end.z};
+    // the quantity whose sign and size steer the walk: the direction, or the reference broadband walk's position
+    const float g[3] = {quirk ? o.x : d.x, quirk ? o.y : d.y, quirk ? o.z : d.z};
+    int c[3], ce[3], step[3];
+    float tmax[3], tdel[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c[a] = map_cell_index(sp[a], M.lo[a], M.vd[a]);
+        ce[a] = map_cell_index(ep[a], M.lo[a], M.vd[a]);
+        c[a] = c[a] < 0 ? 0 : (c[a] >= M.n[a] ? M.n[a] - 1 : c[a]);
+        if ((g[a] < 0.f && c[a] < ce[a]) || (g[a] >= 0.f && c[a] > ce[a])) return;
+        step[a] = g[a] < 0.f ? -1 : 1;
+        const float bound = (float)(g[a] < 0.f ? c[a] : c[a] + 1) * M.vd[a] + M.lo[a];
+        tmax[a] = (bound - sp[a]) / g[a];
+        tdel[a] = M.vd[a] / g[a] * (float)step[a];
+    }
+    // the last three cells visited: a receiver listed in an earlier cell of this walk is listed in one
+    // of them (a sphere spans at most two cells per axis and every step moves one axis by one cell)
+    int3 p0 = make_int3(-4, -4, -4), p1 = p0, p2 = p0;  // far from every cell until visited
+    auto near_bit = [&](int3 p) -> uint32_t {
+        const int dx = p.x - c[0], dy = p.y - c[1], dz = p.z - c[2];
+        return (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1)
+                   ? 1u << ((dx + 1) * 9 + (dy + 1) * 3 + (dz + 1))
+                   : 0u;
+    };
+    const int max_steps = M.n[0] + M.n[1] + M.n[2] + 1;
+    for (int it = 0; it <= max_steps; ++it) {
+        const uint32_t seen = near_bit(p0) | near_bit(p1) | near_bit(p2);
+        const int ci = (c[0] * M.n[1] + c[1]) * M.n[2] + c[2];
+        const int e1 = __ldg(M.cell + ci + 1);
+        for (int e = __ldg(M.cell + ci); e < e1; ++e) {
+            const uint2 en = __ldg(M.entry + e);
+            if (en.y & seen) continue;
+            visit((int)en.x);
+        }
+        p2 = p1;
+        p1 = p0;
+        p0 = make_int3(c[0], c[1], c[2]);
+        if (M.walk && c[0] == ce[0] && c[1] == ce[1] && c[2] == ce[2]) return;
+        // the reference's comparison order (ties go to z, then y)
+        const bool sx = tmax[0] < tmax[1] && tmax[0] < tmax[2];
+        const bool sy = !(tmax[0] < tmax[1]) && tmax[1] < tmax[2];
+        if (sx) {
+            c[0] += step[0];
+            if (c[0] < 0 || c[0] >= M.n[0]) return;  // outside the grid
+            tmax[0] += tdel[0];
+        } else if (sy) {
+            c[1] += step[1];
+            if (c[1] < 0 || c[1] >= M.n[1]) return;
+            tmax[1] += tdel[1];
+        } else {
+            c[2] += step[2];
+            if (c[2] < 0 || c[2] >= M.n[2]) return;
+            tmax[2] += tdel[2];
+        }
+        if (quirk) {
+            if (!(c[0] != ce[0] && c[1] != ce[1] && c[2] != ce[2])) return;
+        } else if (M.walk == 0) {
+            if (c[0] == ce[0] && c[1] == ce[1] && c[2] == ce[2]) return;
+        }
+    }
+}
+
+// Map_Receiver.CheckRay (Pach_Map_Receiver.cs:1810-1826) over the grid: energy
+// I 10^(-0.1 m t) / (pi r^2), t = arrival time after the receiver's direct arrival (s).
+__device__ __forceinline__ uint32_t map_detect_octave(const MapDev &M, const RoomParams &P, float3 o, float3 d,
+                                                      float tseg, double t_sum, float Iabs, int oct) {
+    uint32_t n = 0;
+    map_walk(M, o, d, o + d * tseg, false, [&](int k) {
+        float t, half;
+        if (!sphere_hit(__ldg(M.rec + k), o, d, tseg, t, half)) return;
+        ++n;
+        const double time = t_sum + (double)(t * P.inv_c) - __ldg(M.direct + k);
+        map_add(M, k, oct, time, Iabs * exp2f(M.atten_k[oct] * (float)time) * M.size_mod);
+    });
+    return n;
+}
+
+// Map_Receiver.CheckBroadbandRay (Pach_Map_Receiver.cs:1780-1808): all eight bands, whatever the
+// octave range.
+__device__ __forceinline__ uint32_t map_detect_broad(const MapDev &M, const RoomParams &P, float3 o, float3 d,
+                                                     float tseg, double t_sum, const float (&E)[kBands],
+                                                     const float (&sc)[kBands]) {
+    uint32_t n = 0;
+    map_walk(M, o, d, o + d * tseg, true, [&](int k) {
+        float t, half;
+        if (!sphere_hit(__ldg(M.rec + k), o, d, tseg, t, half)) return;
+        ++n;
+        const double time = t_sum + (double)(t * P.inv_c) - __ldg(M.direct + k);
+#pragma unroll
+        for (int oct = 0; oct < kBands; ++oct)
+            map_add(M, k, oct, time, E[oct] * sc[oct] * exp2f(M.atten_k[oct] * (float)time) * M.size_mod);
+    });
+    return n;
+}
+
+// ------------------------------------------------------------------------------------------
 // emission
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ float3 emit_dir(const DevRun &r, int nsrc, long long prim, int kind) {

@@ -120,6 +120,40 @@ inline int receiver_smem_bytes(int R) { return 16 * (R > 0 && R <= kSmemReceiver
 
 constexpr long long kPilotPrimaries = 256;
 
+// Mapping receivers on the device (PachMapReceiver).  The grid is the reference's: cells of
+// BoxDims / ceil(BoxDims / (4, 4, 2.5 increments)) over the spheres' bounding box; cell c lists
+// the receivers whose sphere overlaps it (FP64 sphere-box test on the host), each entry with a
+// 27-bit mask of the neighbouring cells (bit (dx+1)*9 + (dy+1)*3 + (dz+1)) that list it too, so a
+// walk tests a receiver once (the reference's Ray_ID mailbox).
+struct MapDev {
+    const float4 *rec;        // [M] (x, y, z, r^2)
+    const double *direct;     // [M] direct arrival time (s)
+    const int *cell;          // [cells + 1] entry offsets, cell = (x * ny + y) * nz + z
+    const uint2 *entry;       // (receiver, neighbour mask)
+    double *E, *P;            // [M][8][T]
+    float lo[3], hi[3];       // grid box (OBox)
+    float vd[3];              // cell size
+    int n[3];                 // cells per axis
+    int M, T;
+    int one_pt;               // Histogram_1Pt: every arrival in bin 0, no pressure
+    int walk;                 // 0 the reference's walks, 1 every crossed cell
+    float size_mod;           // 1 / (pi r^2)
+    float atten_k[kBands];    // exp2 factor per second after the direct arrival: -0.1 log2(10) m
+};
+
+// Host side of the mapping receivers (map_grid.cpp): the grid in FP64 and its cell lists.
+struct MapGrid {
+    int M = 0, T = 1, walk = 0;
+    bool one_pt = false;
+    double r = 0, r2 = 0;
+    double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0}, vd[3] = {1, 1, 1};
+    int n[3] = {1, 1, 1};
+    std::vector<int> cell_off;      // [cells + 1]
+    std::vector<uint2> entry;       // (receiver, neighbour mask)
+    std::vector<double> direct;     // [M] s
+};
+bool build_map_grid(const pach_map_desc &d, const double src[3], int nsrc, double c, MapGrid &g, std::string &err);
+
 // Launch-wide parameters (kernel argument).
 struct DevRun {
     DevScene S;
@@ -170,6 +204,8 @@ struct DevRun {
     float *capture;
     int capture_mode;
     float cap_edge[3];             // window edges, ms after the direct arrival
+    // mapping receivers (used by the map variants of the broadband and shading kernels)
+    MapDev map;
 };
 
 constexpr int kLobes = PACH_MLP_LOBES;
@@ -213,7 +249,7 @@ constexpr int kSortBins = 8 * kSortGrid * kSortGrid * kSortGrid;  // x 8 directi
 //   -> trace (BVH walk of every ray of the wave) -> shade (detect, absorb, scatter, append).
 cudaError_t launch_feed(const DevRun &r, cudaStream_t s);
 cudaError_t launch_cond(const DevRun &r, cudaGraphConditionalHandle h, cudaStream_t s);
-cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s);
+cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s, bool map = false);
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s);
 cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count -> scan -> scatter
 // variant: 256-thread blocks per SM the trace kernel is compiled for (3..6; others -> 4), plus 16 for the
@@ -242,7 +278,12 @@ inline bool use_quantised_nodes(int bvh_format, int ntri) {
 cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, cudaStream_t s);
 // fused: k_shade walks the rays itself (no k_trace launch) -- the default for scenes of at most
 // kFuseMaxTris triangles, or traversal = 3
-cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused = false);
+// map: also detect the run's mapping receivers (kernel variants compiled with the grid walk)
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused = false, bool map = false);
+// Room-acoustic parameters of n energy-time curves etc [n][T] x scale on the device (map_params.cu).
+cudaError_t launch_map_params(const double *etc, int n, int T, double scale, int decay_depth, double clarity_s,
+                              double *t_x, double *edt, double *clarity, double *definition, double *sum,
+                              cudaStream_t s);
 constexpr int kFuseMaxTris = 64;
 inline bool fused_walk(int traversal, int ntri) { return traversal == 3 || (traversal == 0 && ntri <= kFuseMaxTris); }
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);

@@ -66,9 +66,9 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
     if (n_receivers < 0 || n_receivers > kNaMaxReceivers || (n_receivers > 0 && !receivers))
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "pach_trace_run_noalloc takes 0..256 receivers");
     const pach_trace_params &p = *params;
-    if (p.prim_dirs || p.prim_weights || p.proposal || p.capture)
+    if (p.prim_dirs || p.prim_weights || p.proposal || p.capture || p.map)
         return na_fail(PACH_ERR_INVALID_ARGUMENT,
-                       "pach_trace_run_noalloc does not take emission overrides, a proposal or capture");
+                       "pach_trace_run_noalloc does not take emission overrides, a proposal, capture or a map");
     if (p.ray_count < 1 || p.ray_begin < 0 || p.ray_begin + p.ray_count > (1ll << 32))
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "ray_count must be >= 1 and ray_begin + ray_count <= 2^32");
     if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi || p.sample_rate < 1 || !(p.cutoff_length_m > 0))

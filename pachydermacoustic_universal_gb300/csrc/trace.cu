@@ -150,6 +150,7 @@ __global__ void k_cond(DevRun r, cudaGraphConditionalHandle h) {
 // ------------------------------------------------------------------------------------------
 // phase A: broadband rays (cast_ray_distributed, TaskAll:347-424)
 // ------------------------------------------------------------------------------------------
+template <bool MAP>
 __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
     const float4 *s_rec = stage_receivers(r, s_rec_buf);
@@ -187,13 +188,19 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             L.v[C_RET] += tw.retests;
             ++L.v[C_SEGA];
             if (!hit) {
-                if (order > P.is_order) L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
+                if (order > P.is_order) {
+                    L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
+                    if constexpr (MAP) L.v[C_DET] += map_detect_broad(r.map, P, pos, d, 1e6f, t_sum, E, sc);
+                }
 #pragma unroll
                 for (int o = 0; o < kBands; ++o) L.lost += (double)(E[o] * sc[o]);
                 lost = true;
                 break;
             }
-            if (order > P.is_order) L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, t, t_sum, E, sc, (uint32_t)prim);
+            if (order > P.is_order) {
+                L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, t, t_sum, E, sc, (uint32_t)prim);
+                if constexpr (MAP) L.v[C_DET] += map_detect_broad(r.map, P, pos, d, t, t_sum, E, sc);
+            }
             t_sum += (double)t * P.inv_c_d;
             pos = pos + d * t;
             const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
@@ -484,7 +491,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
 
 // FUSED: walk the ray here instead of reading k_trace's hit (small scenes, whose walk is a few
 // cached nodes: the separate trace pass would only re-read the ray and round-trip its hit via HBM).
-template <bool FUSED>
+template <bool FUSED, bool MAP>
 __global__ void __launch_bounds__(256) k_shade(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
     const float4 *s_rec = stage_receivers(r, s_rec_buf);
@@ -521,6 +528,8 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
             const RoomParams &P = r.rooms[R.room];
             L.v[C_DET] += detect_octave(r, P, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask,
                                         R.prim);
+            if constexpr (MAP)
+                L.v[C_DET] += map_detect_octave(r.map, P, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct);
             if (!hit) {
                 // lost: no End_Trace after a miss in phase B (TaskAll:437-443), loop exit in phase C (500-505)
                 L.lost += (double)(R.I * R.scale);
@@ -691,8 +700,9 @@ cudaError_t launch_feed(const DevRun &r, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s) {
-    k_broadband<<<blocks, threads, rec_smem(r), s>>>(r);
+cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s, bool map) {
+    if (map) k_broadband<true><<<blocks, threads, rec_smem(r), s>>>(r);
+    else k_broadband<false><<<blocks, threads, rec_smem(r), s>>>(r);
     return cudaGetLastError();
 }
 
@@ -729,9 +739,14 @@ cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused) {
-    if (fused) k_shade<true><<<blocks, threads, rec_smem(r), s>>>(r);
-    else k_shade<false><<<blocks, threads, rec_smem(r), s>>>(r);
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused, bool map) {
+    if (map) {
+        if (fused) k_shade<true, true><<<blocks, threads, rec_smem(r), s>>>(r);
+        else k_shade<false, true><<<blocks, threads, rec_smem(r), s>>>(r);
+    } else {
+        if (fused) k_shade<true, false><<<blocks, threads, rec_smem(r), s>>>(r);
+        else k_shade<false, false><<<blocks, threads, rec_smem(r), s>>>(r);
+    }
     return cudaGetLastError();
 }
 
@@ -747,7 +762,7 @@ cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int 
         default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false, false>, threads, 0); break;
     }
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false>, threads, smem_shade);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false, false>, threads, smem_shade);
 }
 
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,

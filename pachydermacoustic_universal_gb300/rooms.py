@@ -341,3 +341,16 @@ def arena_c5(seed: int = 5, rays: int = 10_000_000, target_tris: int = 500_000) 
     recs = _interior_points(rng, (0, 0, 0), size, 64, margin=3.0, avoid=srcs, min_sep=1.0)
     return Workload("arena_120x90x35_500ktri", scene, [SourceSpec(s) for s in srcs],
                     [ReceiverSpec(r) for r in recs], rays, 3.5)
+
+
+def audience_plane(lo, hi, height: float, increment: float) -> np.ndarray:
+    """Receiver centres [M][3] of a flat audience mesh of increment-sized squares covering [lo, hi] in
+    (x, y) at `height`, placed as PachMapReceiver places face receivers with Z displacement
+    (Pach_Map_Receiver.cs:107-139): each square's centroid raised by increment / 2."""
+    nx = int(round((hi[0] - lo[0]) / increment))
+    ny = int(round((hi[1] - lo[1]) / increment))
+    xs = lo[0] + (np.arange(nx) + 0.5) * increment
+    ys = lo[1] + (np.arange(ny) + 0.5) * increment
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    Z = np.full_like(X, height + increment * 0.5)
+    return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 
 import numpy as np
 
@@ -68,11 +69,39 @@ def receiver_array(receivers):
     return arr
 
 
+@dataclasses.dataclass
+class MapReceivers:
+    """Mapping receivers (PachMapReceiver): spheres of diameter `increment` centred at `origins`
+    [M][3], histograms of `cutoff_ms` ms at 1000 Hz counted from each receiver's direct arrival (one
+    bin with time_1pt).  walk 0 reproduces the reference's grid walks, 1 visits every crossed cell."""
+    origins: np.ndarray
+    increment: float
+    cutoff_ms: float
+    time_1pt: bool = False
+    walk: int = 0
+
+    def desc(self):
+        org = np.ascontiguousarray(self.origins, dtype=np.float64).reshape(-1, 3)
+        d = _capi.MapDesc()
+        d.n_receivers = org.shape[0]
+        d.time_1pt = int(bool(self.time_1pt))
+        d.origins = dptr(org)
+        d.increment = float(self.increment)
+        d.cutoff_ms = float(self.cutoff_ms)
+        d.walk = int(self.walk)
+        d._keep = org
+        return d
+
+    @property
+    def bins(self):
+        return 1 if self.time_1pt else int(float(self.cutoff_ms) / 1000.0 * 1000.0)
+
+
 def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 7), is_order=-1, sample_rate=1000,
                 pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
                 block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
                 ring_log2=0, kernel_timing=False, ray_sort=0, traversal=0, capture=False, capture_edges_ms=None,
-                proposal=None, proposal_mix=0.0, bvh_format=0):
+                proposal=None, proposal_mix=0.0, bvh_format=0, map_receivers=None):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -103,6 +132,10 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
         p.proposal = _capi.fptr(proposal)
         p.n_proposal = int(proposal.shape[0])
         p.proposal_mix = float(proposal_mix)
+    if map_receivers is not None:
+        md = map_receivers.desc()
+        p.map = C.pointer(md)
+        p._map_keep = md
     return p
 
 
@@ -152,6 +185,30 @@ class Run:
         else:
             out = np.zeros((self.R, _capi.CAPTURE_WINDOWS, _capi.DIR_BINS), dtype=np.float32)
         check(_capi.lib().pach_trace_get_capture(self.handle, _capi.fptr(out), out.size))
+        return out
+
+    def map_histograms(self, scaled=False):
+        """Map histograms energy / pressure [M][8][T] (time 0 = each receiver's direct arrival) and
+        the direct arrival times [M] (s)."""
+        L = _capi.lib()
+        sizes = np.zeros(2, dtype=np.int32)
+        check(L.pach_trace_get_map(self.handle, 0, None, None, None, iptr(sizes), 0))
+        M, T = int(sizes[0]), int(sizes[1])
+        E, P, D = np.zeros((M, 8, T)), np.zeros((M, 8, T)), np.zeros(M)
+        check(L.pach_trace_get_map(self.handle, int(bool(scaled)), dptr(E), dptr(P), dptr(D), None, E.size))
+        return {"energy": E, "pressure": P, "direct_time": D}
+
+    def map_parameters(self, decay_depth=30, clarity_ms=80):
+        """T_X, EDT, clarity (dB), definition (%) and total energy of every map receiver and band [M][8],
+        computed on the device."""
+        L = _capi.lib()
+        sizes = np.zeros(2, dtype=np.int32)
+        check(L.pach_trace_get_map(self.handle, 0, None, None, None, iptr(sizes), 0))
+        M = int(sizes[0])
+        out = {k: np.zeros((M, 8)) for k in ("t_x", "edt", "clarity", "definition", "energy")}
+        check(L.pach_map_parameters(self.handle, int(decay_depth), int(clarity_ms), dptr(out["t_x"]),
+                                    dptr(out["edt"]), dptr(out["clarity"]), dptr(out["definition"]),
+                                    dptr(out["energy"])))
         return out
 
     def stats(self):
@@ -275,6 +332,8 @@ def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, **kw):
         h = run.histograms(scaled=scaled)
         if params.capture:
             h["capture"] = run.capture()
+        if kw.get("map_receivers") is not None:
+            h["map"] = run.map_histograms(scaled=scaled)
         return h, run.stats()
     finally:
         run.close()
