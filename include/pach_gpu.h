@@ -289,6 +289,11 @@ pach_status pach_trace_get_map(pach_run *run, int32_t scaled, double *energy, do
  * reaches the fit limits, as T_X); any may be NULL.  energy_sum = the band's total scaled energy. */
 pach_status pach_map_parameters(pach_run *run, int32_t decay_depth, int32_t clarity_ms, double *t_x, double *edt,
                                 double *clarity, double *definition, double *energy_sum);
+/* The same parameters for n caller curves etc [n][T] at sample_rate Hz (host arrays; the work runs on
+ * the current device): T_X / EDT / Clarity (clarity_s seconds) / Definition (50 ms), start time 0. */
+pach_status pach_etc_parameters(const double *etc, int32_t n, int32_t T, int32_t sample_rate, int32_t decay_depth,
+                                double clarity_s, double *t_x, double *edt, double *clarity, double *definition,
+                                double *energy_sum);
 void pach_run_destroy(pach_run *run);
 
 /* Synchronous convenience: begin + wait + histograms + stats. */

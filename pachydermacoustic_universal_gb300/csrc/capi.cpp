@@ -1113,8 +1113,8 @@ pach_status pach_map_parameters(pach_run *run, int32_t decay_depth, int32_t clar
     if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "parameter map buffers"));
     double *d = out.as<double>();
     const double scale = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
-    e = launch_map_params(run->mE.as<double>(), n, g.T, scale, decay_depth, clarity_ms / 1000.0, d, d + n, d + 2 * (size_t)n,
-                          d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
+    e = launch_map_params(run->mE.as<double>(), n, g.T, 1000.0, scale, decay_depth, clarity_ms / 1000.0, d, d + n,
+                          d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map kernel"));
     double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
@@ -1122,6 +1122,36 @@ pach_status pach_map_parameters(pach_run *run, int32_t decay_depth, int32_t clar
         if (!dst[i]) continue;
         e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map copy"));
+    }
+    return PACH_OK;
+}
+
+pach_status pach_etc_parameters(const double *etc, int32_t n, int32_t T, int32_t sample_rate, int32_t decay_depth,
+                                double clarity_s, double *t_x, double *edt, double *clarity, double *definition,
+                                double *energy_sum) {
+    if (n < 0 || T < 1 || sample_rate < 1 || (n > 0 && !etc))
+        return fail(PACH_ERR_INVALID_ARGUMENT, "etc_parameters: need n >= 0 curves of T >= 1 bins at a positive rate");
+    if (n == 0) return PACH_OK;
+    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
+    DevMem in, out;
+    struct Release {
+        DevMem &a, &b;
+        ~Release() { a.release(); b.release(); }
+    } release_bufs{in, out};
+    const size_t bytes = (size_t)n * T * sizeof(double);
+    cudaError_t e = upload(in, etc, bytes);
+    if (e == cudaSuccess) e = out.alloc((size_t)5 * n * sizeof(double));
+    if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "etc_parameters buffers"));
+    double *d = out.as<double>();
+    e = launch_map_params(in.as<double>(), n, T, (double)sample_rate, 1.0, decay_depth, clarity_s, d, d + n,
+                          d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "etc_parameters kernel"));
+    double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
+    for (int i = 0; i < 5; ++i) {
+        if (!dst[i]) continue;
+        e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "etc_parameters copy"));
     }
     return PACH_OK;
 }

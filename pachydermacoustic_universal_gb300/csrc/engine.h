@@ -280,10 +280,10 @@ cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, 
 // kFuseMaxTris triangles, or traversal = 3
 // map: also detect the run's mapping receivers (kernel variants compiled with the grid walk)
 cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused = false, bool map = false);
-// Room-acoustic parameters of n energy-time curves etc [n][T] x scale on the device (map_params.cu).
-cudaError_t launch_map_params(const double *etc, int n, int T, double scale, int decay_depth, double clarity_s,
-                              double *t_x, double *edt, double *clarity, double *definition, double *sum,
-                              cudaStream_t s);
+// Room-acoustic parameters of n energy-time curves etc [n][T] x scale at fs Hz on the device (map_params.cu).
+cudaError_t launch_map_params(const double *etc, int n, int T, double fs, double scale, int decay_depth,
+                              double clarity_s, double *t_x, double *edt, double *clarity, double *definition,
+                              double *sum, cudaStream_t s);
 constexpr int kFuseMaxTris = 64;
 inline bool fused_walk(int traversal, int ntri) { return traversal == 3 || (traversal == 0 && ntri <= kFuseMaxTris); }
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);

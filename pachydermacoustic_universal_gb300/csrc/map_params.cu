@@ -44,13 +44,12 @@ __device__ __forceinline__ int first_set(unsigned ballot, int base, int from) {
     return ballot ? base + __ffs(ballot) - 1 : -1;
 }
 
-__global__ void __launch_bounds__(256) k_map_params(const double *etc, int n, int T, double scale, int depth,
-                                                    double clar_s, double *t_x, double *edt, double *clar,
+__global__ void __launch_bounds__(256) k_map_params(const double *etc, int n, int T, double fs, double scale,
+                                                    int depth, double clar_s, double *t_x, double *edt, double *clar,
                                                     double *defi, double *sum) {
     const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (w >= n) return;
     const double *x = etc + (size_t)w * T;
-    const double fs = 1000.0;
     // pass 1: total, and the early sums of Clarity (start 0: bins [0, ei)) and Definition
     const int ei_c = (int)floor((clar_s + 0.0) * fs), ei_d = (int)floor(0.05 * fs);
     double tot = 0, ec = 0, lc = 0, ed = 0;
@@ -139,12 +138,13 @@ __global__ void __launch_bounds__(256) k_map_params(const double *etc, int n, in
 
 }  // namespace
 
-cudaError_t launch_map_params(const double *etc, int n, int T, double scale, int decay_depth, double clarity_s,
-                              double *t_x, double *edt, double *clarity, double *definition, double *sum,
-                              cudaStream_t s) {
+cudaError_t launch_map_params(const double *etc, int n, int T, double fs, double scale, int decay_depth,
+                              double clarity_s, double *t_x, double *edt, double *clarity, double *definition,
+                              double *sum, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int blocks = (int)(((long long)n * 32 + 255) / 256);
-    k_map_params<<<blocks, 256, 0, s>>>(etc, n, T, scale, decay_depth, clarity_s, t_x, edt, clarity, definition, sum);
+    k_map_params<<<blocks, 256, 0, s>>>(etc, n, T, fs, scale, decay_depth, clarity_s, t_x, edt, clarity, definition,
+                                        sum);
     return cudaGetLastError();
 }
 

@@ -129,6 +129,7 @@ class Polygon_Scene:
 
 class Source:
     kind = 0
+    type = ""
 
     def __init__(self, power_In_db, Source_, ID=0, Third_Octave=False):
         if Third_Octave:
@@ -155,19 +156,27 @@ class Source:
     def Revolution_Period(self):
         return 80
 
+    def Type(self):
+        """Source.Type() (Classes_Sources.cs:220-223)."""
+        return self.type
+
     def specs(self):
         return [SourceSpec(self.Center, tuple(self.SPL), self.kind)]
 
 
 class GeodesicSource(Source):
     kind = 0
+    type = "Geodesic"
 
 
 class RandomSource(Source):
     kind = 1
+    type = "PseudoRandom"
 
 
 class SourceCluster(Source):
+    type = "Cluster"
+
     def __init__(self, sources, id=0, third_octave=False):
         self.Sources = list(sources)
         self.S_ID = id
@@ -260,10 +269,15 @@ class SplitRayTracer:
         self._st = time.time()
         self.Room._need()
         specs = self.Source.specs()
-        recs = [ReceiverSpec(r.Origin, r.Radius) for r in self.RecMain.Rec_List]
+        # a PachMapReceiver bank is traced as the run's mapping receivers (pach_map_desc)
+        self._is_map = hasattr(self.RecMain, "map_receivers")
+        recs = [] if self._is_map else [ReceiverSpec(r.Origin, r.Radius) for r in self.RecMain.Rec_List]
+        kw = dict(self._kw)
+        if self._is_map:
+            kw["map_receivers"] = self.RecMain.map_receivers()
         params = make_params(rays=self.Raycount, cutoff_length_m=self._cutoff_len,
                              hist_cotime_ms=self.RecMain.CutOffTime, seed=self._seed, oct_range=self._oct,
-                             is_order=self.IS_Order, sample_rate=self.RecMain.SampleRate, **self._kw)
+                             is_order=self.IS_Order, sample_rate=self.RecMain.SampleRate, **kw)
         self._run = Run(self.Room._dev, specs, recs, params)
 
     def ThreadState(self):
@@ -295,6 +309,12 @@ class SplitRayTracer:
 
     def Combine_ThreadLocal_Results(self):
         self._run.wait()
+        if self._is_map:
+            self.RecMain._set(self._run.map_histograms(scaled=True))
+            self._stats = self._run.stats()
+            self._lost_percent = self._stats["percent_lost"]
+            self._ts = time.time() - self._st
+            return
         h = self._run.histograms(scaled=True)
         for i, rec in enumerate(self.RecMain.Rec_List):
             rec._E[:] = h["energy"][i]

@@ -165,3 +165,33 @@ def test_hall_map_matches_oracle_within_jnd():
     hg, sg, ho, so = _both(w, m, n, 11, oracle_kw={"grid_domain": 31})
     assert sg["queue_overflows"] == 0
     np.testing.assert_allclose(hg["map"]["energy"].sum(), ho["map_energy"].sum(), rtol=0.03)
+
+
+def test_split_ray_tracer_fills_a_pach_map_receiver_and_parameter_maps():
+    from pachydermacoustic_universal_gb300.mapping import (Get_Clarity_Map, Get_Definition_Map, Get_EDT_Map,
+                                                           Get_RT_Map, MapMesh, PachMapReceiver)
+    from pachydermacoustic_universal_gb300.simulation import GeodesicSource, Polygon_Scene, SplitRayTracer
+    w, _ = _shifted(rooms.shoebox_c1(), np.zeros((1, 3)))
+    room = Polygon_Scene.from_arrays(w.scene)
+    src = GeodesicSource([120.0] * 8, w.sources[0].origin)
+    mesh = MapMesh.grid((4.0, 3.0), (12.0, 9.0), 2.0, 1.0)
+    pm = PachMapReceiver(mesh, src, 1000, 1.0, room, 2000.0, False, True, False, False, False)
+    rt = SplitRayTracer(src, pm, room, w.cutoff_length_m, (0, 7), -1, 2000, seed=3)
+    rt.Begin()
+    rt.Combine_ThreadLocal_Results()
+    rt.close()
+    h, _ = tracer.trace(w, rays=2000, seed=3, scaled=True, map_receivers=pm.map_receivers())
+    np.testing.assert_allclose(pm._E, h["map"]["energy"], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose([r.Direct_Time for r in pm.Rec_List], h["map"]["direct_time"], rtol=1e-15)
+    for oct in (1, 5):
+        maps = {"t_x": Get_RT_Map([pm], 30, oct, [0]), "edt": Get_EDT_Map([pm], oct, [0]),
+                "clarity": Get_Clarity_Map([pm], 80, oct, [0]), "definition": Get_Definition_Map([pm], oct, [0])}
+        for i in range(pm.Count):
+            etc = np.zeros(2000 + 16384)
+            etc[:2000] = pm._E[i, oct]
+            sch = AcousticalMath.Schroeder_Integral(etc)
+            ref = {"t_x": AcousticalMath.T_X(sch, 30, 1000), "edt": AcousticalMath.EarlyDecayTime(sch, 1000),
+                   "clarity": AcousticalMath.Clarity(etc, 1000, 0.08, 0.0, False),
+                   "definition": AcousticalMath.Definition(etc, 1000, 0.05, 0.0, False)}
+            for k in maps:
+                np.testing.assert_allclose(maps[k][i], ref[k], rtol=1e-9, equal_nan=True, err_msg=k)
