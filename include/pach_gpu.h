@@ -339,6 +339,13 @@ pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, in
 pach_status pach_medium_properties(double temp_c, double rel_humidity, double pressure_hpa, int32_t air_choice,
                                    int32_t edge_correction, double atten_db_per_m[PACH_BANDS],
                                    double *sound_speed, double *rho);
+/* The same air model at the reference's third-octave centres (Calculate_Attenuation with Third_Octave,
+ * Classes_Medium_Props.cs:51-89, 290): 23 values (its table skips 2500 Hz); centres_hz may be NULL.
+ * The reference computes them (Atten_Coef_3rd) but its tracer does not use them: the split ray
+ * tracer works in the 8 octave bands. */
+pach_status pach_medium_attenuation_third_octave(double temp_c, double rel_humidity, double pressure_hpa,
+                                                 int32_t air_choice, int32_t edge_correction, double atten[23],
+                                                 double centres_hz[23]);
 
 /* AcousticalMath (Classes_Math.cs). */
 pach_status pach_math_schroeder(const double *etc, int32_t n, double *out);              /* 282-299 */

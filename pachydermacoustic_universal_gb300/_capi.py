@@ -107,7 +107,7 @@ EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_c
            "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_direct_sound", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_map_parameters", "pach_etc_parameters",
            "pach_run_destroy", "pach_trace_run",
-           "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_math_schroeder",
+           "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_medium_attenuation_third_octave", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
            "pach_math_strength", "pach_math_sound_speed",
            # include/pach_proposal.h
@@ -157,6 +157,8 @@ def _declare(L):
         "pach_scene_shoot_host": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, _dp, _dp, _ip, _dp]),
         "pach_emit_directions": (C.c_int, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _dp]),
         "pach_medium_properties": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _dp, _dp, _dp]),
+        "pach_medium_attenuation_third_octave": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                                           _dp, _dp]),
         "pach_math_schroeder": (C.c_int, [_dp, C.c_int32, _dp]),
         "pach_math_t_x": (C.c_double, [_dp, C.c_int32, C.c_int32, C.c_int32]),
         "pach_math_edt": (C.c_double, [_dp, C.c_int32, C.c_int32]),

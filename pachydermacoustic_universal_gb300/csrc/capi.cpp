@@ -812,6 +812,16 @@ pach_status pach_medium_properties(double temp_c, double hr, double pa_hpa, int3
     return PACH_OK;
 }
 
+pach_status pach_medium_attenuation_third_octave(double temp_c, double hr, double pa_hpa, int32_t air_choice,
+                                                 int32_t edge, double *atten, double *centres_hz) {
+    if (!atten) return fail(PACH_ERR_INVALID_ARGUMENT, "atten is null");
+    if (!(pa_hpa > 0) || !(hr > 0) || air_choice < 0 || air_choice > 2)
+        return fail(PACH_ERR_INVALID_ARGUMENT, "medium: pressure and humidity must be positive, air_choice 0..2");
+    medium_attenuation_third_octave(temp_c, hr, pa_hpa, air_choice, edge, atten);
+    if (centres_hz) for (int i = 0; i < kThirdOctaveBands; ++i) centres_hz[i] = kThirdOctaveCentres[i];
+    return PACH_OK;
+}
+
 pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
     if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
     *out = nullptr;

@@ -304,6 +304,10 @@ void set_last_error(const char *msg);
 bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err);
 void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, int edge, double atten[kBands],
                        double *c, double *rho);
+constexpr int kThirdOctaveBands = 23;  // the reference's third-octave table (50 Hz .. 10 kHz without 2500 Hz)
+extern const double kThirdOctaveCentres[kThirdOctaveBands];
+void medium_attenuation_third_octave(double temp_c, double hr, double pa_hpa, int air_choice, int edge,
+                                     double atten[kThirdOctaveBands]);
 void geodesic_faces(std::vector<double> &faces);  // [80][3][3]
 void geodesic_faces_fixed(double out[kGeoFaces * 9]);
 unsigned long long derived_broadband_bound(const HostScene &hs, int h_oct, bool pure_specular);

@@ -314,18 +314,19 @@ void quantize_bvh(HostScene &hs) {
 
 }  // namespace
 
-// Calculate_Attenuation (Classes_Medium_Props.cs:51-191) as coded, including the C# integer
-// divisions in the exponents (-1/2 -> 0, -1/3 -> 0, -5/2 -> -2, 1/2 -> 0); called by the
-// Uniform_Medium ctor with Pa/10 (hPa -> kPa).  Density: Calculate_Density(Tk, Pa*100, hr).
-void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, int edge, double atten[kBands],
-                       double *c, double *rho) {
-    static const double F[kBands] = {62.5, 125, 250, 500, 1000, 2000, 4000, 8000};
+// Calculate_Attenuation (Classes_Medium_Props.cs:51-191) as coded, over a frequency table: the eight
+// octave centres, or the reference's third-octave table (23 entries: it skips 2500 Hz).  Includes the
+// C# integer divisions in the exponents (-1/2 -> 0, -1/3 -> 0, -5/2 -> -2, 1/2 -> 0); the Evans-Bazley
+// and table branches fill the first eight entries only, whatever the table.  Called by the
+// Uniform_Medium ctor with Pa/10 (hPa -> kPa).
+static void attenuation_table(const double *F, int nf, double temp_c, double hr, double pa_hpa, int air_choice,
+                              int edge, double *atten) {
     const double Tk = temp_c + 273.15, Pa = pa_hpa / 10.0;
-    for (int o = 0; o < kBands; ++o) atten[o] = 0.0;
+    for (int o = 0; o < nf; ++o) atten[o] = 0.0;
     if (air_choice == 0) {
         const double h = hr * std::pow(10.0, -6.8346 * std::pow(273.16 / Tk, 1.261) + 4.6151) / (Pa / 101.325);
         const int e_half = -1 / 2, e_third = -1 / 3, e_fivehalf = -5 / 2, e_pos_half = 1 / 2;
-        for (int o = 0; o < kBands; ++o) {
+        for (int o = 0; o < nf; ++o) {
             double frO = (Pa / 101.325) * (24 + 4.04e4 * h * ((0.02 + h) / (0.391 + h)));
             double frN = (Pa / 101.325) * std::pow(Tk / 293.15, (double)e_half) *
                          (9 + 280 * h * std::exp(-4.170 * (std::pow(Tk / 293.15, (double)e_third) - 1)));
@@ -335,7 +336,7 @@ void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, 
             atten[o] = 8.686 * F[o] * F[o] * ((1.84e-11 / (Pa / 101.325) * std::pow(Tk / 293.15, (double)e_pos_half)) + y);
         }
     } else if (air_choice == 1) {
-        for (int o = 0; o < kBands; ++o) {
+        for (int o = 0; o < kBands && o < nf; ++o) {
             double m = ((85 / hr) * ((F[o] / 1000) * (F[o] / 1000) * 0.0001)) / 8.7;
             m -= 0.04 * (Tk - 273.15 - 20) * m;
             atten[o] = m * 0.50248756218905477;
@@ -350,10 +351,27 @@ void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, 
         const double(*tab)[kBands] = (Tk - 273.15 > 15) ? W : Cd;
         int row = hr < 50 ? 0 : hr < 70 ? 1 : hr > 70 ? 2 : -1;  // hr == 70 falls through every branch
         if (row >= 0)
-            for (int o = 0; o < kBands; ++o) atten[o] = tab[row][o];
+            for (int o = 0; o < kBands && o < nf; ++o) atten[o] = tab[row][o];
         if (edge)
-            for (int o = 0; o < kBands; ++o) atten[o] /= std::sqrt(2.0);
+            for (int o = 0; o < kBands && o < nf; ++o) atten[o] /= std::sqrt(2.0);
     }
+}
+
+const double kThirdOctaveCentres[kThirdOctaveBands] = {50,   62.5, 80,   100,  125,  160,  200,  250,
+                                                      315,  400,  500,  630,  800,  1000, 1250, 1600,
+                                                      2000, 3150, 4000, 5000, 6300, 8000, 10000};
+
+void medium_attenuation_third_octave(double temp_c, double hr, double pa_hpa, int air_choice, int edge,
+                                     double atten[kThirdOctaveBands]) {
+    attenuation_table(kThirdOctaveCentres, kThirdOctaveBands, temp_c, hr, pa_hpa, air_choice, edge, atten);
+}
+
+// The octave bands, with sound speed and density (Calculate_Density(Tk, Pa*100, hr)).
+void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, int edge, double atten[kBands],
+                       double *c, double *rho) {
+    static const double F[kBands] = {62.5, 125, 250, 500, 1000, 2000, 4000, 8000};
+    attenuation_table(F, kBands, temp_c, hr, pa_hpa, air_choice, edge, atten);
+    const double Tk = temp_c + 273.15;
     if (c) *c = 331 + 0.6 * (Tk - 273.15);                      // AcousticalMath.SoundSpeed
     if (rho) {
         const double P = pa_hpa * 100, Rd = 287.05, T = Tk - 273.15;

@@ -244,3 +244,22 @@ def test_workload_generators_have_the_named_shapes():
     assert 19_000 <= c2.scene.n_triangles <= 21_000 and len(c2.sources) == 2 and len(c2.receivers) == 16
     lo, hi = c2.scene.bounds()
     assert np.all(hi - lo > np.array([39, 24, 14]))
+
+
+def test_third_octave_air_table_matches_the_octave_model():
+    """Third-octave attenuation (Calculate_Attenuation with Third_Octave): the reference's 23-entry
+    table (no 2500 Hz); at the shared centres it equals the octave-band values exactly."""
+    import ctypes as C
+    L = _capi.lib()
+    for air in (0, 1, 2):
+        a3, f3 = np.zeros(23), np.zeros(23)
+        assert L.pach_medium_attenuation_third_octave(20.0, 50.0, 1013.25, air, 0, _capi.dptr(a3), _capi.dptr(f3)) == 0
+        a8 = np.zeros(8)
+        c, rho = C.c_double(), C.c_double()
+        assert L.pach_medium_properties(20.0, 50.0, 1013.25, air, 0, _capi.dptr(a8), C.byref(c), C.byref(rho)) == 0
+        assert 2500.0 not in f3 and f3[0] == 50.0 and f3[-1] == 10000.0
+        if air == 0:
+            for o, f in enumerate((62.5, 125, 250, 500, 1000, 2000, 4000, 8000)):
+                assert a3[list(f3).index(f)] == a8[o]
+        else:   # the other two models fill the first eight entries only, as the reference's loops do
+            assert np.all(a3[8:] == 0) and np.all(a3[:8] > 0)
