@@ -553,7 +553,7 @@ void run_worker(pach_run *run) {
             cudaError_t x;
             if ((x = launch_feed(r, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k], stream))) return x;
-            if ((x = launch_broadband(r, bb_blocks, bb_threads, stream, map))) return x;
+            if ((x = launch_broadband(r, bb_blocks, bb_threads, stream, map, ntri_max <= kFuseMaxTris))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 1], stream))) return x;
             if ((x = launch_wave(r, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 2], stream))) return x;

@@ -147,6 +147,24 @@ __device__ __forceinline__ void test_tri(const DevScene &S, float t_eps, int i, 
 // Empty child slot of a 4-wide node (no leaf can have this code below 2^27 triangles).
 constexpr int kEmptyChild = (int)0x80000000;
 
+// Walk stack entries.  int2: (node or leaf code, entry distance of its box when it was pushed); a
+// pop skips the entries whose box starts beyond the best hit found since -- the test a parent
+// applies before pushing, applied again with the smaller best, so the walk's result is unchanged.
+// Measured +1.8 % on a 20k-triangle hall, -4.5 % on a 12-triangle shoebox (a two-level tree culls
+// nothing and pays for the wider entries): int, no distance, for the small-scene walk.
+__device__ __forceinline__ void stack_push(int2 *stack, int &sp, int id, float t) {
+    stack[sp++] = make_int2(id, __float_as_int(t));
+}
+__device__ __forceinline__ void stack_push(int *stack, int &sp, int id, float) { stack[sp++] = id; }
+__device__ __forceinline__ int stack_pop(const int2 *stack, int &sp, float best) {
+    while (sp > 0) {
+        const int2 e = stack[--sp];
+        if (__int_as_float(e.y) <= best) return e.x;
+    }
+    return kEmptyChild;
+}
+__device__ __forceinline__ int stack_pop(const int *stack, int &sp, float) { return sp > 0 ? stack[--sp] : kEmptyChild; }
+
 __device__ __forceinline__ void cswap(float &ka, int &va, float &kb, int &vb) {
     if (kb < ka) {
         const float k = ka; ka = kb; kb = k;
@@ -157,8 +175,9 @@ __device__ __forceinline__ void cswap(float &ka, int &va, float &kb, int &vb) {
 // One 4-wide node: slab-test the children against [0, best], order the hit ones by entry distance
 // (5-exchange sorting network), push all but the nearest (farthest first), return the nearest in
 // `next`.  Returns false when no child is hit.
+template <typename E>
 __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int node, float ix, float iy, float iz,
-                                          float ox, float oy, float oz, float best, int *stack, int &sp, int &next) {
+                                          float ox, float oy, float oz, float best, E *stack, int &sp, int &next) {
     const float4 *N = bvh + (kBvhNodeFloats / 4) * node;
     const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3);
     const float4 lz = __ldg(N + 4), hz = __ldg(N + 5);
@@ -185,7 +204,7 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
     if (tk[0] == FLT_MAX) return false;
 #pragma unroll
     for (int k = 3; k >= 1; --k)
-        if (tk[k] != FLT_MAX && sp < kBvhStack) stack[sp++] = id[k];
+        if (tk[k] != FLT_MAX && sp < kBvhStack) stack_push(stack, sp, id[k], tk[k]);
     next = id[0];
     return true;
 }
@@ -193,9 +212,9 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
 // The same step on a 64-byte quantised node: child bounds are 8-bit steps from the node's origin,
 // a power-of-two step per axis, so the slab distance q (s / d) + (origin - o) / d is one FMA per
 // bound as with float nodes (s / d is exact: s is a power of two).
+template <typename E>
 __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int node, float ix, float iy, float iz,
-                                           float ox, float oy, float oz, float best, int *stack, int &sp,
-                                           int &next) {
+                                           float ox, float oy, float oz, float best, E *stack, int &sp, int &next) {
     const float4 *N = bvhq + (kBvhQNodeFloats / 4) * node;
     const float4 H = __ldg(N);
     const uint4 A = __ldg(reinterpret_cast<const uint4 *>(N + 1));
@@ -228,7 +247,7 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
     if (tk[0] == FLT_MAX) return false;
 #pragma unroll
     for (int k = 3; k >= 1; --k)
-        if (tk[k] != FLT_MAX && sp < kBvhStack) stack[sp++] = id[k];
+        if (tk[k] != FLT_MAX && sp < kBvhStack) stack_push(stack, sp, id[k], tk[k]);
     next = id[0];
     return true;
 }
@@ -236,6 +255,8 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
 // Nearest hit along o + t d with t > t_eps, skipping triangles of plane `skip` (the surface the ray
 // leaves).  4-wide BVH, nearest-child-first walk with a per-thread stack of the other hit
 // children; a child box is entered only if the ray meets it before the best hit so far.
+// E: the stack entry (int2 culls on pop, int does not; see stack_push).
+template <typename E = int2>
 __device__ __forceinline__ bool trace_ray(const DevScene &S, int root, float t_eps, float3 o, float3 d, int skip,
                                           float &t_best, int &tri_best, TraceWork &w) {
     const float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
@@ -243,32 +264,27 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, int root, float t_e
     const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
     const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
     const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
-    int stack[kBvhStack];
+    E stack[kBvhStack];
     int sp = 0;
     int node = root;
     float best = FLT_MAX;
     int bi = -1;
-    for (;;) {
-        bool done = false;
-        while (node >= 0) {
+    while (node != kEmptyChild) {
+        if (node >= 0) {
             ++w.nodes;
             int next;
-            if (!(S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
-                        : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))) {
-                if (sp == 0) { done = true; break; }
-                node = stack[--sp];
-                continue;
-            }
-            node = next;
+            node = (S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                           : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
+                       ? next
+                       : stack_pop(stack, sp, best);
+            continue;
         }
-        if (done) break;
         // leaf ~(first * 16 + count - 1)
         const int code = ~node;
         const int f0 = code >> 4, cnt = (code & 15) + 1;
         w.tris += (unsigned)cnt;
         for (int k = 0; k < cnt; ++k) test_tri(S, t_eps, f0 + k, o, d, skip, best, bi, w);
-        if (sp == 0) break;
-        node = stack[--sp];
+        node = stack_pop(stack, sp, best);
     }
     if (bi < 0) return false;
     t_best = best;

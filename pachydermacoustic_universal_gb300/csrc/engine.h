@@ -249,7 +249,9 @@ constexpr int kSortBins = 8 * kSortGrid * kSortGrid * kSortGrid;  // x 8 directi
 //   -> trace (BVH walk of every ray of the wave) -> shade (detect, absorb, scatter, append).
 cudaError_t launch_feed(const DevRun &r, cudaStream_t s);
 cudaError_t launch_cond(const DevRun &r, cudaGraphConditionalHandle h, cudaStream_t s);
-cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s, bool map = false);
+// small: every room has at most kFuseMaxTris triangles (walk with the plain stack)
+cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s, bool map = false,
+                             bool small = false);
 cudaError_t launch_wave(const DevRun &r, cudaStream_t s);
 cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count -> scan -> scatter
 // variant: 256-thread blocks per SM the trace kernel is compiled for (3..6; others -> 4), plus 16 for the

@@ -233,7 +233,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         for (long long it = 0;;) {
             for (int k = 0; k < 32; ++k, ++it) {
                 NA_TRY(launch_feed(r, stream));
-                NA_TRY(launch_broadband(r, sms * 2, 128, stream));
+                NA_TRY(launch_broadband(r, sms * 2, 128, stream, false, hs.ntri <= kFuseMaxTris));
                 NA_TRY(launch_wave(r, stream));
                 const bool fused = fused_walk(p.traversal, (int)hs.tri_poly.size());
                 if (!fused) NA_TRY(launch_trace(r, variant, tr_blocks, 256, stream));

@@ -150,7 +150,8 @@ __global__ void k_cond(DevRun r, cudaGraphConditionalHandle h) {
 // ------------------------------------------------------------------------------------------
 // phase A: broadband rays (cast_ray_distributed, TaskAll:347-424)
 // ------------------------------------------------------------------------------------------
-template <bool MAP>
+// SMALL: scenes of at most kFuseMaxTris triangles walk with the plain stack (see stack_push).
+template <bool MAP, bool SMALL>
 __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
     const float4 *s_rec = stage_receivers(r, s_rec_buf);
@@ -184,7 +185,8 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             float t;
             int tri;
             TraceWork tw;
-            const bool hit = trace_ray(S, P.bvh_root, P.t_eps, pos, d, plane, t, tri, tw);
+            const bool hit = SMALL ? trace_ray<int>(S, P.bvh_root, P.t_eps, pos, d, plane, t, tri, tw)
+                                   : trace_ray<int2>(S, P.bvh_root, P.t_eps, pos, d, plane, t, tri, tw);
             L.v[C_RET] += tw.retests;
             ++L.v[C_SEGA];
             if (!hit) {
@@ -380,7 +382,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f, best = FLT_MAX;
     int skip = -1, node = 0, sp = 0, bi = -1, leaf = 0;
     float teps = S.t_eps;
-    int stack[kBvhStack];
+    int2 stack[kBvhStack];
     for (;;) {
         const unsigned need = __ballot_sync(FULL, !have && !exhausted);
         if (need) {
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             // together.  node: >= 0 inner node, < 0 leaf, kEmptyChild nothing left; leaf: 0 none.
             if (have && node < 0 && node != kEmptyChild && leaf == 0) {
                 leaf = node;
-                node = sp ? stack[--sp] : kEmptyChild;
+                node = stack_pop(stack, sp, best);
             }
             for (;;) {
                 if (!__any_sync(FULL, have && node >= 0 && leaf == 0)) break;
@@ -428,10 +430,10 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                     if (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
                               : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
                         node = next;
-                    else node = sp ? stack[--sp] : kEmptyChild;
+                    else node = stack_pop(stack, sp, best);
                     if (node < 0 && node != kEmptyChild && leaf == 0) {
                         leaf = node;
-                        node = sp ? stack[--sp] : kEmptyChild;
+                        node = stack_pop(stack, sp, best);
                     }
                 }
             }
@@ -448,27 +450,23 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             }
         } else {
             if (!have) continue;
-            bool fin = false;
             while (node >= 0) {
                 ++w.nodes;
                 int next;
-                if (!(QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
-                            : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))) {
-                    if (sp == 0) { fin = true; break; }
-                    node = stack[--sp];
-                    continue;
-                }
-                node = next;
+                node = (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                              : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
+                           ? next
+                           : stack_pop(stack, sp, best);
             }
+            const bool fin = node == kEmptyChild;
             if (!fin) {
                 const int code = ~node;
                 const int f0 = code >> 4, cnt = (code & 15) + 1;
                 w.tris += (unsigned)cnt;
                 for (int k = 0; k < cnt; ++k) test_tri(S, teps, f0 + k, o, d, skip, best, bi, w);
-                if (sp == 0) fin = true;
-                else node = stack[--sp];
+                node = stack_pop(stack, sp, best);
             }
-            if (fin) {
+            if (node == kEmptyChild) {
                 r.hits[j] = make_int2(bi, __float_as_int(best));
                 have = false;
             }
@@ -516,7 +514,7 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
                 TraceWork tw;
                 const int root = r.n_rooms > 1 ? __ldg(&r.rooms[R.room].bvh_root) : 0;
                 const float teps = r.n_rooms > 1 ? __ldg(&r.rooms[R.room].t_eps) : S.t_eps;
-                h = trace_ray(S, root, teps, R.p, R.d, R.plane, tt, tri, tw) ? make_int2(tri, __float_as_int(tt))
+                h = trace_ray<int>(S, root, teps, R.p, R.d, R.plane, tt, tri, tw) ? make_int2(tri, __float_as_int(tt))
                                                                               : make_int2(-1, 0);
                 L.v[C_RET] += tw.retests;
             } else {
@@ -700,9 +698,14 @@ cudaError_t launch_feed(const DevRun &r, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s, bool map) {
-    if (map) k_broadband<true><<<blocks, threads, rec_smem(r), s>>>(r);
-    else k_broadband<false><<<blocks, threads, rec_smem(r), s>>>(r);
+cudaError_t launch_broadband(const DevRun &r, int blocks, int threads, cudaStream_t s, bool map, bool small) {
+    if (map) {
+        if (small) k_broadband<true, true><<<blocks, threads, rec_smem(r), s>>>(r);
+        else k_broadband<true, false><<<blocks, threads, rec_smem(r), s>>>(r);
+    } else {
+        if (small) k_broadband<false, true><<<blocks, threads, rec_smem(r), s>>>(r);
+        else k_broadband<false, false><<<blocks, threads, rec_smem(r), s>>>(r);
+    }
     return cudaGetLastError();
 }
 
