@@ -228,7 +228,7 @@ def main():
     ap.add_argument("--batch", type=int, default=131072, help="primaries per step (single-room workloads)")
     ap.add_argument("--ray-scale", type=float, default=0.004, help="batched: fraction of each room's rays per step")
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-sample", type=int, default=400, help="primaries of the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=3000, help="primaries of the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=200, help="primaries per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

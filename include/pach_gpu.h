@@ -17,7 +17,12 @@
  *                            (TaskAll:768-774; Classes_Receivers.cs:676-679, 924-927, 1088-1102, 1774-1786)
  *   pach_trace_get_stats     PercentLost, _currentRay, _rayTotal, _ts (TaskAll:40-47, 776-782)
  *   pach_medium_properties   Uniform_Medium ctor (Classes_Medium_Props.cs:286-299)
+ *   pach_medium_attenuation_third_octave  Calculate_Attenuation, third octaves (Classes_Medium_Props.cs:51-89)
  *   pach_math_*              AcousticalMath (Classes_Math.cs:272-586, 934-1005)
+ *   pach_direct_sound        Direct_Sound, point sources (Classes_Direct.cs:654-685, 772-823)
+ *   pach_trace_get_map       PachMapReceiver as the run's Receiver_Bank (Pach_Map_Receiver.cs:34-1834)
+ *   pach_map_parameters, pach_etc_parameters  Get_RT_Map / Get_EDT_Map / Get_Clarity_Map /
+ *                            Get_Definition_Map without coherent superposition (Pach_Map_Receiver.cs:925-1270)
  *
  * Error behaviour: every entry point returns a pach_status; the message of the last failure on
  * the calling thread is available from pach_last_error.  No callbacks cross the ABI.
