@@ -4,8 +4,9 @@ Default workload (one GPU): the 40 x 25 x 15 m jittered hall with 200 diffusers 
 2 sources, 16 receivers of radius 0.5 m, 3 s cutoff, 1 ms bins, 1M primary rays.  A step traces
 one batch of primaries (default 131072); the timed steps together cover the 1M-ray job, each step
 tracing its own primaries (ray_begin = step * batch), the warm-up steps trace primaries after them.
---workload shoebox: the 12-triangle 10 x 8 x 4 m shoebox; --workload batched: the 64-room batch
-(each room's ray count x --ray-scale per step) as one batch run with autotuned knobs.
+--workload shoebox: the 12-triangle 10 x 8 x 4 m shoebox; --workload arena: the 500k-triangle
+120 x 90 x 35 m arena; --workload batched: the 64-room batch (each room's ray count x --ray-scale
+per step) as one batch run with autotuned knobs.
 
 Metric: segment-bounces/s = shoot calls (broadband + octave rays, hit or miss) per second.
   value  -- device time of the engine's kernels (CUDA events on the engine's stream), scene resident.
@@ -162,13 +163,15 @@ def cpu_baseline(ws, sample_rays, seed):
 
 
 def workload(name, ray_scale):
-    """The rooms of a bench workload: the irregular hall (default), the 12-triangle shoebox, or the
-    64-room batch (ray counts scaled by ray_scale)."""
+    """The rooms of a bench workload: the irregular hall (default), the 12-triangle shoebox, the
+    500k-triangle arena, or the 64-room batch (ray counts scaled by ray_scale)."""
     from pachydermacoustic_universal_gb300 import rooms
     if name == "hall":
         return [rooms.irregular_hall_c2()]
     if name == "shoebox":
         return [rooms.shoebox_c1()]
+    if name == "arena":
+        return [rooms.arena_c5()]
     ws = rooms.batched_rooms_c3()
     for w in ws:
         w.rays = max(100, int(round(w.rays * ray_scale)))
@@ -224,15 +227,21 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hall", choices=["hall", "shoebox", "batched"])
+    ap.add_argument("--workload", default="hall", choices=["hall", "shoebox", "batched", "arena"])
     ap.add_argument("--batch", type=int, default=131072, help="primaries per step (single-room workloads)")
     ap.add_argument("--ray-scale", type=float, default=0.004, help="batched: fraction of each room's rays per step")
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-sample", type=int, default=3000, help="primaries of the CPU baseline sample")
-    ap.add_argument("--ref-sample", type=int, default=200, help="primaries per step of the reference arm")
+    ap.add_argument("--cpu-sample", type=int, default=None,
+                    help="primaries of the CPU baseline sample (default: about 10 s of CPU work per workload)")
+    ap.add_argument("--ref-sample", type=int, default=None, help="primaries per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    # bounded CPU samples: the FP64 restatement's grid makes a 500k-triangle arena ~100x slower per segment
+    if args.cpu_sample is None:
+        args.cpu_sample = {"hall": 3000, "shoebox": 3000, "batched": 400, "arena": 40}[args.workload]
+    if args.ref_sample is None:
+        args.ref_sample = {"hall": 200, "shoebox": 200, "batched": 200, "arena": 8}[args.workload]
 
     if args.impl == "reference":
         return run_reference_arm(args)

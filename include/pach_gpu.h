@@ -77,7 +77,7 @@ typedef struct {
     double pressure_hpa;           /* hPa, as the Scene ctor (1013.25 = 101.325 kPa) */
     int32_t air_choice;            /* 0 ISO 9613-1, 1 Evans-Bazley, 2 tables */
     int32_t edge_correction;
-    int32_t bvh_leaf_max;          /* triangles per BVH leaf at most (1..8); 0 = default (4) */
+    int32_t bvh_leaf_max;          /* triangles per BVH leaf at most (1..8); 0 = default (3) */
     int32_t reserved1;
 } pach_scene_desc;
 
