@@ -166,13 +166,19 @@ class Run:
     def wait(self, timeout_ms=-1):
         check(_capi.lib().pach_trace_wait(self.handle, timeout_ms))
 
-    def histograms(self, scaled=False):
+    def histograms(self, scaled=False, out=None):
+        """Histograms; out: optional dict of preallocated float64 arrays of these shapes (for example
+        views of pinned host memory, which the library's device-to-host copies then use directly)."""
         R, T = self.R, self.T
-        E = np.zeros((R, 8, T))
-        P = np.zeros((R, 8, T))
-        Dp = np.zeros((R, 3, 8, T))
-        Dn = np.zeros((R, 3, 8, T))
-        An = np.zeros((R, 3, 8, T))
+        shapes = {"energy": (R, 8, T), "pressure": (R, 8, T), "dir_pos": (R, 3, 8, T), "dir_neg": (R, 3, 8, T),
+                  "analysis": (R, 3, 8, T)}
+        if out is None:
+            out = {k: np.zeros(v) for k, v in shapes.items()}
+        for k, v in shapes.items():
+            a = out[k]
+            if a.shape != v or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of shape {v}")
+        E, P, Dp, Dn, An = (out[k] for k in shapes)
         check(_capi.lib().pach_trace_get_histograms(self.handle, int(bool(scaled)), dptr(E), dptr(P), dptr(Dp),
                                                     dptr(Dn), dptr(An), E.size))
         return {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}
@@ -254,9 +260,9 @@ class BatchRun(Run):
         check(L.pach_batch_begin(descs, len(workloads), C.byref(params), C.byref(h)))
         self.handle = h
 
-    def room_histograms(self, scaled=False):
+    def room_histograms(self, scaled=False, out=None):
         """Histograms split per room (the run's receiver rows in room order)."""
-        h = self.histograms(scaled=scaled)
+        h = self.histograms(scaled=scaled, out=out)
         out, k = [], 0
         for n in self.room_receivers:
             out.append({name: v[k:k + n] for name, v in h.items()})
@@ -297,9 +303,9 @@ def autotune(workloads, *, dscenes=None, rays=None, sample_rays=20_000, cache_pa
     return {k: getattr(res, k) for k, _ in res._fields_}
 
 
-def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, tune=None, **kw):
+def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, tune=None, out=None, **kw):
     """Trace several rooms.Workload as one batch run; returns (per-room histograms, stats).
-    tune: a dict from autotune() whose knobs are applied."""
+    tune: a dict from autotune() whose knobs are applied; out: see Run.histograms."""
     ds = dscenes or [DeviceScene(w.scene) for w in workloads]
     n = [w.rays for w in workloads] if rays is None else list(rays)
     if tune:
@@ -309,13 +315,13 @@ def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, tun
     run = BatchRun(ds, workloads, n, params)
     try:
         run.wait()
-        return run.room_histograms(scaled=scaled), run.stats()
+        return run.room_histograms(scaled=scaled, out=out), run.stats()
     finally:
         run.close()
 
 
-def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, **kw):
-    """Trace a rooms.Workload on the GPU; returns (histograms, stats)."""
+def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, out=None, **kw):
+    """Trace a rooms.Workload on the GPU; returns (histograms, stats).  out: see Run.histograms."""
     ds = dscene or DeviceScene(workload.scene)
     n = workload.rays if rays is None else rays
     pd = kw.pop("prim_dirs", None)
@@ -329,7 +335,7 @@ def trace(workload, *, dscene=None, seed=1, rays=None, scaled=False, **kw):
     run = Run(ds, workload.sources, workload.receivers, params, keep=(pd, pw, pr))
     try:
         run.wait()
-        h = run.histograms(scaled=scaled)
+        h = run.histograms(scaled=scaled, out=out)
         if params.capture:
             h["capture"] = run.capture()
         if kw.get("map_receivers") is not None:
