@@ -151,7 +151,8 @@ typedef struct pach_map_desc {
                                       by the sign of the ray's POSITION and stops when any cell index reaches
                                       the end cell's; the octave walk never visits the end cell);
                                       1: every cell the segment crosses, end cell included */
-    int32_t reserved;
+    int32_t directional;           /* 1: Directional_Histogram per receiver (pressure sqrt(E rho c), +-x/y/z
+                                      arrival components; pach_trace_get_map_directions) */
 } pach_map_desc;
 
 /* One room of a batch run (pach_batch_begin). */
@@ -287,6 +288,12 @@ pach_status pach_trace_get_stats(pach_run *run, pach_stats *stats);
  * energy and pressure in doubles. */
 pach_status pach_trace_get_map(pach_run *run, int32_t scaled, double *energy, double *pressure, double *direct_time,
                                int32_t *sizes, size_t cap_bins);
+/* Arrival-direction histograms of a directional map, dir_pos / dir_neg [M][3][8][T] (+x, +y, +z
+ * components; Directional_Histogram.Add and Scale, Classes_Receivers.cs:1774-1825: the pressure of a
+ * directional map is scaled by 1 / sqrt(N) where a plain map's is scaled by 1 / N).  cap_bins = capacity
+ * of each in doubles. */
+pach_status pach_trace_get_map_directions(pach_run *run, int32_t scaled, double *dir_pos, double *dir_neg,
+                                          size_t cap_bins);
 /* Room-acoustic parameters of every map receiver and band, computed on the device from the map
  * histograms (Get_RT_Map, Get_EDT_Map, Get_Clarity_Map, Get_Definition_Map without coherent
  * superposition, Pach_Map_Receiver.cs:925-1270: AcousticalMath.T_X / EarlyDecayTime of the Schroeder

@@ -53,7 +53,7 @@ class OrcStats(C.Structure):
 
 class OrcMap(C.Structure):
     _fields_ = [("n_receivers", C.c_int32), ("time_1pt", C.c_int32), ("origins", C.POINTER(C.c_double)),
-                ("increment", C.c_double), ("cutoff_ms", C.c_double), ("walk", C.c_int32), ("pad", C.c_int32)]
+                ("increment", C.c_double), ("cutoff_ms", C.c_double), ("walk", C.c_int32), ("directional", C.c_int32)]
 
 
 def build(force: bool = False) -> str:
@@ -79,6 +79,8 @@ def lib():
                                     C.POINTER(OrcReceiver), C.POINTER(OrcMap), C.POINTER(OrcParams), C.c_int64,
                                     C.c_int64, C.c_int32, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp,
                                     C.POINTER(OrcStats)]
+        L.orc_map_directions.restype = C.c_int
+        L.orc_map_directions.argtypes = [dp, dp, C.c_size_t]
         L.orc_specular_paths.restype = C.c_int
         L.orc_specular_paths.argtypes = [C.POINTER(OrcScene), C.c_int32, C.c_int32, C.c_int32, dp, dp, C.c_int32,
                                          C.POINTER(C.c_int32), dp, dp]
@@ -189,7 +191,8 @@ def trace(workload, *, seed=1, rays=None, ray_begin=0, threads=0, pure_specular=
         morg = np.ascontiguousarray(m.origins, dtype=np.float64).reshape(-1)
         M = morg.size // 3
         Tm = 1 if m.time_1pt else int(float(m.cutoff_ms) / 1000.0 * 1000.0)
-        mdesc = OrcMap(M, int(bool(m.time_1pt)), _dp(morg), float(m.increment), float(m.cutoff_ms), int(m.walk), 0)
+        mdesc = OrcMap(M, int(bool(m.time_1pt)), _dp(morg), float(m.increment), float(m.cutoff_ms), int(m.walk),
+                       int(bool(getattr(m, "directional", False))))
         mE, mP, mD = np.zeros((M, 8, Tm)), np.zeros((M, 8, Tm)), np.zeros(M)
         out.update(map_energy=mE, map_pressure=mP, map_direct=mD)
     rc = L.orc_trace_map(C.byref(sh.desc), ns, srcs, nr, recs, C.byref(mdesc) if mdesc is not None else None,
@@ -197,6 +200,11 @@ def trace(workload, *, seed=1, rays=None, ray_begin=0, threads=0, pure_specular=
                          _dp(Dn), _dp(An), _dp(mE), _dp(mP), _dp(mD), C.byref(st))
     if rc != 0:
         raise RuntimeError(f"orc_trace failed ({rc})")
+    if mdesc is not None and mdesc.directional:
+        Dp, Dn = np.zeros((M, 3, 8, Tm)), np.zeros((M, 3, 8, Tm))
+        if not L.orc_map_directions(_dp(Dp), _dp(Dn), Dp.size):
+            raise RuntimeError("orc_map_directions: no direction histograms")
+        out.update(map_dir_pos=Dp, map_dir_neg=Dn)
     stats = {k: getattr(st, k) for k, _ in OrcStats._fields_}
     stats["air_atten_db_per_m"] = list(st.air_atten_db_per_m)
     return out, stats

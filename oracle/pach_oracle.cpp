@@ -419,9 +419,13 @@ struct Rec { V3 o; double r2; };
 /* ----------------------------------------------------------------------------------------
  * Mapping receivers (PachMapReceiver, Pach_Map_Receiver.cs).
  * -------------------------------------------------------------------------------------- */
+/* direction histograms of the last directional map traced on this thread (orc_map_directions) */
+thread_local std::vector<double> g_map_dp, g_map_dn;
+
 struct MapBank {
     int M = 0, T = 1, walk = 0;
-    bool one_pt = false;
+    bool one_pt = false, directional = false;
+    double rho_c = 0;
     double r = 0, r2 = 0, sizemod = 0, c = 343;
     double atten[8] = {0};
     std::vector<V3> org;
@@ -441,6 +445,7 @@ bool build_map(const orc_map_desc *d, V3 src, int nsrc, double c, const double a
     B.M = d->n_receivers;
     B.one_pt = d->time_1pt != 0;
     B.walk = d->walk;
+    B.directional = d->directional != 0;
     B.T = B.one_pt ? 1 : (int)(d->cutoff_ms / 1000.0 * 1000.0);  /* Histogram(1000, COTime_in) */
     if (B.T < 1) return false;
     B.r = d->increment * 0.5;                                       /* Radius = Diameter * 0.5 */
@@ -563,6 +568,7 @@ struct Worker {
     orc_stats st{};
     std::vector<ORay> queue;
     std::vector<double> mE, mP;       /* map histograms [M][8][T] */
+    std::vector<double> mDp, mDn;     /* directional maps: [M][3][8][T] */
     std::vector<uint32_t> stamp;      /* Map_Receiver.Ray_ID: the walk that last tested the receiver */
     uint32_t walk_id = 0;
     Worker(Ctx &c) : C(c), tr(c.S) {
@@ -570,6 +576,10 @@ struct Worker {
         if (c.map.M) {
             mE.assign((size_t)c.map.M * 8 * c.map.T, 0);
             mP.assign((size_t)c.map.M * 8 * c.map.T, 0);
+            if (c.map.directional) {
+                mDp.assign((size_t)c.map.M * 24 * c.map.T, 0);
+                mDn.assign((size_t)c.map.M * 24 * c.map.T, 0);
+            }
             stamp.assign(c.map.M, 0);
         }
     }
@@ -624,8 +634,9 @@ struct Worker {
         }
     }
 
-    /* Histogram.Add / Histogram_1Pt.Add (Classes_Receivers.cs:1159-1166, 1393-1396), 1000 Hz */
-    void map_add(int k, int oct, double time, double e) {
+    /* Histogram.Add / Histogram_1Pt.Add / Directional_Histogram.Add (Classes_Receivers.cs:1159-1166,
+     * 1393-1396, 1813-1825), 1000 Hz; d = the ray direction (the arrival direction is -d) */
+    void map_add(int k, int oct, double time, double e, V3 d) {
         const MapBank &B = C.map;
         size_t i = ((size_t)k * 8 + oct) * B.T;
         if (B.one_pt) { mE[i] += e; return; }
@@ -633,7 +644,14 @@ struct Worker {
         if (!(x > -1) || x >= B.T) return;   /* (int) truncates: (-1, 0) is sample 0 */
         const int sample = (int)x;
         mE[i + sample] += e;
-        mP[i + sample] += std::sqrt(e);
+        if (!B.directional) { mP[i + sample] += std::sqrt(e); return; }
+        mP[i + sample] += std::sqrt(e * B.rho_c);
+        const double c[3] = {-d.x, -d.y, -d.z};
+        for (int a = 0; a < 3; ++a) {
+            const size_t j = (((size_t)k * 3 + a) * 8 + oct) * B.T + sample;
+            const double v = (double)(float)(c[a] * e);
+            if (c[a] > 0) mDp[j] += v; else mDn[j] += v;
+        }
     }
 
     /* Map_Receiver.CheckRay / CheckBroadbandRay geometry (Pach_Map_Receiver.cs:1780-1826) */
@@ -657,7 +675,7 @@ struct Worker {
             if (!map_hit(k, R.p, R.d, end, t)) return;
             st.detections++;
             double raydist = t / B.c + R.t_sum - B.direct[k];
-            map_add(k, R.oct, raydist, R.I * scale * std::pow(10, -.1 * B.atten[R.oct] * raydist) * B.sizemod);
+            map_add(k, R.oct, raydist, R.I * scale * std::pow(10, -.1 * B.atten[R.oct] * raydist) * B.sizemod, R.d);
         });
     }
     void map_broad(V3 o, V3 d, double t_sum, const double E[8], V3 end) {
@@ -667,7 +685,7 @@ struct Worker {
             if (!map_hit(k, o, d, end, t)) return;
             st.detections++;
             double raydist = t / B.c + t_sum - B.direct[k];
-            for (int oct = 0; oct < 8; ++oct) map_add(k, oct, raydist, E[oct] * std::pow(10, -.1 * B.atten[oct] * raydist) * B.sizemod);
+            for (int oct = 0; oct < 8; ++oct) map_add(k, oct, raydist, E[oct] * std::pow(10, -.1 * B.atten[oct] * raydist) * B.sizemod, d);
         });
     }
 
@@ -1076,6 +1094,7 @@ int orc_trace_map(const orc_scene_desc *scene, int32_t n_src, const orc_source *
     C.T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
     if (C.T < 1) return -1;
     if (map && !build_map(map, C.src_org[0], n_src, S.c, S.atten, C.map)) return -1;
+    C.map.rho_c = S.rho_c;
     /* Derived phase-A bound: E[h] shrinks at least by fmax per bounce. */
     if (p.max_broadband_bounces <= 0) {
         double fmax = 0;
@@ -1122,6 +1141,8 @@ int orc_trace_map(const orc_scene_desc *scene, int32_t n_src, const orc_source *
             if (map_energy) map_energy[i] = (t ? map_energy[i] : 0) + w.mE[i];
             if (map_pressure) map_pressure[i] = (t ? map_pressure[i] : 0) + w.mP[i];
         }
+        if (t == 0) { g_map_dp.assign(w.mDp.size(), 0.0); g_map_dn.assign(w.mDn.size(), 0.0); }
+        for (size_t i = 0; i < w.mDp.size(); ++i) { g_map_dp[i] += w.mDp[i]; g_map_dn[i] += w.mDn[i]; }
         delete W[t];
     }
     if (map_direct) for (int k = 0; k < C.map.M; ++k) map_direct[k] = C.map.direct[k];
@@ -1129,6 +1150,13 @@ int orc_trace_map(const orc_scene_desc *scene, int32_t n_src, const orc_source *
     for (int o = 0; o < 8; ++o) out.air_atten_db_per_m[o] = S.atten[o];
     if (stats) *stats = out;
     return 0;
+}
+
+int orc_map_directions(double *dir_pos, double *dir_neg, size_t cap) {
+    if (g_map_dp.empty() || cap < g_map_dp.size()) return 0;
+    if (dir_pos) std::copy(g_map_dp.begin(), g_map_dp.end(), dir_pos);
+    if (dir_neg) std::copy(g_map_dn.begin(), g_map_dn.end(), dir_neg);
+    return 1;
 }
 
 int orc_trace(const orc_scene_desc *scene, int32_t n_src, const orc_source *src,

@@ -124,7 +124,7 @@ typedef struct {
     double increment;
     double cutoff_ms;
     int32_t walk;
-    int32_t pad;
+    int32_t directional;           /* Directional_Histogram: pressure sqrt(E rho c), +-x/y/z arrival sums */
 } orc_map_desc;
 
 /* As orc_trace_ex with mapping receivers as well (map may be NULL): map_energy / map_pressure
@@ -136,6 +136,10 @@ int orc_trace_map(const orc_scene_desc *scene, int32_t n_src, const orc_source *
                   const double *prim_dirs, const double *prim_weights,
                   double *energy, double *pressure, double *dir_pos, double *dir_neg, double *analysis,
                   double *map_energy, double *map_pressure, double *map_direct, orc_stats *stats);
+
+/* The direction histograms [M][3][8][Tm] of the last orc_trace_map call on this thread with a
+ * directional map (RAW sums); returns 0 when there are none. */
+int orc_map_directions(double *dir_pos, double *dir_neg, size_t cap);
 
 /* Pure specular path of each ray: per bounce the hit polygon (-1 = miss, then stop), the leg
  * length and the hit point.  Used for the image-lattice known answers. */

@@ -46,7 +46,7 @@ class ReceiverDesc(C.Structure):
 
 class MapDesc(C.Structure):
     _fields_ = [("n_receivers", C.c_int32), ("time_1pt", C.c_int32), ("origins", _dp), ("increment", C.c_double),
-                ("cutoff_ms", C.c_double), ("walk", C.c_int32), ("reserved", C.c_int32)]
+                ("cutoff_ms", C.c_double), ("walk", C.c_int32), ("directional", C.c_int32)]
 
 
 class TraceParams(C.Structure):
@@ -105,7 +105,8 @@ class Stats(C.Structure):
 # Every symbol include/pach_gpu.h declares (checked by the CPU test suite).
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
            "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_direct_sound", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
-           "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_map_parameters", "pach_etc_parameters",
+           "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_trace_get_map_directions", "pach_map_parameters",
+           "pach_etc_parameters",
            "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_medium_attenuation_third_octave", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
@@ -144,6 +145,7 @@ def _declare(L):
         "pach_trace_get_histograms": (C.c_int, [vp, C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_size_t]),
         "pach_trace_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
         "pach_trace_get_map": (C.c_int, [vp, C.c_int32, _dp, _dp, _dp, _ip, C.c_size_t]),
+        "pach_trace_get_map_directions": (C.c_int, [vp, C.c_int32, _dp, _dp, C.c_size_t]),
         "pach_map_parameters": (C.c_int, [vp, C.c_int32, C.c_int32, _dp, _dp, _dp, _dp, _dp]),
         "pach_etc_parameters": (C.c_int, [_dp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, _dp, _dp, _dp,
                                           _dp, _dp]),

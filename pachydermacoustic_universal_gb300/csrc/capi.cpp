@@ -14,6 +14,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "engine.h"
@@ -89,7 +90,7 @@ struct pach_run {
     bool has_map = false;
     MapGrid mg;
     std::vector<double> map_org;
-    DevMem mrec, mdir, mcell, mentry, mE, mP;
+    DevMem mrec, mdir, mcell, mentry, mE, mP, mDp, mDn;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -109,7 +110,7 @@ struct pach_run {
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
                           &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh, &bbvhq,
-                          &mrec, &mdir, &mcell, &mentry, &mE, &mP})
+                          &mrec, &mdir, &mcell, &mentry, &mE, &mP, &mDp, &mDn})
             m->release();
     }
 };
@@ -415,6 +416,12 @@ void run_worker(pach_run *run) {
             TRY(run->mP.alloc(nm * sizeof(double)));
             TRY(cudaMemsetAsync(run->mE.p, 0, run->mE.bytes, stream));
             TRY(cudaMemsetAsync(run->mP.p, 0, run->mP.bytes, stream));
+            if (g.directional) {
+                TRY(run->mDp.alloc(3 * nm * sizeof(double)));
+                TRY(run->mDn.alloc(3 * nm * sizeof(double)));
+                TRY(cudaMemsetAsync(run->mDp.p, 0, run->mDp.bytes, stream));
+                TRY(cudaMemsetAsync(run->mDn.p, 0, run->mDn.bytes, stream));
+            }
         }
 
         // launch shapes: one resident wave of blocks for the trace and shade kernels
@@ -493,6 +500,9 @@ void run_worker(pach_run *run) {
             m.entry = run->mentry.as<uint2>();
             m.E = run->mE.as<double>();
             m.P = run->mP.as<double>();
+            m.Dp = g.directional ? run->mDp.as<double>() : nullptr;
+            m.Dn = g.directional ? run->mDn.as<double>() : nullptr;
+            m.directional = g.directional ? 1 : 0;
             for (int a = 0; a < 3; ++a) {
                 m.lo[a] = (float)g.mn[a];
                 m.hi[a] = (float)g.mx[a];
@@ -506,6 +516,7 @@ void run_worker(pach_run *run) {
             m.size_mod = (float)(1.0 / (M_PI * g.r2));
             const HostScene &hs0 = run->rooms[0].scene->hs;
             for (int o = 0; o < kBands; ++o) m.atten_k[o] = (float)(-0.1 * std::log2(10.0) * hs0.atten[o]);
+            m.rho_c = (float)(hs0.rho * hs0.c);  // Map_Receiver: Rho_C = rho * Sound_Speed
         }
         r.seed = run->p.seed;
         r.max_seg = run->p.max_segments_per_ray > 0 ? run->p.max_segments_per_ray : (1ll << 22);
@@ -1089,13 +1100,39 @@ pach_status pach_trace_get_map(pach_run *run, int32_t scaled, double *energy, do
     const size_t n = (size_t)g.M * kBands * g.T;
     if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 8 * bins");
     cudaSetDevice(run->scene->device);
-    // Histogram.Scale(N) divides energy and pressure by N; a cluster's Scale(1 / n_sources) multiplies back
+    // Histogram.Scale(N) divides energy and pressure by N (Directional_Histogram.Scale: pressure by
+    // sqrt(N)); a cluster's Scale(1 / n_sources) multiplies back
     const double N = (double)std::max(1ll, run->rays_done.load());
     const double f = (double)run->nsrc / N;
-    for (auto [dst, src] : {std::pair<double *, DevMem *>{energy, &run->mE}, {pressure, &run->mP}}) {
+    const double fp = g.directional ? std::sqrt((double)run->nsrc / N) : f;
+    for (auto [dst, src, k] : {std::tuple<double *, DevMem *, double>{energy, &run->mE, f}, {pressure, &run->mP, fp}}) {
         if (!dst) continue;
         cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map copy"));
+        if (scaled)
+            for (size_t i = 0; i < n; ++i) dst[i] *= k;
+    }
+    return PACH_OK;
+}
+
+pach_status pach_trace_get_map_directions(pach_run *run, int32_t scaled, double *dir_pos, double *dir_neg,
+                                          size_t cap_bins) {
+    if (pach_status s = check_run(run)) return s;
+    if (!run->has_map || !run->mg.directional) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no directional map");
+    {
+        std::lock_guard<std::mutex> lk(run->mu);
+        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+    }
+    const MapGrid &g = run->mg;
+    const size_t n = (size_t)g.M * 3 * kBands * g.T;
+    if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 3 * 8 * bins");
+    cudaSetDevice(run->scene->device);
+    const double f = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
+    for (auto [dst, src] : {std::pair<double *, DevMem *>{dir_pos, &run->mDp}, {dir_neg, &run->mDn}}) {
+        if (!dst) continue;
+        cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map direction copy"));
         if (scaled)
             for (size_t i = 0; i < n; ++i) dst[i] *= f;
     }

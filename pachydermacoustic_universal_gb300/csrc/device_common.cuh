@@ -411,7 +411,11 @@ __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomPara
 // sample is (int)(time * 1000), a truncation, so arrivals up to 1 ms before the direct arrival
 // land in bin 0; samples outside [0, T) are dropped.  Histogram_1Pt keeps every arrival in bin 0
 // and no pressure.
-__device__ __forceinline__ void map_add(const MapDev &M, int k, int oct, double time, float e) {
+// Directional_Histogram.Add (1813-1825) for a directional map: pressure sqrt(E rho c), and the
+// arrival direction -d split by sign into the +/- component histograms, each term rounded to float
+// as the reference rounds it.  (The reference has no lower bound there; an arrival more than 1 ms
+// before the direct one cannot occur at a receiver the direct path reaches, and is dropped.)
+__device__ __forceinline__ void map_add(const MapDev &M, int k, int oct, double time, float e, float3 d) {
     long long s = 0;
     if (!M.one_pt) {
         const double x = time * 1000.0;
@@ -420,7 +424,18 @@ __device__ __forceinline__ void map_add(const MapDev &M, int k, int oct, double 
     }
     const size_t i = ((size_t)k * kBands + oct) * M.T + s;
     atomicAdd(M.E + i, (double)e);
-    if (!M.one_pt) atomicAdd(M.P + i, (double)sqrtf(e));
+    if (M.one_pt) return;
+    if (!M.directional) {
+        atomicAdd(M.P + i, (double)sqrtf(e));
+        return;
+    }
+    atomicAdd(M.P + i, (double)sqrtf(e * M.rho_c));
+    const float ca[3] = {-d.x, -d.y, -d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const size_t j = (((size_t)k * 3 + a) * kBands + oct) * M.T + s;
+        atomicAdd((ca[a] > 0.f ? M.Dp : M.Dn) + j, (double)(ca[a] * e));
+    }
 }
 
 // OBox.IsPointInBox and OBox.Intersect (Hare AABB, not in the reference tree), restated as
@@ -540,7 +555,7 @@ __device__ __forceinline__ uint32_t map_detect_octave(const MapDev &M, const Roo
         if (!sphere_hit(__ldg(M.rec + k), o, d, tseg, t, half)) return;
         ++n;
         const double time = t_sum + (double)(t * P.inv_c) - __ldg(M.direct + k);
-        map_add(M, k, oct, time, Iabs * exp2f(M.atten_k[oct] * (float)time) * M.size_mod);
+        map_add(M, k, oct, time, Iabs * exp2f(M.atten_k[oct] * (float)time) * M.size_mod, d);
     });
     return n;
 }
@@ -558,7 +573,7 @@ __device__ __forceinline__ uint32_t map_detect_broad(const MapDev &M, const Room
         const double time = t_sum + (double)(t * P.inv_c) - __ldg(M.direct + k);
 #pragma unroll
         for (int oct = 0; oct < kBands; ++oct)
-            map_add(M, k, oct, time, E[oct] * sc[oct] * exp2f(M.atten_k[oct] * (float)time) * M.size_mod);
+            map_add(M, k, oct, time, E[oct] * sc[oct] * exp2f(M.atten_k[oct] * (float)time) * M.size_mod, d);
     });
     return n;
 }

@@ -131,12 +131,15 @@ struct MapDev {
     const int *cell;          // [cells + 1] entry offsets, cell = (x * ny + y) * nz + z
     const uint2 *entry;       // (receiver, neighbour mask)
     double *E, *P;            // [M][8][T]
+    double *Dp, *Dn;          // [M][3][8][T] (directional maps)
     float lo[3], hi[3];       // grid box (OBox)
     float vd[3];              // cell size
     int n[3];                 // cells per axis
     int M, T;
     int one_pt;               // Histogram_1Pt: every arrival in bin 0, no pressure
     int walk;                 // 0 the reference's walks, 1 every crossed cell
+    int directional;          // Directional_Histogram: pressure sqrt(E rho c) and arrival directions
+    float rho_c;
     float size_mod;           // 1 / (pi r^2)
     float atten_k[kBands];    // exp2 factor per second after the direct arrival: -0.1 log2(10) m
 };
@@ -144,7 +147,7 @@ struct MapDev {
 // Host side of the mapping receivers (map_grid.cpp): the grid in FP64 and its cell lists.
 struct MapGrid {
     int M = 0, T = 1, walk = 0;
-    bool one_pt = false;
+    bool one_pt = false, directional = false;
     double r = 0, r2 = 0;
     double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0}, vd[3] = {1, 1, 1};
     int n[3] = {1, 1, 1};

@@ -19,6 +19,8 @@ bool build_map_grid(const pach_map_desc &d, const double src[3], int nsrc, doubl
     g.M = M;
     g.one_pt = d.time_1pt != 0;
     g.walk = d.walk;
+    g.directional = d.directional != 0;
+    if (g.directional && g.one_pt) { err = "map: a one-point histogram has no directions"; return false; }
     // Histogram(SampleRate 1000, COTime_in ms): CO_Time = COTime_in / 1000, SampleCT = (int)(CO_Time * 1000)
     g.T = g.one_pt ? 1 : (int)(d.cutoff_ms / 1000.0 * 1000.0);
     if (g.T < 1) { err = "map: no histogram bins"; return false; }

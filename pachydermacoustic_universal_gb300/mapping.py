@@ -93,15 +93,28 @@ class Map_Receiver:
     def Pressure_rms(self, t, Octave):
         return float(self._bank._P[self.Index, Octave, t])
 
+    def Directions_Pos(self, Octave, t):
+        """Directional_Histogram.Directions_Pos: the (+x, +y, +z) arrival sums at sample t."""
+        return tuple(float(v) for v in self._bank._Dp[self.Index, :, Octave, t])
+
+    def Directions_Neg(self, Octave, t):
+        return tuple(float(v) for v in self._bank._Dn[self.Index, :, Octave, t])
+
     def Energy(self, t, oct):
         return float(self._bank._E[self.Index, oct, t])
 
-    def Combine_Sample(self, sample, Energy_in, Pressure_in, Octave):
-        """Histogram.Combine_Sample (Classes_Receivers.cs:1168-1173)."""
+    def Combine_Sample(self, sample, Energy_in, Pressure_in, Octave, dir_pos=None, dir_neg=None):
+        """Histogram.Combine_Sample / Directional_Histogram.Combine_Sample (Classes_Receivers.cs:1168-1173,
+        1750-1772)."""
         if sample >= self._bank._E.shape[2]:
             return
+        if self._bank.Directional and sample < 0:
+            sample = 0
         self._bank._E[self.Index, Octave, sample] += Energy_in
         self._bank._P[self.Index, Octave, sample] += Pressure_in
+        if self._bank.Directional and dir_pos is not None:
+            self._bank._Dp[self.Index, :, Octave, sample] += dir_pos
+            self._bank._Dn[self.Index, :, Octave, sample] += dir_neg
 
 
 class PachMapReceiver:
@@ -118,10 +131,11 @@ class PachMapReceiver:
         self.Map_Mesh = Map_MeshIn
         self.delay_ms = 0.0
         self.Rec_List = []
+        self.Directional = bool(DirectionalIn)
         if Map_MeshIn is None:          # the reading constructor (Read_pachm fills the fields)
             return
-        if DirectionalIn:
-            raise NotImplementedError("directional map histograms are not part of the GPU engine")
+        if self.Directional and Time1Pt:
+            raise ValueError("a one-point map histogram has no directions")
         self.SWL = Src_Pt.SWL()
         self.Src = tuple(Src_Pt.Origin)
         self.SrcType = Src_Pt.Type()
@@ -131,7 +145,6 @@ class PachMapReceiver:
         self.Rec_Vertex = bool(RecOnVertex)
         self.Mesh_Offset = bool(Offset_Mesh)
         self.Z_Displacement = bool(Z_displacementIn)
-        self.Directional = False
         self.Time1Pt = bool(Time1Pt)
         self.walk = int(walk)
         self.SampleCT = 1 if self.Time1Pt else int(np.floor(self.CutOffTime * self.SampleRate / 1000))
@@ -163,17 +176,26 @@ class PachMapReceiver:
             direct = np.zeros(len(pts))
         self._origins = pts
         T = 1 if self.Time1Pt else int(self.CutOffTime / 1000.0 * 1000.0)
-        self._E = np.zeros((len(pts), 8, T))
-        self._P = np.zeros((len(pts), 8, T))
+        self._alloc(len(pts), T)
         self.Rec_List = [Map_Receiver(self, i, p, direct[i], rho_c) for i, p in enumerate(pts)]
 
+    def _alloc(self, M, T):
+        self._E = np.zeros((M, 8, T))
+        self._P = np.zeros((M, 8, T))
+        if self.Directional:
+            self._Dp = np.zeros((M, 3, 8, T))
+            self._Dn = np.zeros((M, 3, 8, T))
+
     def map_receivers(self) -> MapReceivers:
-        return MapReceivers(self._origins, self.increment, self.CutOffTime, self.Time1Pt, self.walk)
+        return MapReceivers(self._origins, self.increment, self.CutOffTime, self.Time1Pt, self.walk, self.Directional)
 
     def _set(self, h):
         """Results of a run (tracer.Run.map_histograms): histograms and the engine's direct arrival times."""
         self._E[:] = h["energy"]
         self._P[:] = h["pressure"]
+        if self.Directional:
+            self._Dp[:] = h["dir_pos"]
+            self._Dn[:] = h["dir_neg"]
         for r, t in zip(self.Rec_List, h["direct_time"]):
             r.Direct_Time = float(t)
 
@@ -185,7 +207,7 @@ class PachMapReceiver:
         return [r.Origin for r in self.Rec_List]
 
     def Data_Type(self):
-        return "Type;Map_Data_NoDir"
+        return "Type;Map_Data" if self.Directional else "Type;Map_Data_NoDir"
 
     def MapMesh(self):
         return self.Map_Mesh
@@ -208,15 +230,21 @@ class PachMapReceiver:
         for i, rec in enumerate(self.Rec_List):
             if not (D.Validity[i] or D.Screen_atten):
                 continue
+            # a directional histogram adds the unit vector towards the source to both direction sums
+            u = np.subtract(S.Origin, rec.Origin)
+            u = u / np.linalg.norm(u)
             for oct in range(8):
                 Io = D.Io[i][oct]
                 for s in range(Io.size):
                     if s < self.SampleCT:
-                        rec.Combine_Sample(s, Io[s], np.sqrt(Io[s]), oct)
+                        rec.Combine_Sample(s, Io[s], np.sqrt(Io[s]), oct, u, u)
 
     def Combine_Clones(self, other):
         self._E += other._E
         self._P += other._P
+        if self.Directional:
+            self._Dp += other._Dp
+            self._Dn += other._Dn
 
 
 # ---------------------------------------------------------------- parameter maps

@@ -11,6 +11,9 @@ then per source and receiver its index (uint32), direct arrival time and rho c (
 the band index (uint32) and per sample energy and pressure (doubles), "End_Receiver_Hits";
 "End_of_File".  The reader takes the receivers from the mesh (face centroids or vertices, without
 the placement offset) as the reference's reader does, and the v2.5+ layout (pressure stored).
+Directional maps ("Type;Map_Data") add six doubles per sample after the pressure, the +x +y +z and
+-x -y -z arrival sums, as the reference's writer writes them; the reference's reader takes those six
+as singles (ReadSingle) and so misreads its own directional files -- this reader takes doubles.
 """
 from __future__ import annotations
 
@@ -60,10 +63,13 @@ def write_pachm(filename, maps):
                 w.double(m0.Rec_List[i].Rho_C)
                 for o in range(8):
                     w.uint32(o)
-                    pairs = np.empty((n, 2))
-                    pairs[:, 0] = m._E[i, o, :n]
-                    pairs[:, 1] = m._P[i, o, :n]
-                    w.doubles(pairs.reshape(-1))
+                    rec = np.empty((n, 8 if m0.Directional else 2))
+                    rec[:, 0] = m._E[i, o, :n]
+                    rec[:, 1] = m._P[i, o, :n]
+                    if m0.Directional:
+                        rec[:, 2:5] = m._Dp[i, :, o, :n].T
+                        rec[:, 5:8] = m._Dn[i, :, o, :n].T
+                    w.doubles(rec.reshape(-1))
                 w.string("End_Receiver_Hits")
         w.string("End_of_File")
 
@@ -125,8 +131,8 @@ def read_pachm(filename):
                 m.Rec_Vertex = on_vertex
                 m.increment = 0.0
                 m.Time1Pt = SampleCT == 1
-                m._E = np.zeros((Rec_CT, 8, SampleCT))
-                m._P = np.zeros((Rec_CT, 8, SampleCT))
+                m.Directional = directional
+                m._alloc(Rec_CT, SampleCT)
                 m.Rec_List = []
                 for i in range(Rec_CT):
                     r.uint32()
@@ -139,12 +145,15 @@ def read_pachm(filename):
                     for o in range(8):
                         if r.uint32() != o:
                             raise ValueError(f"Octave {o} Expected")
-                        per = (2 if version >= 2.5 else 1) + (6 if directional else 0)
-                        vals = r.doubles(per * SampleCT).reshape(SampleCT, per) if not directional else \
-                            _read_directional(r, SampleCT, version)
+                        npr = 2 if version >= 2.5 else 1
+                        per = npr + (6 if directional else 0)
+                        vals = r.doubles(per * SampleCT).reshape(SampleCT, per)
                         m._E[i, o] = vals[:, 0]
                         if version >= 2.5:
                             m._P[i, o] = vals[:, 1]
+                        if directional:
+                            m._Dp[i, :, o] = vals[:, npr:npr + 3].T
+                            m._Dn[i, :, o] = vals[:, npr + 3:npr + 6].T
                     if r.string() != "End_Receiver_Hits":
                         raise ValueError("End of Receiver Hits Expected")
         elif tag == "End_of_File":
@@ -157,15 +166,3 @@ def _location(mesh, on_vertex, i):
     if on_vertex:
         return mesh.vertices[i]
     return mesh.Polygon_Vertices(i).mean(axis=0)
-
-
-def _read_directional(r, n, version):
-    """Directional records: energy, [pressure,] then six single-precision direction components (the
-    reference's reader takes ReadSingle although its writer writes doubles)."""
-    out = np.zeros((n, 2))
-    for e in range(n):
-        out[e, 0] = r.double()
-        if version >= 2.5:
-            out[e, 1] = r.double()
-        r.floats(6)
-    return out

@@ -79,6 +79,7 @@ class MapReceivers:
     cutoff_ms: float
     time_1pt: bool = False
     walk: int = 0
+    directional: bool = False
 
     def desc(self):
         org = np.ascontiguousarray(self.origins, dtype=np.float64).reshape(-1, 3)
@@ -89,6 +90,7 @@ class MapReceivers:
         d.increment = float(self.increment)
         d.cutoff_ms = float(self.cutoff_ms)
         d.walk = int(self.walk)
+        d.directional = int(bool(self.directional))
         d._keep = org
         return d
 
@@ -202,7 +204,13 @@ class Run:
         M, T = int(sizes[0]), int(sizes[1])
         E, P, D = np.zeros((M, 8, T)), np.zeros((M, 8, T)), np.zeros(M)
         check(L.pach_trace_get_map(self.handle, int(bool(scaled)), dptr(E), dptr(P), dptr(D), None, E.size))
-        return {"energy": E, "pressure": P, "direct_time": D}
+        out = {"energy": E, "pressure": P, "direct_time": D}
+        pm = self.params.map
+        if pm and pm.contents.directional:
+            Dp, Dn = np.zeros((M, 3, 8, T)), np.zeros((M, 3, 8, T))
+            check(L.pach_trace_get_map_directions(self.handle, int(bool(scaled)), dptr(Dp), dptr(Dn), Dp.size))
+            out.update(dir_pos=Dp, dir_neg=Dn)
+        return out
 
     def map_parameters(self, decay_depth=30, clarity_ms=80):
         """T_X, EDT, clarity (dB), definition (%) and total energy of every map receiver and band [M][8],

@@ -195,3 +195,19 @@ def test_split_ray_tracer_fills_a_pach_map_receiver_and_parameter_maps():
                    "definition": AcousticalMath.Definition(etc, 1000, 0.05, 0.0, False)}
             for k in maps:
                 np.testing.assert_allclose(maps[k][i], ref[k], rtol=1e-9, equal_nan=True, err_msg=k)
+
+
+def test_directional_map_matches_oracle():
+    """Directional_Histogram in a map: pressure sqrt(E rho c) and the +/- arrival sums."""
+    w, org = _shifted(rooms.shoebox_c1(), rooms.audience_plane((1.0, 1.0), (9.0, 7.0), 1.0, 1.0))
+    m = tracer.MapReceivers(org, 1.0, 2000.0, walk=1, directional=True)
+    hg, sg = tracer.trace(w, rays=1500, seed=13, pure_specular=True, map_receivers=m)
+    om = types.SimpleNamespace(origins=org, increment=1.0, cutoff_ms=2000.0, time_1pt=False, walk=1, directional=True)
+    ho, so = O.trace(w, rays=1500, seed=13, pure_specular=True, map_receivers=om, threads=4)
+    g = hg["map"]
+    np.testing.assert_allclose(g["energy"].sum(axis=2), ho["map_energy"].sum(axis=2), rtol=1e-3)
+    np.testing.assert_allclose(g["pressure"].sum(axis=2), ho["map_pressure"].sum(axis=2), rtol=1e-3)
+    for k, ko in (("dir_pos", "map_dir_pos"), ("dir_neg", "map_dir_neg")):
+        a, b = g[k].sum(axis=-1), ho[ko].sum(axis=-1)
+        np.testing.assert_allclose(a, b, rtol=2e-3, atol=1e-6 * np.abs(b).max())
+    assert (g["dir_pos"] >= 0).all() and (g["dir_neg"] <= 0).all()

@@ -43,18 +43,21 @@ def test_receiver_placement_follows_partition():
     assert all(r.Direct_Time == 0 for r in m4.Rec_List)
 
 
-def _filled(seed=0, time_1pt=False):
+def _filled(seed=0, time_1pt=False, directional=False):
     src = GeodesicSource([100.0] * 8, (1.0, 1.0, 3.0))
-    m = PachMapReceiver(_mesh(), src, 1000, 0.5, SC, 500.0, time_1pt, True, False, False, False)
+    m = PachMapReceiver(_mesh(), src, 1000, 0.5, SC, 500.0, time_1pt, True, directional, False, False)
     rng = np.random.default_rng(seed)
     m._E[:] = rng.random(m._E.shape) * 1e-6
     m._P[:] = np.sqrt(m._E)
+    if directional:
+        m._Dp[:] = rng.random(m._Dp.shape) * 1e-6
+        m._Dn[:] = -rng.random(m._Dn.shape) * 1e-6
     return m
 
 
-@pytest.mark.parametrize("time_1pt", [False, True])
-def test_pachm_round_trip(tmp_path, time_1pt):
-    a, b = _filled(1, time_1pt), _filled(2, time_1pt)
+@pytest.mark.parametrize("time_1pt,directional", [(False, False), (True, False), (False, True)])
+def test_pachm_round_trip(tmp_path, time_1pt, directional):
+    a, b = _filled(1, time_1pt, directional), _filled(2, time_1pt, directional)
     b.Src = (5.0, 1.0, 3.0)
     b.delay_ms = 12.5
     fn = tmp_path / "map.pachm"
@@ -67,6 +70,10 @@ def test_pachm_round_trip(tmp_path, time_1pt):
         assert [r.Direct_Time for r in got.Rec_List] == [r.Direct_Time for r in src_map.Rec_List]
         assert got.Src == src_map.Src and got.SrcType == "Geodesic" and got.delay_ms == src_map.delay_ms
         assert got.SampleCT == src_map.SampleCT and got.SampleRate == 1000
+        assert got.Directional == directional
+        if directional:
+            np.testing.assert_array_equal(got._Dp, src_map._Dp)
+            np.testing.assert_array_equal(got._Dn, src_map._Dn)
     np.testing.assert_array_equal(maps[0].Map_Mesh.vertices, a.Map_Mesh.vertices)
     assert maps[0].Map_Mesh.faces == a.Map_Mesh.faces
     # the reader places receivers on the (unoffset) face centroids
