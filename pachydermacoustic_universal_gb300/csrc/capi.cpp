@@ -90,7 +90,7 @@ struct pach_run {
     bool has_map = false;
     MapGrid mg;
     std::vector<double> map_org;
-    DevMem mrec, mdir, mcell, mentry, mE, mP, mDp, mDn;
+    DevMem mrec, mdir, mcell, mentry, mE, mP, mDp, mDn, drecid;
     // worker
     std::thread worker;
     std::mutex mu;
@@ -110,7 +110,7 @@ struct pach_run {
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
                           &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh, &bbvhq,
-                          &mrec, &mdir, &mcell, &mentry, &mE, &mP, &mDp, &mDn})
+                          &mrec, &mdir, &mcell, &mentry, &mE, &mP, &mDp, &mDn, &drecid})
             m->release();
     }
 };
@@ -332,6 +332,7 @@ void run_worker(pach_run *run) {
         }
         // receivers, sources, powers and room table over all rooms
         std::vector<float4> rec(std::max(R, 1)), src;
+        std::vector<int> rec_id(std::max(R, 1), 0);
         std::vector<float> e0;
         std::vector<RoomParams> rp(n_rooms);
         std::vector<long long> rprim(n_rooms + 1);
@@ -356,9 +357,27 @@ void run_worker(pach_run *run) {
             P.t_eps = (float)(2e-7 * hs.scale);
             P.rec_begin = k;
             P.R = (int)rm.rec.size();
-            for (const pach_receiver_desc &q : rm.rec)
-                rec[k++] = make_float4((float)q.origin[0], (float)q.origin[1], (float)q.origin[2],
-                                       (float)(q.radius * q.radius));
+            // the room's receivers ordered by the coordinate of their widest spread; rec_id keeps each
+            // slot's histogram row
+            {
+                double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+                for (const pach_receiver_desc &q : rm.rec)
+                    for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], q.origin[a]); hi[a] = std::max(hi[a], q.origin[a]); }
+                int ax = 0;
+                for (int a = 1; a < 3; ++a)
+                    if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+                std::vector<int> ord(rm.rec.size());
+                for (size_t i = 0; i < ord.size(); ++i) ord[i] = (int)i;
+                std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+                    return (float)rm.rec[a].origin[ax] < (float)rm.rec[b].origin[ax];
+                });
+                for (int i : ord) {
+                    const pach_receiver_desc &q = rm.rec[(size_t)i];
+                    rec_id[k] = P.rec_begin + i;
+                    rec[k++] = make_float4((float)q.origin[0], (float)q.origin[1], (float)q.origin[2],
+                                           (float)(q.radius * q.radius));
+                }
+            }
             P.src_begin = (int)src.size();
             P.nsrc = (int)rm.src.size();
             for (const pach_source_desc &s : rm.src) {
@@ -382,6 +401,7 @@ void run_worker(pach_run *run) {
         }
         rprim[n_rooms] = rp[n_rooms - 1].prim_end;
         TRY(upload(run->drec, rec.data(), rec.size() * sizeof(float4)));
+        TRY(upload(run->drecid, rec_id.data(), rec_id.size() * sizeof(int)));
         TRY(upload(run->dsrc, src.data(), src.size() * sizeof(float4)));
         TRY(upload(run->de0, e0.data(), e0.size() * sizeof(float)));
         TRY(upload(run->droom, rp.data(), rp.size() * sizeof(RoomParams)));
@@ -471,6 +491,7 @@ void run_worker(pach_run *run) {
         r.room_prim = run->droomprim.as<long long>();
         r.n_rooms = n_rooms;
         r.rec = run->drec.as<float4>();
+        r.rec_id = run->drecid.as<int>();
         r.R = R;
         r.T = T;
         r.fs = (double)run->p.sample_rate;

@@ -355,39 +355,43 @@ __device__ __forceinline__ void hist_add(const DevRun &r, float rho_c, int k, in
     atomicAdd(r.hAn + (((size_t)k * 3 + kind) * kBands + oct) * r.T + bin, (double)e);
 }
 
-__device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, const float4 *rec, int k,
-                                            uint32_t prim, double time, float e);
+__device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, float4 rc, int k, uint32_t prim,
+                                            double time, float e);
 
 // Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half,
 // over the receivers of the ray's room (rec: the run's receiver table in shared memory).
-__device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomParams &P, const float4 *rec, float3 o,
-                                                  float3 d, float tseg, double t_sum, float Iabs, int oct, int mask,
-                                                  uint32_t prim) {
+__device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomParams &P, const float4 *rec,
+                                                  const int *rid, float3 o, float3 d, float tseg, double t_sum,
+                                                  float Iabs, int oct, int mask, uint32_t prim) {
     uint32_t n = 0;
-    for (int k = P.rec_begin; k < P.rec_begin + P.R; ++k) {
+    for (int s = P.rec_begin; s < P.rec_begin + P.R; ++s) {
+        const float4 c = rec[s];
         float t, half;
-        if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
+        if (!sphere_hit(c, o, d, tseg, t, half)) continue;
         ++n;
+        const int row = rid ? rid[s] : s;
         const double time = t_sum + (double)(t * P.inv_c);
         const long long bin = (long long)(time * r.fs);
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
         const float e = Iabs * exp2f(P.atten_k[oct] * (float)time) * kInvPi * half;
-        hist_add(r, P.rho_c, k, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
-        if (r.capture) capture_add(r, P, rec, k, prim, time, e);
+        hist_add(r, P.rho_c, row, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
+        if (r.capture) capture_add(r, P, c, row, prim, time, e);
     }
     return n;
 }
 
 // Spherical_Receiver.CheckBroadbandRay (Classes_Receivers.cs:803-829): every band of the range,
 // analysis bin 0 (specular).
-__device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomParams &P, const float4 *rec, float3 o,
-                                                 float3 d, float tseg, double t_sum, const float (&E)[kBands],
-                                                 const float (&sc)[kBands], uint32_t prim) {
+__device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomParams &P, const float4 *rec,
+                                                 const int *rid, float3 o, float3 d, float tseg, double t_sum,
+                                                 const float (&E)[kBands], const float (&sc)[kBands], uint32_t prim) {
     uint32_t n = 0;
-    for (int k = P.rec_begin; k < P.rec_begin + P.R; ++k) {
+    for (int s = P.rec_begin; s < P.rec_begin + P.R; ++s) {
+        const float4 c = rec[s];
         float t, half;
-        if (!sphere_hit(rec[k], o, d, tseg, t, half)) continue;
+        if (!sphere_hit(c, o, d, tseg, t, half)) continue;
         ++n;
+        const int k = rid ? rid[s] : s;
         const double time = t_sum + (double)(t * P.inv_c);
         const long long bin = (long long)(time * r.fs);
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
@@ -399,7 +403,7 @@ __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomPara
             hist_add(r, P.rho_c, k, oct, bin, e, d, 0);
             esum += e;
         }
-        if (r.capture) capture_add(r, P, rec, k, prim, time, esum);
+        if (r.capture) capture_add(r, P, c, k, prim, time, esum);
     }
     return n;
 }
@@ -669,11 +673,12 @@ __device__ __forceinline__ float3 primary_dir(const DevRun &r, int nsrc, uint32_
 
 // Training capture: energy e detected at receiver k at time (s) from primary prim, added to the bin
 // of the primary's emission direction in the window of (time - direct arrival).
-__device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, const float4 *rec, int k,
-                                            uint32_t prim, double time, float e) {
+// rc: the receiver (x, y, z, r^2), k: its histogram row
+__device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, float4 rc, int k, uint32_t prim,
+                                            double time, float e) {
     const int s = P.src_begin + (int)((prim + 1ull) % (unsigned long long)P.nsrc);
     const float4 src = r.src[s];
-    const double dx = rec[k].x - src.x, dy = rec[k].y - src.y, dz = rec[k].z - src.z;
+    const double dx = rc.x - src.x, dy = rc.y - src.y, dz = rc.z - src.z;
     const float ms = (float)((time - sqrt(dx * dx + dy * dy + dz * dz) * P.inv_c_d) * 1000.0);
     const int win = (ms >= r.cap_edge[0]) + (ms >= r.cap_edge[1]) + (ms >= r.cap_edge[2]);
     if (r.capture_mode == 2) {
@@ -800,10 +805,19 @@ __device__ void flush_counters(const DevRun &r, const LocalCounters &L) {
 
 // Receiver table for detection: staged in shared memory when it is small (the common case), else read
 // through L1 (a batch of many rooms: each ray tests only its room's receivers).
-__device__ __forceinline__ const float4 *stage_receivers(const DevRun &r, float4 *smem) {
-    if (r.R > kSmemReceivers) return r.rec;
-    for (int i = threadIdx.x; i < r.R; i += blockDim.x) smem[i] = r.rec[i];
+// The run's receiver table (and the row of each sorted slot) in shared memory when it fits.
+__device__ __forceinline__ const float4 *stage_receivers(const DevRun &r, float4 *smem, const int *&rid) {
+    if (r.R > kSmemReceivers) {
+        rid = r.rec_id;
+        return r.rec;
+    }
+    int *sid = reinterpret_cast<int *>(smem + (r.R > 0 ? r.R : 1));
+    for (int i = threadIdx.x; i < r.R; i += blockDim.x) {
+        smem[i] = r.rec[i];
+        if (r.rec_id) sid[i] = r.rec_id[i];
+    }
     __syncthreads();
+    rid = r.rec_id ? sid : nullptr;
     return smem;
 }
 

@@ -154,7 +154,8 @@ __global__ void k_cond(DevRun r, cudaGraphConditionalHandle h) {
 template <bool MAP, bool SMALL>
 __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
-    const float4 *s_rec = stage_receivers(r, s_rec_buf);
+    const int *s_rid;
+    const float4 *s_rec = stage_receivers(r, s_rec_buf, s_rid);
     LocalCounters L;
     const DevScene &S = r.S;
     WaveCtl *c = r.ctl;
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
             ++L.v[C_SEGA];
             if (!hit) {
                 if (order > P.is_order) {
-                    L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
+                    L.v[C_DET] += detect_broad(r, P, s_rec, s_rid, pos, d, 1e6f, t_sum, E, sc, (uint32_t)prim);
                     if constexpr (MAP) L.v[C_DET] += map_detect_broad(r.map, P, pos, d, 1e6f, t_sum, E, sc);
                 }
 #pragma unroll
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(128) k_broadband(DevRun r) {
                 break;
             }
             if (order > P.is_order) {
-                L.v[C_DET] += detect_broad(r, P, s_rec, pos, d, t, t_sum, E, sc, (uint32_t)prim);
+                L.v[C_DET] += detect_broad(r, P, s_rec, s_rid, pos, d, t, t_sum, E, sc, (uint32_t)prim);
                 if constexpr (MAP) L.v[C_DET] += map_detect_broad(r.map, P, pos, d, t, t_sum, E, sc);
             }
             t_sum += (double)t * P.inv_c_d;
@@ -492,7 +493,8 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
 template <bool FUSED, bool MAP>
 __global__ void __launch_bounds__(256) k_shade(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
-    const float4 *s_rec = stage_receivers(r, s_rec_buf);
+    const int *s_rid;
+    const float4 *s_rec = stage_receivers(r, s_rec_buf, s_rid);
     LocalCounters L;
     const DevScene &S = r.S;
     WaveCtl *c = r.ctl;
@@ -524,8 +526,8 @@ __global__ void __launch_bounds__(256) k_shade(DevRun r) {
             const float t = __int_as_float(h.y);
             ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
             const RoomParams &P = r.rooms[R.room];
-            L.v[C_DET] += detect_octave(r, P, s_rec, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct, R.mask,
-                                        R.prim);
+            L.v[C_DET] += detect_octave(r, P, s_rec, s_rid, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct,
+                                        R.mask, R.prim);
             if constexpr (MAP)
                 L.v[C_DET] += map_detect_octave(r.map, P, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct);
             if (!hit) {
