@@ -254,7 +254,7 @@ def main():
     _capi.lib()
     rooms_ = workload(args.workload, args.ray_scale)
     batched = len(rooms_) > 1
-    scenes = [tracer.DeviceScene(w.scene) for w in rooms_]
+    scenes = tracer.DeviceScene.many([w.scene for w in rooms_])
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
     B = sum(w.rays for w in rooms_) if batched else args.batch
     # this rank's primaries: steps are consecutive batches; ranks own disjoint ranges
@@ -279,7 +279,7 @@ def main():
         kw = dict(seed=args.seed, ray_begin=base + idx * B, kernel_timing=not e2e)
         t0 = time.perf_counter()
         # e2e: the public API from host buffers -- upload the scenes, trace, download the histograms
-        ds = [tracer.DeviceScene(w.scene) for w in rooms_] if e2e else scenes
+        ds = tracer.DeviceScene.many([w.scene for w in rooms_]) if e2e else scenes
         out = pinned if e2e else None
         if batched:
             h, s = tracer.trace_batch(rooms_, dscenes=ds, tune=tune, out=out, **kw)

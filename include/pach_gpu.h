@@ -222,6 +222,10 @@ int pach_last_error(char *buf, size_t cap);
 int pach_device_count(void);
 
 pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out);
+/* n scenes at once (a batch's rooms): the host builds (BVH, materials) run on `threads` host threads
+ * (0 = all cores), the device copies go to the calling thread's device.  On failure no scene is
+ * returned. */
+pach_status pach_scenes_create(const pach_scene_desc *descs, int32_t n, pach_scene **out, int32_t threads);
 void pach_scene_destroy(pach_scene *scene);
 /* Scene facts the SplitRayTracer ctor derives (Scene.SurfaceArea, Sound_speed, Rho_C, Attenuation). */
 pach_status pach_scene_info(const pach_scene *scene, int32_t *n_polys, int32_t *n_triangles,

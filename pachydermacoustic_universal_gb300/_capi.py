@@ -103,7 +103,8 @@ class Stats(C.Structure):
 
 
 # Every symbol include/pach_gpu.h declares (checked by the CPU test suite).
-EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scene_destroy",
+EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scenes_create",
+           "pach_scene_destroy",
            "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_direct_sound", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_trace_get_map_directions", "pach_map_parameters",
            "pach_etc_parameters",
@@ -130,6 +131,7 @@ def _declare(L):
         "pach_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "pach_device_count": (C.c_int, []),
         "pach_scene_create": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(vp)]),
+        "pach_scenes_create": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, C.POINTER(vp), C.c_int32]),
         "pach_scene_destroy": (None, [vp]),
         "pach_scene_info": (C.c_int, [vp, _ip, _ip, _dp, _dp, _dp, _dp]),
         "pach_trace_begin": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,

@@ -11,6 +11,7 @@
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -879,6 +880,52 @@ pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
         return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
     }
     *out = sc;
+    return PACH_OK;
+}
+
+pach_status pach_scenes_create(const pach_scene_desc *descs, int32_t n, pach_scene **out, int32_t threads) {
+    if (!out || (n > 0 && !descs) || n < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "scenes: bad arguments");
+    for (int i = 0; i < n; ++i) out[i] = nullptr;
+    for (int i = 0; i < n; ++i)
+        if (!(descs[i].pressure_hpa > 0) || !(descs[i].rel_humidity > 0) || descs[i].air_choice < 0 ||
+            descs[i].air_choice > 2)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) +
+                                                       ": pressure and humidity must be positive, air_choice 0..2");
+    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
+    int device = 0;
+    cudaGetDevice(&device);
+    // host builds (BVH, quantised nodes, materials) on worker threads, largest scenes first
+    std::vector<std::unique_ptr<pach_scene>> sc((size_t)n);
+    std::vector<std::string> errs((size_t)n);
+    std::vector<int> order((size_t)n);
+    for (int i = 0; i < n; ++i) order[(size_t)i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return descs[a].n_polys > descs[b].n_polys; });
+    std::atomic<int> next{0};
+    const int nt = std::max(1, std::min(n, threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency())));
+    auto work = [&] {
+        for (int j; (j = next.fetch_add(1)) < n;) {
+            const int i = order[(size_t)j];
+            sc[(size_t)i].reset(new pach_scene());
+            if (!build_host_scene(&descs[i], sc[(size_t)i]->hs, errs[(size_t)i])) sc[(size_t)i].reset();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (std::thread &t : pool) t.join();
+    for (int i = 0; i < n; ++i)
+        if (!sc[(size_t)i]) return fail(PACH_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) + ": " + errs[(size_t)i]);
+    // device copies on the caller's device
+    for (int i = 0; i < n; ++i) {
+        pach_scene *s = sc[(size_t)i].get();
+        s->device = device;
+        SceneArrays A;
+        append_scene(s->hs, A);
+        const cudaError_t e = upload_scene(A, s->tri, s->tri64, s->norm, s->mat, s->trans, s->bvh, s->bvhq, s->dev);
+        if (e != cudaSuccess)
+            return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
+    }
+    for (int i = 0; i < n; ++i) out[i] = sc[(size_t)i].release();
     return PACH_OK;
 }
 

@@ -13,8 +13,35 @@ from ._capi import check, dptr, iptr
 class DeviceScene:
     """A scene resident on the GPU (pach_scene_create)."""
 
-    def __init__(self, scene, bvh_leaf_max: int = 0):
+    def __init__(self, scene, bvh_leaf_max: int = 0, _handle=None):
         L = _capi.lib()
+        desc = self._desc(scene, bvh_leaf_max)
+        if _handle is not None:
+            self.handle = _handle
+        else:
+            h = C.c_void_p()
+            check(L.pach_scene_create(C.byref(desc), C.byref(h)))
+            self.handle = h
+        self.n_polys = self._o.size - 1
+
+    @classmethod
+    def many(cls, scenes, bvh_leaf_max: int = 0, threads: int = 0):
+        """Several scenes at once (pach_scenes_create: host builds in parallel)."""
+        L = _capi.lib()
+        holders = [cls.__new__(cls) for _ in scenes]
+        descs = (_capi.SceneDesc * max(1, len(scenes)))()
+        for i, (hd, sc) in enumerate(zip(holders, scenes)):
+            descs[i] = hd._desc(sc, bvh_leaf_max)
+        hs = (C.c_void_p * max(1, len(scenes)))()
+        check(L.pach_scenes_create(descs, len(scenes), hs, int(threads)))
+        out = []
+        for i, (hd, sc) in enumerate(zip(holders, scenes)):
+            hd.handle = C.c_void_p(hs[i])
+            hd.n_polys = hd._o.size - 1
+            out.append(hd)
+        return out
+
+    def _desc(self, scene, bvh_leaf_max):
         self._v = np.ascontiguousarray(scene.vertices, dtype=np.float64).reshape(-1)
         self._o = np.ascontiguousarray(scene.poly_offsets, dtype=np.int32)
         self._i = np.ascontiguousarray(scene.poly_indices, dtype=np.int32)
@@ -22,13 +49,9 @@ class DeviceScene:
         self._s = np.ascontiguousarray(scene.scattering, dtype=np.float64).reshape(-1)
         tr = getattr(scene, "transmission", None)
         self._t = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1) if tr is not None else None
-        desc = _capi.SceneDesc(self._v.size // 3, dptr(self._v), self._o.size - 1, iptr(self._o), iptr(self._i),
+        return _capi.SceneDesc(self._v.size // 3, dptr(self._v), self._o.size - 1, iptr(self._o), iptr(self._i),
                                dptr(self._a), dptr(self._s), dptr(self._t), scene.temp_c, scene.rel_humidity,
                                scene.pressure_hpa, scene.air_choice, scene.edge_correction, int(bvh_leaf_max), 0)
-        h = C.c_void_p()
-        check(L.pach_scene_create(C.byref(desc), C.byref(h)))
-        self.handle = h
-        self.n_polys = self._o.size - 1
 
     def info(self):
         L = _capi.lib()
@@ -290,7 +313,7 @@ TUNE_KNOBS = ("wave_kilo_items", "block_threads", "blocks_per_sm", "traversal")
 def autotune(workloads, *, dscenes=None, rays=None, sample_rays=20_000, cache_path=None, force=False, seed=1, **kw):
     """Packet size and block shape for these rooms (pach_autotune); returns a dict with the four knobs
     (TUNE_KNOBS), the measured sample throughput and whether it came from the cache."""
-    ds = dscenes or [DeviceScene(w.scene) for w in workloads]
+    ds = dscenes or DeviceScene.many([w.scene for w in workloads])
     n = [w.rays for w in workloads] if rays is None else list(rays)
     params = _batch_params(workloads, n, seed, **kw)
     src = [source_array(w.sources) for w in workloads]
@@ -314,7 +337,7 @@ def autotune(workloads, *, dscenes=None, rays=None, sample_rays=20_000, cache_pa
 def trace_batch(workloads, *, dscenes=None, seed=1, rays=None, scaled=False, tune=None, out=None, **kw):
     """Trace several rooms.Workload as one batch run; returns (per-room histograms, stats).
     tune: a dict from autotune() whose knobs are applied; out: see Run.histograms."""
-    ds = dscenes or [DeviceScene(w.scene) for w in workloads]
+    ds = dscenes or DeviceScene.many([w.scene for w in workloads])
     n = [w.rays for w in workloads] if rays is None else list(rays)
     if tune:
         for k in TUNE_KNOBS:

@@ -110,3 +110,19 @@ def test_fused_walk_traces_the_same_rays():
         hb, sb = tracer.trace(w, dscene=ds, rays=1500, seed=8, traversal=3)
         assert sa["segments"] == sb["segments"]
         assert np.allclose(ha["energy"], hb["energy"], rtol=1e-9, atol=1e-30)
+
+
+def test_scenes_built_together_equal_scenes_built_one_by_one():
+    """pach_scenes_create (parallel host builds) gives the scenes pach_scene_create gives."""
+    ws = rooms.batched_rooms_c3(max_rays=20_000)[:6]
+    many = tracer.DeviceScene.many([w.scene for w in ws], threads=4)
+    one = [tracer.DeviceScene(w.scene) for w in ws]
+    for a, b in zip(many, one):
+        ia, ib = a.info(), b.info()
+        assert ia["n_triangles"] == ib["n_triangles"]
+        np.testing.assert_array_equal(ia["poly_area"], ib["poly_area"])
+    ha, sa = tracer.trace_batch(ws, dscenes=many, rays=[200] * len(ws), seed=9)
+    hb, sb = tracer.trace_batch(ws, dscenes=one, rays=[200] * len(ws), seed=9)
+    assert sa["segments"] == sb["segments"] and sa["accel"] == sb["accel"]
+    for x, y in zip(ha, hb):
+        np.testing.assert_allclose(x["energy"], y["energy"], rtol=1e-12, atol=1e-300)
