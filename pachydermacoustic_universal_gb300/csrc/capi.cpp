@@ -455,7 +455,7 @@ void run_worker(pach_run *run) {
         if (!quant) S.bvhq = nullptr;  // trace_ray walks whichever node array is set
         const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max, quant);
         const bool fused = fused_walk(run->p.traversal, ntri_max) && run->p.ray_sort <= 0;
-        TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh));
+        TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh, fused));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
         // ring and wave sizing

@@ -295,7 +295,8 @@ cudaError_t launch_map_params(const double *etc, int n, int T, double fs, double
                               double *sum, cudaStream_t s);
 constexpr int kFuseMaxTris = 64;
 inline bool fused_walk(int traversal, int ntri) { return traversal == 3 || (traversal == 0 && ntri <= kFuseMaxTris); }
-cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade);
+cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade,
+                                  bool fused = false);
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
                          double *t, double *pts, cudaStream_t s);
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s);

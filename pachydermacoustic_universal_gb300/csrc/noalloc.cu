@@ -226,8 +226,8 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         const bool quant = use_quantised_nodes(p.bvh_format, (int)hs.tri_poly.size());
         if (!quant) r.S.bvhq = nullptr;
         const int variant = trace_variant(p.blocks_per_sm, p.traversal, (int)hs.tri_poly.size(), quant);
-        NA_TRY(wave_kernel_occupancy(variant, 256, receiver_smem_bytes(n_receivers), &bps_tr,
-                                     &bps_sh));
+        NA_TRY(wave_kernel_occupancy(variant, 256, receiver_smem_bytes(n_receivers), &bps_tr, &bps_sh,
+                                     fused_walk(p.traversal, (int)hs.tri_poly.size())));
         const int tr_blocks = sms * (bps_tr > 0 ? bps_tr : 1), sh_blocks = sms * (bps_sh > 0 ? bps_sh : 1);
         long long launches = 0;
         for (long long it = 0;;) {

@@ -490,8 +490,11 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
 
 // FUSED: walk the ray here instead of reading k_trace's hit (small scenes, whose walk is a few
 // cached nodes: the separate trace pass would only re-read the ray and round-trip its hit via HBM).
+// the shading pass alone fits three 256-thread blocks per SM (80 registers; +1.6 % on a 500k-triangle
+// arena, equal on a 20k-triangle hall); the fused walk, two (128 registers)
+constexpr int kShadeMinBlocks = 3;
 template <bool FUSED, bool MAP>
-__global__ void __launch_bounds__(256) k_shade(DevRun r) {
+__global__ void __launch_bounds__(256, FUSED ? 2 : kShadeMinBlocks) k_shade(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
     const int *s_rid;
     const float4 *s_rec = stage_receivers(r, s_rec_buf, s_rid);
@@ -755,7 +758,8 @@ cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade) {
+cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade,
+                                  bool fused) {
     cudaError_t e;
     switch (variant) {
 #define PACH_OCC(M, SP, Q)                                                                           \
@@ -767,7 +771,8 @@ cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int 
         default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false, false>, threads, 0); break;
     }
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false, false>, threads, smem_shade);
+    return fused ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<true, false>, threads, smem_shade)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false, false>, threads, smem_shade);
 }
 
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
