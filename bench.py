@@ -5,8 +5,9 @@ Default workload (one GPU): the 40 x 25 x 15 m jittered hall with 200 diffusers 
 one batch of primaries (default 131072); the timed steps together cover the 1M-ray job, each step
 tracing its own primaries (ray_begin = step * batch), the warm-up steps trace primaries after them.
 --workload shoebox: the 12-triangle 10 x 8 x 4 m shoebox; --workload arena: the 500k-triangle
-120 x 90 x 35 m arena; --workload batched: the 64-room batch (each room's ray count x --ray-scale
-per step) as one batch run with autotuned knobs.
+120 x 90 x 35 m arena; --workload hall_map: the hall with a 608-receiver audience map (1 m squares at
+1.5 m, the reference's grid walks); --workload batched: the 64-room batch (each room's ray count x
+--ray-scale per step) as one batch run with autotuned knobs.
 
 Metric: segment-bounces/s = shoot calls (broadband + octave rays, hit or miss) per second.
   value  -- device time of the engine's kernels (CUDA events on the engine's stream), scene resident.
@@ -138,6 +139,18 @@ def sum_over_ranks(dist, x, device=None):
     return float(t.item())
 
 
+def map_of(w, oracle_side=False):
+    """The workload's mapping receivers, for the engine (tracer.MapReceivers) or the oracle."""
+    m = w.extra.get("map")
+    if m is None:
+        return None
+    if oracle_side:
+        import types
+        return types.SimpleNamespace(time_1pt=False, directional=False, **m)
+    from pachydermacoustic_universal_gb300 import tracer
+    return tracer.MapReceivers(**m)
+
+
 def reference_work(ws, sample_rays, seed):
     """k_cell, k_tri: mean voxel cells stepped and polygon tests per segment of the reference
     traversal (grid domain 7) on a sample of the same rays (shared among the rooms ws)."""
@@ -146,7 +159,7 @@ def reference_work(ws, sample_rays, seed):
     tot = {}
     per = max(1, sample_rays // len(ws))
     for w in ws:
-        _, st = O.trace(w, rays=per, seed=seed, threads=0, grid_domain=7)
+        _, st = O.trace(w, rays=per, seed=seed, threads=0, grid_domain=7, map_receivers=map_of(w, True))
         for k, v in st.items():
             if isinstance(v, (int, float)):
                 tot[k] = tot.get(k, 0) + v
@@ -172,6 +185,11 @@ def workload(name, ray_scale):
         return [rooms.shoebox_c1()]
     if name == "arena":
         return [rooms.arena_c5()]
+    if name == "hall_map":
+        w = rooms.irregular_hall_c2()
+        w.extra["map"] = dict(origins=rooms.audience_plane((4.0, 3.0), (36.0, 22.0), 1.0, 1.0), increment=1.0,
+                              cutoff_ms=3000.0, walk=0)
+        return [w]
     ws = rooms.batched_rooms_c3()
     for w in ws:
         w.rays = max(100, int(round(w.rays * ray_scale)))
@@ -191,7 +209,8 @@ def run_reference_arm(args):
         t0 = time.time()
         seg = 0
         for w in rooms_:
-            _, st = O.trace(w, rays=per, ray_begin=step * per, seed=args.seed, threads=0, grid_domain=7)
+            _, st = O.trace(w, rays=per, ray_begin=step * per, seed=args.seed, threads=0, grid_domain=7,
+                            map_receivers=map_of(w, True))
             seg += st["segments"]
         dt = time.time() - t0
         if step >= args.warmup:
@@ -227,7 +246,7 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hall", choices=["hall", "shoebox", "batched", "arena"])
+    ap.add_argument("--workload", default="hall", choices=["hall", "shoebox", "batched", "arena", "hall_map"])
     ap.add_argument("--batch", type=int, default=131072, help="primaries per step (single-room workloads)")
     ap.add_argument("--ray-scale", type=float, default=0.004, help="batched: fraction of each room's rays per step")
     ap.add_argument("--seed", type=int, default=2024)
@@ -239,9 +258,9 @@ def main():
     args = ap.parse_args()
     # bounded CPU samples: the FP64 restatement's grid makes a 500k-triangle arena ~100x slower per segment
     if args.cpu_sample is None:
-        args.cpu_sample = {"hall": 3000, "shoebox": 3000, "batched": 400, "arena": 40}[args.workload]
+        args.cpu_sample = {"hall": 3000, "shoebox": 3000, "batched": 400, "arena": 40, "hall_map": 3000}[args.workload]
     if args.ref_sample is None:
-        args.ref_sample = {"hall": 200, "shoebox": 200, "batched": 200, "arena": 8}[args.workload]
+        args.ref_sample = {"hall": 200, "shoebox": 200, "batched": 200, "arena": 8, "hall_map": 200}[args.workload]
 
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -284,7 +303,11 @@ def main():
         if batched:
             h, s = tracer.trace_batch(rooms_, dscenes=ds, tune=tune, out=out, **kw)
         else:
+            mr = map_of(rooms_[0])
+            if mr is not None:
+                kw["map_receivers"] = mr
             h, s = tracer.trace(rooms_[0], dscene=ds[0], rays=B, out=out, **kw)
+            h.pop("map", None)
             h = [h]
         if e2e:
             for d in ds:
@@ -363,6 +386,12 @@ def main():
            "sources": sum(len(w.sources) for w in rooms_), "receivers": sum(len(w.receivers) for w in rooms_),
            "cutoff_s": max(w.cutoff_s for w in rooms_), "bins_ms": 1, "l2": "256 MiB buffer written between steps",
            "bvh_nodes_leaves_depth": stats[0]["accel"], "walk": stats[0]["walk"]}
+    if rooms_[0].extra.get("map") is not None:
+        m = rooms_[0].extra["map"]
+        cfg["workload"] += "_map"
+        cfg["map_receivers"] = int(len(m["origins"]))
+        cfg["map_increment_m"] = m["increment"]
+        cfg["map_walk"] = m["walk"]
     if batched:
         cfg["rooms"] = len(rooms_)
         cfg["ray_scale"] = args.ray_scale
