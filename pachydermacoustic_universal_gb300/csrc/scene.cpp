@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <future>
 #include <map>
 #include <tuple>
 
@@ -29,9 +30,15 @@ inline D3 unit(D3 a) { double l = std::sqrt(dot(a, a)); return l > 0 ? mul(a, 1.
 struct BTri { float lo[3], hi[3], c[3]; };
 struct BNode { double lo[3], hi[3]; int left = -1, right = -1, first = 0, count = 0; };
 
+// Subtrees of at least this many triangles, in the top levels, are built on their own threads (each
+// into a builder of its own, appended in left-right order: the result equals the sequential build).
+constexpr int kParallelBuildMin = 16384;
+constexpr int kParallelBuildDepth = 5;
+
 struct BvhBuilder {
-    std::vector<BTri> t;
+    std::vector<BTri> t;            // the root builder's; subtree builders read it through src
     std::vector<int> idx;
+    const BvhBuilder *src = nullptr;
     std::vector<BNode> nodes;
     std::vector<int> order;
     int max_depth = 0, leaves = 0;
@@ -42,12 +49,16 @@ struct BvhBuilder {
         return 2 * (e0 * e1 + e1 * e2 + e2 * e0);
     }
 
+    const BTri &tri(int i) const { return src ? src->t[i] : t[i]; }
+    int &id(int i) { return src ? const_cast<BvhBuilder *>(src)->idx[i] : idx[i]; }
+    int id(int i) const { return src ? src->idx[i] : idx[i]; }
+
     int make_leaf(int b, int e) {
         BNode n;
         bounds(b, e, n.lo, n.hi);
         n.first = (int)order.size();
         n.count = e - b;
-        for (int i = b; i < e; ++i) order.push_back(idx[i]);
+        for (int i = b; i < e; ++i) order.push_back(id(i));
         nodes.push_back(n);
         ++leaves;
         return (int)nodes.size() - 1;
@@ -56,7 +67,21 @@ struct BvhBuilder {
     void bounds(int b, int e, double lo[3], double hi[3]) const {
         for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
         for (int i = b; i < e; ++i)
-            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], (double)t[idx[i]].lo[k]); hi[k] = std::max(hi[k], (double)t[idx[i]].hi[k]); }
+            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], (double)tri(id(i)).lo[k]); hi[k] = std::max(hi[k], (double)tri(id(i)).hi[k]); }
+    }
+
+    // appends a subtree builder's nodes and leaf order; returns its root's index here
+    int append(const BvhBuilder &s, int root) {
+        const int noff = (int)nodes.size(), ooff = (int)order.size();
+        for (BNode n : s.nodes) {
+            if (n.left >= 0) { n.left += noff; n.right += noff; }
+            else n.first += ooff;
+            nodes.push_back(n);
+        }
+        order.insert(order.end(), s.order.begin(), s.order.end());
+        leaves += s.leaves;
+        max_depth = std::max(max_depth, s.max_depth);
+        return root + noff;
     }
 
     int build(int b, int e, int depth) {
@@ -67,7 +92,7 @@ struct BvhBuilder {
         }
         double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
         for (int i = b; i < e; ++i)
-            for (int k = 0; k < 3; ++k) { clo[k] = std::min(clo[k], (double)t[idx[i]].c[k]); chi[k] = std::max(chi[k], (double)t[idx[i]].c[k]); }
+            for (int k = 0; k < 3; ++k) { clo[k] = std::min(clo[k], (double)tri(id(i)).c[k]); chi[k] = std::max(chi[k], (double)tri(id(i)).c[k]); }
         double nlo[3], nhi[3];
         bounds(b, e, nlo, nhi);
         const double parea = area(nlo, nhi);
@@ -82,7 +107,7 @@ struct BvhBuilder {
             for (int q = 0; q < NB; ++q)
                 for (int k = 0; k < 3; ++k) { blo[q][k] = 1e300; bhi[q][k] = -1e300; }
             for (int i = b; i < e; ++i) {
-                const BTri &x = t[idx[i]];
+                const BTri &x = tri(id(i));
                 int q = std::min(NB - 1, (int)((x.c[ax] - clo[ax]) / ext * NB));
                 ++cnt[q];
                 for (int k = 0; k < 3; ++k) { blo[q][k] = std::min(blo[q][k], (double)x.lo[k]); bhi[q][k] = std::max(bhi[q][k], (double)x.hi[k]); }
@@ -113,17 +138,32 @@ struct BvhBuilder {
             mid = b + n / 2;  // coincident centroids: split the list
         } else {
             const double ext = chi[best_axis] - clo[best_axis];
-            auto it = std::partition(idx.begin() + b, idx.begin() + e, [&](int i) {
-                int q = std::min(NB - 1, (int)((t[i].c[best_axis] - clo[best_axis]) / ext * NB));
+            std::vector<int> &ix = src ? const_cast<BvhBuilder *>(src)->idx : idx;
+            auto it = std::partition(ix.begin() + b, ix.begin() + e, [&](int i) {
+                int q = std::min(NB - 1, (int)((tri(i).c[best_axis] - clo[best_axis]) / ext * NB));
                 return q <= best_split;
             });
-            mid = (int)(it - idx.begin());
+            mid = (int)(it - ix.begin());
             if (mid == b || mid == e) mid = b + n / 2;
         }
         BNode node;
         for (int k = 0; k < 3; ++k) { node.lo[k] = nlo[k]; node.hi[k] = nhi[k]; }
         nodes.push_back(node);
         const int me = (int)nodes.size() - 1;
+        if (n >= kParallelBuildMin && depth < kParallelBuildDepth) {
+            // both halves on their own builders (disjoint ranges of the shared index array)
+            BvhBuilder L, R;
+            L.src = R.src = src ? src : this;
+            L.leaf_max = R.leaf_max = leaf_max;
+            auto fl = std::async(std::launch::async, [&] { return L.build(b, mid, depth + 1); });
+            const int rr = R.build(mid, e, depth + 1);
+            const int lr = fl.get();
+            const int l = append(L, lr);
+            const int r = append(R, rr);
+            nodes[me].left = l;
+            nodes[me].right = r;
+            return me;
+        }
         const int l = build(b, mid, depth + 1);
         const int r = build(mid, e, depth + 1);
         nodes[me].left = l;
@@ -246,10 +286,29 @@ void build_bvh(HostScene &hs, int leaf_max) {
 //   uint4  (lo.x of children 0-3 as bytes, hi.x, lo.y, hi.y)
 //   uint4  (lo.z, hi.z, 0, 0)
 //   int4   child codes (as the 128-byte nodes)
+static void quantize_nodes(HostScene &hs, size_t q0, size_t q1);
+
 void quantize_bvh(HostScene &hs) {
     const size_t nodes = hs.bvh.size() / kBvhNodeFloats;
     hs.bvhq.assign(nodes * kBvhQNodeFloats, 0.f);
-    for (size_t q = 0; q < nodes; ++q) {
+    // nodes are independent: large trees are quantised in chunks on several threads
+    const size_t chunk = 8192;
+    const size_t nchunks = (nodes + chunk - 1) / chunk;
+    if (nchunks > 1) {
+        std::vector<std::future<void>> parts;
+        for (size_t c = 0; c < nchunks; ++c)
+            parts.push_back(std::async(std::launch::async, [&hs, c, chunk, nodes] {
+                quantize_nodes(hs, c * chunk, std::min(nodes, (c + 1) * chunk));
+            }));
+        for (auto &p : parts) p.get();
+    } else {
+        quantize_nodes(hs, 0, nodes);
+    }
+}
+
+// Quantised copy of nodes [q0, q1) (see quantize_bvh).
+static void quantize_nodes(HostScene &hs, size_t q0, size_t q1) {
+    for (size_t q = q0; q < q1; ++q) {
         const float *f = &hs.bvh[q * kBvhNodeFloats];
         int code[4];
         for (int k = 0; k < 4; ++k) std::memcpy(&code[k], &f[24 + k], 4);
@@ -585,18 +644,36 @@ bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err)
     for (int k = 0; k < 3; ++k) { hs.bmin[k] -= pad; hs.bmax[k] += pad; ext[k] = hs.bmax[k] - hs.bmin[k]; }
 
     // Coplanar groups: quantised (canonical normal, offset) of each triangle's own plane.
-    std::map<std::tuple<long long, long long, long long, long long>, int> planes;
+    // (flat open-addressing table; ids in order of first appearance)
+    struct PlaneKey {
+        long long v[4];
+        bool operator==(const PlaneKey &o) const { return v[0] == o.v[0] && v[1] == o.v[1] && v[2] == o.v[2] && v[3] == o.v[3]; }
+    };
+    auto hash = [](const PlaneKey &k) {
+        uint64_t h = 0x9E3779B97F4A7C15ull;
+        for (long long x : k.v) h = (h ^ (uint64_t)x) * 0xBF58476D1CE4E5B9ull + (h >> 29);
+        return h ^ (h >> 31);
+    };
+    size_t cap = 16;
+    while (cap < 2 * (size_t)hs.ntri) cap <<= 1;
+    std::vector<PlaneKey> slot_key(cap);
+    std::vector<int> slot_id(cap, -1);
+    int n_planes = 0;
     hs.tri_plane.resize(hs.ntri);
     for (int i = 0; i < hs.ntri; ++i) {
         const double *t = &hs.tri64[9 * (size_t)i];
         D3 n = unit(cross(D3{t[3], t[4], t[5]}, D3{t[6], t[7], t[8]}));
         if (n.x < 0 || (n.x == 0 && (n.y < 0 || (n.y == 0 && n.z < 0)))) n = mul(n, -1);
         double off = dot(n, D3{t[0], t[1], t[2]}) / hs.scale;
-        auto key = std::make_tuple(std::llround(n.x * 1e6), std::llround(n.y * 1e6), std::llround(n.z * 1e6),
-                                   std::llround(off * 1e6));
-        auto it = planes.find(key);
-        if (it == planes.end()) it = planes.emplace(key, (int)planes.size()).first;
-        hs.tri_plane[i] = it->second;
+        const PlaneKey key{{std::llround(n.x * 1e6), std::llround(n.y * 1e6), std::llround(n.z * 1e6),
+                            std::llround(off * 1e6)}};
+        size_t h = (size_t)hash(key) & (cap - 1);
+        while (slot_id[h] >= 0 && !(slot_key[h] == key)) h = (h + 1) & (cap - 1);
+        if (slot_id[h] < 0) {
+            slot_key[h] = key;
+            slot_id[h] = n_planes++;
+        }
+        hs.tri_plane[i] = slot_id[h];
     }
 
     build_bvh(hs, d->bvh_leaf_max);
