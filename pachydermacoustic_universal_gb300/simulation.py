@@ -467,6 +467,30 @@ class AcousticalMath:
         return _capi.lib().pach_math_sound_speed(float(Air_Temp))
 
     @staticmethod
+    def Sabine(Room, volume):
+        """Sabine reverberation time per octave band (Classes_Math.cs:212-228): T60 = 0.161 V /
+        (sum S alpha + 4 m V), with m the scene's air attenuation as the reference takes it
+        (Room.Attenuation(0), dB/m)."""
+        m = Room.Attenuation(0)
+        T60 = np.zeros(8)
+        for t in range(8):
+            TA = sum(Room.SurfaceArea(q) * Room.AbsorptionValue[q].Coefficient_A_Broad(t) for q in range(Room.Count()))
+            T60[t] = 0.161 * (volume / (TA + 4 * m[t] * volume))
+        return T60
+
+    @staticmethod
+    def Eyring(Room, volume):
+        """The reference's Eyring time (Classes_Math.cs:246-263): T60 = 0.161 V / (sum S (-ln(1 - alpha))
+        + 4 m V), the logarithm taken per surface."""
+        m = Room.Attenuation(0)
+        T60 = np.zeros(8)
+        for t in range(8):
+            TA = sum(Room.SurfaceArea(q) * -np.log(1 - Room.AbsorptionValue[q].Coefficient_A_Broad(t))
+                     for q in range(Room.Count()))
+            T60[t] = 0.161 * volume / (TA + 4 * m[t] * volume)
+        return T60
+
+    @staticmethod
     def Schroeder_Integral(etc):
         e = np.ascontiguousarray(etc, dtype=np.float64)
         out = np.zeros_like(e)
