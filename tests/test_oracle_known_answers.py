@@ -296,3 +296,38 @@ def test_diffuse_box_decay_lies_near_sabine_and_eyring():
     for band in (1, 2, 3, 4):
         t30 = np.mean([O.t_x(O.schroeder(h["energy"][r, band]), 30, 1000) for r in range(3)])
         assert abs(t30 / ey[band] - 1) < 0.25, (band, t30, ey[band], sa[band])
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_device():
+    """Argument checks of the map, multi-scene, curve-parameter and air entry points run before any
+    device work, so they answer the same on a machine without a GPU."""
+    import ctypes as C
+    L = _capi.lib()
+    a = np.zeros(23)
+    assert L.pach_medium_attenuation_third_octave(20.0, 0.0, 1013.25, 0, 0, _capi.dptr(a), None) == 1
+    assert L.pach_medium_attenuation_third_octave(20.0, 50.0, 1013.25, 3, 0, _capi.dptr(a), None) == 1
+    etc = np.ones((2, 10))
+    out = np.zeros(2)
+    assert L.pach_etc_parameters(_capi.dptr(etc), -1, 10, 1000, 30, 0.08, _capi.dptr(out), None, None, None, None) == 1
+    assert L.pach_etc_parameters(_capi.dptr(etc), 2, 0, 1000, 30, 0.08, _capi.dptr(out), None, None, None, None) == 1
+    assert L.pach_etc_parameters(None, 2, 10, 1000, 30, 0.08, _capi.dptr(out), None, None, None, None) == 1
+    assert L.pach_etc_parameters(None, 0, 10, 1000, 30, 0.08, None, None, None, None, None) == 0
+    assert L.pach_trace_get_map(None, 0, None, None, None, None, 0) == 1
+    assert L.pach_map_parameters(None, 30, 80, None, None, None, None, None) == 1
+    assert L.pach_trace_get_map_directions(None, 0, None, None, 0) == 1
+    hs = (C.c_void_p * 2)()
+    assert L.pach_scenes_create(None, -1, hs, 0) == 1
+    w = rooms.shoebox_c1()
+    v = np.ascontiguousarray(w.scene.vertices).reshape(-1)
+    o, i = w.scene.poly_offsets, w.scene.poly_indices
+    ab, sc = w.scene.absorption.reshape(-1), w.scene.scattering.reshape(-1)
+    descs = (_capi.SceneDesc * 2)()
+    for k in range(2):
+        descs[k] = _capi.SceneDesc(v.size // 3, _capi.dptr(v), o.size - 1, _capi.iptr(o), _capi.iptr(i), _capi.dptr(ab),
+                                   _capi.dptr(sc), None, 20.0, 50.0, 1013.25, 0, 0, 0, 0)
+    descs[1].pressure_hpa = -1.0
+    assert L.pach_scenes_create(descs, 2, hs, 0) == 1 and "scene 1" in _capi.last_error()
+    if _capi.device_count() == 0:
+        descs[1].pressure_hpa = 1013.25
+        assert L.pach_scenes_create(descs, 2, hs, 0) == 8     # PACH_ERR_NO_DEVICE: no CPU fallback
+        assert not hs[0] and not hs[1]
