@@ -109,8 +109,9 @@ typedef struct {
     int64_t feed_batch;            /* primaries handed to the device per phase-A launch (0 = default) */
     int32_t block_threads;         /* threads per block of the trace and shade kernels; 0 = default */
     int32_t blocks_per_sm;         /* resident blocks per SM to launch; 0 = occupancy maximum */
-    int32_t wave_kilo_items;       /* octave rays per wave, in units of 1024; 0 = default */
-    int32_t ring_log2;             /* ring queue capacity 2^ring_log2 octave rays; 0 = default */
+    int32_t wave_kilo_items;       /* octave rays per wave, in units of 1024; 0 = default (8192) */
+    int32_t ring_log2;             /* ring queue capacity 2^ring_log2 octave rays; 0 = default (2^22..2^28 by
+                                      the run's primaries, 2048 rays each) */
     int32_t kernel_timing;         /* 1: CUDA events around every kernel (per-kernel times in pach_stats) */
     int32_t ray_sort;              /* 1: order each wave by (direction octant, origin cell) before tracing;
                                       0 = default (off: measured +6 % walk rate in the 20k-triangle

@@ -138,7 +138,7 @@ extern "C" pach_status pach_autotune(const pach_room_desc *rooms, int32_t n_room
         d.ray_count = std::max<int64_t>(1, (int64_t)std::llround((double)std::max<int64_t>(1, d.ray_count) * sample_rays / total));
     const auto t0 = std::chrono::steady_clock::now();
     int trials = 0;
-    Knobs cur{2048, 256, 4, 0};
+    Knobs cur{8192, 256, 6, 0};
     if (time_sample(sample, *params, cur) < 0) {  // warm-up (and a check that the sample runs at all)
         return PACH_ERR_INVALID_ARGUMENT;
     }
@@ -156,7 +156,7 @@ extern "C" pach_status pach_autotune(const pach_room_desc *rooms, int32_t n_room
         for (int bps : {4, 6}) consider(Knobs{cur.wave_kilo, cur.threads, bps, trav});
     consider(Knobs{cur.wave_kilo, cur.threads, 4, 3});  // the walk inside the shading kernel
     const Knobs stage1 = best;
-    for (int w : {512, 1024, 4096}) consider(Knobs{w, stage1.threads, stage1.bps, stage1.traversal});
+    for (int w : {2048, 4096, 16384}) consider(Knobs{w, stage1.threads, stage1.bps, stage1.traversal});
     const Knobs stage2 = best;
     consider(Knobs{stage2.wave_kilo, 128, stage2.bps, stage2.traversal});
     if (best_rate <= 0) {

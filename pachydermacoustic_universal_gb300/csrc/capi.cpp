@@ -459,9 +459,14 @@ void run_worker(pach_run *run) {
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
         // ring and wave sizing
-        const int ring_log2 = run->p.ring_log2 > 0 ? std::min(32, std::max(16, run->p.ring_log2)) : 27;
+        // default ring: room for the run's rays at up to 2048 live octave rays per primary, 2^22..2^28
+        // (17 GB); default wave 8M rays -- measured against 2M: +7 % on a 20k-triangle hall and a
+        // 500k-triangle arena, +19 % on a 12-triangle shoebox (fewer, fuller iterations)
+        int ring_default = 22;
+        while (ring_default < 28 && (1ull << ring_default) < (unsigned long long)rprim_total(run) * 2048ull) ++ring_default;
+        const int ring_log2 = run->p.ring_log2 > 0 ? std::min(32, std::max(16, run->p.ring_log2)) : ring_default;
         const unsigned long long ring_cap = 1ull << ring_log2;
-        const unsigned long long max_wave = run->p.wave_kilo_items > 0 ? 1024ull * run->p.wave_kilo_items : (1ull << 21);
+        const unsigned long long max_wave = run->p.wave_kilo_items > 0 ? 1024ull * run->p.wave_kilo_items : (1ull << 23);
         if (bound * 4 > ring_cap) {
             status = PACH_ERR_BOUNDS;
             msg = "the ring queue (2^" + std::to_string(ring_log2) + " rays) cannot hold the phase-A output of one "

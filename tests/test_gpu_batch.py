@@ -77,7 +77,7 @@ def test_autotune_picks_and_caches(tmp_path):
     cache = str(tmp_path / "tune.txt")
     t1 = tracer.autotune(ws, dscenes=ds, rays=[2000, 2000], sample_rays=600, cache_path=cache)
     assert t1["from_cache"] == 0 and t1["trials"] >= 5 and t1["segments_per_s"] > 0
-    assert t1["wave_kilo_items"] in (512, 1024, 2048, 4096) and t1["block_threads"] in (128, 256)
+    assert t1["wave_kilo_items"] in (2048, 4096, 8192, 16384) and t1["block_threads"] in (128, 256)
     assert t1["blocks_per_sm"] in (4, 6) and t1["traversal"] in (1, 2, 3)
     t2 = tracer.autotune(ws, dscenes=ds, rays=[2000, 2000], sample_rays=600, cache_path=cache)
     assert t2["from_cache"] == 1
