@@ -135,51 +135,21 @@ cudaError_t upload(DevMem &m, const void *src, size_t bytes) {
 // normals, materials, transmission and the 4-wide BVH.  A batch run appends several scenes into one
 // set of arrays: triangle, polygon, plane and node ids are offset, and each scene's root is kept.
 struct SceneArrays {
-    std::vector<float4> tri, norm, mat;
-    std::vector<float> trans, bvh, bvhq;
-    std::vector<double> tri64;
+    hvec<float4> tri, norm, mat;
+    hvec<float> trans, bvh, bvhq;
+    hvec<double> tri64;
     int planes = 0;
     float t_eps = 0.f;
     bool has_trans = false;
 };
 
-int append_scene(const HostScene &hs, SceneArrays &A) {
-    const int tri_off = (int)(A.tri.size() / 3), poly_off = (int)A.norm.size(), plane_off = A.planes;
-    const int node_off = (int)(A.bvh.size() / kBvhNodeFloats);
-    int max_plane = -1;
-    for (int i = 0; i < hs.ntri; ++i) {
-        const double *t = &hs.tri64[9 * (size_t)i];
-        const double ax = t[4] * t[8] - t[5] * t[7], ay = t[5] * t[6] - t[3] * t[8], az = t[3] * t[7] - t[4] * t[6];
-        const double graze = 1e-4 * std::sqrt(ax * ax + ay * ay + az * az);  // |det| < 1e-4 |e1 x e2|: near grazing
-        int plane = hs.tri_plane[i] + plane_off, poly = hs.tri_poly[i] + poly_off;
-        max_plane = std::max(max_plane, hs.tri_plane[i]);
-        float pw, qw;
-        std::memcpy(&pw, &plane, 4);
-        std::memcpy(&qw, &poly, 4);
-        A.tri.push_back(make_float4((float)t[0], (float)t[1], (float)t[2], pw));
-        A.tri.push_back(make_float4((float)t[3], (float)t[4], (float)t[5], qw));
-        A.tri.push_back(make_float4((float)t[6], (float)t[7], (float)t[8], (float)graze));
-    }
-    A.planes = plane_off + max_plane + 1;
-    A.tri64.insert(A.tri64.end(), hs.tri64.begin(), hs.tri64.end());
-    for (int p = 0; p < hs.npoly; ++p) {
-        A.norm.push_back(make_float4((float)hs.normal[3 * p], (float)hs.normal[3 * p + 1], (float)hs.normal[3 * p + 2], 0.f));
-        for (int o = 0; o < kBands; ++o) {
-            // Lambert_Scattering thresholds (Classes_Materials.cs:4466-4485)
-            const double s = hs.scat[p * 8 + o];
-            double lo, hi;
-            if (s < 0.25) { lo = 0.1; hi = 0.4; }
-            else { const double mod = std::fabs(1 - s) / 5; lo = s - mod; hi = s + mod; }
-            A.mat.push_back(make_float4((float)(1.0 - hs.alpha[p * 8 + o]), (float)lo, (float)s, (float)hi));
-            A.trans.push_back((float)hs.trans[p * 8 + o]);
-        }
-    }
-    const size_t b0 = A.bvh.size();
-    A.bvh.insert(A.bvh.end(), hs.bvh.begin(), hs.bvh.end());
-    if (tri_off || node_off)
-        for (size_t q = 0; q < hs.bvh.size() / kBvhNodeFloats; ++q)
+// Rebases one node array's child codes by node and triangle offsets (codes at `code_at` in each node
+// of `stride` floats).
+static void rebase_codes(float *nodes, size_t count, int stride, int code_at, int node_off, int tri_off) {
+    parallel_chunks(count, 16384, [=](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q)
             for (int k = 0; k < 4; ++k) {
-                float *f = &A.bvh[b0 + q * kBvhNodeFloats + 24 + k];
+                float *f = nodes + q * stride + code_at + k;
                 int code;
                 std::memcpy(&code, f, 4);
                 if (code == (int)0x80000000) continue;       // empty slot
@@ -190,22 +160,64 @@ int append_scene(const HostScene &hs, SceneArrays &A) {
                 }
                 std::memcpy(f, &code, 4);
             }
+    });
+}
+
+int append_scene(const HostScene &hs, SceneArrays &A) {
+    const int tri_off = (int)(A.tri.size() / 3), poly_off = (int)A.norm.size(), plane_off = A.planes;
+    const int node_off = (int)(A.bvh.size() / kBvhNodeFloats);
+    const size_t t0 = A.tri.size(), d0 = A.tri64.size(), n0 = A.norm.size(), m0 = A.mat.size();
+    A.tri.resize(t0 + 3 * (size_t)hs.ntri);
+    A.tri64.resize(d0 + 9 * (size_t)hs.ntri);
+    A.norm.resize(n0 + (size_t)hs.npoly);
+    A.mat.resize(m0 + (size_t)kBands * hs.npoly);
+    A.trans.resize(m0 + (size_t)kBands * hs.npoly);
+    constexpr size_t kGrain = 65536;
+    std::vector<int> chunk_plane(((size_t)hs.ntri + kGrain - 1) / kGrain, -1);
+    parallel_chunks((size_t)hs.ntri, kGrain, [&](size_t i0, size_t i1) {
+        int mp = -1;
+        for (size_t i = i0; i < i1; ++i) {
+            const double *t = &hs.tri64[9 * i];
+            const double ax = t[4] * t[8] - t[5] * t[7], ay = t[5] * t[6] - t[3] * t[8], az = t[3] * t[7] - t[4] * t[6];
+            const double graze = 1e-4 * std::sqrt(ax * ax + ay * ay + az * az);  // |det| < 1e-4 |e1 x e2|: near grazing
+            int plane = hs.tri_plane[i] + plane_off, poly = hs.tri_poly[i] + poly_off;
+            mp = std::max(mp, (int)hs.tri_plane[i]);
+            float pw, qw;
+            std::memcpy(&pw, &plane, 4);
+            std::memcpy(&qw, &poly, 4);
+            float4 *o = &A.tri[t0 + 3 * i];
+            o[0] = make_float4((float)t[0], (float)t[1], (float)t[2], pw);
+            o[1] = make_float4((float)t[3], (float)t[4], (float)t[5], qw);
+            o[2] = make_float4((float)t[6], (float)t[7], (float)t[8], (float)graze);
+            std::copy(t, t + 9, &A.tri64[d0 + 9 * i]);
+        }
+        chunk_plane[i0 / kGrain] = mp;
+    });
+    int max_plane = -1;
+    for (int m : chunk_plane) max_plane = std::max(max_plane, m);
+    A.planes = plane_off + max_plane + 1;
+    parallel_chunks((size_t)hs.npoly, 16384, [&](size_t p0, size_t p1) {
+        for (size_t p = p0; p < p1; ++p) {
+            A.norm[n0 + p] = make_float4((float)hs.normal[3 * p], (float)hs.normal[3 * p + 1], (float)hs.normal[3 * p + 2], 0.f);
+            for (int o = 0; o < kBands; ++o) {
+                // Lambert_Scattering thresholds (Classes_Materials.cs:4466-4485)
+                const double s = hs.scat[p * 8 + o];
+                double lo, hi;
+                if (s < 0.25) { lo = 0.1; hi = 0.4; }
+                else { const double mod = std::fabs(1 - s) / 5; lo = s - mod; hi = s + mod; }
+                A.mat[m0 + p * kBands + o] = make_float4((float)(1.0 - hs.alpha[p * 8 + o]), (float)lo, (float)s, (float)hi);
+                A.trans[m0 + p * kBands + o] = (float)hs.trans[p * 8 + o];
+            }
+        }
+    });
+    const size_t b0 = A.bvh.size();
+    A.bvh.insert(A.bvh.end(), hs.bvh.begin(), hs.bvh.end());
     const size_t q0 = A.bvhq.size();
     A.bvhq.insert(A.bvhq.end(), hs.bvhq.begin(), hs.bvhq.end());
-    if (tri_off || node_off)
-        for (size_t q = 0; q < hs.bvhq.size() / kBvhQNodeFloats; ++q)
-            for (int k = 0; k < 4; ++k) {
-                float *f = &A.bvhq[q0 + q * kBvhQNodeFloats + 12 + k];
-                int code;
-                std::memcpy(&code, f, 4);
-                if (code == (int)0x80000000) continue;
-                if (code >= 0) code += node_off;
-                else {
-                    const int c = ~code;
-                    code = ~(((c >> 4) + tri_off) * 16 + (c & 15));
-                }
-                std::memcpy(f, &code, 4);
-            }
+    if (tri_off || node_off) {
+        rebase_codes(&A.bvh[b0], hs.bvh.size() / kBvhNodeFloats, kBvhNodeFloats, 24, node_off, tri_off);
+        rebase_codes(&A.bvhq[q0], hs.bvhq.size() / kBvhQNodeFloats, kBvhQNodeFloats, 12, node_off, tri_off);
+    }
     A.t_eps = std::max(A.t_eps, (float)(2e-7 * hs.scale));
     A.has_trans = A.has_trans || hs.has_trans;
     return node_off;

@@ -1,8 +1,14 @@
 // engine.h -- internal structures shared by the host side (scene build, C ABI) and the kernels.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <future>
+#include <memory>
+#include <new>
 #include <string>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -16,23 +22,60 @@ constexpr int kBands = 8;
 constexpr int kMaxSources = 64;
 constexpr int kGeoFaces = 80;
 
+// Allocator whose resize() leaves elements default-initialised (no zero fill): the large host arrays
+// of a scene are sized first and then filled by parallel chunks, which also spreads the first-touch
+// page faults over the threads.
+template <class T>
+struct UninitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind { using other = UninitAlloc<U>; };
+    UninitAlloc() = default;
+    template <class U>
+    UninitAlloc(const UninitAlloc<U> &) noexcept {}
+    template <class U>
+    void construct(U *p) noexcept { ::new ((void *)p) U; }
+    template <class U, class... A>
+    void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+template <class T>
+using hvec = std::vector<T, UninitAlloc<T>>;
+
+// Runs f(c0, c1) over [0, n) in chunks of `grain` elements on up to hardware_concurrency() threads;
+// inline when one chunk covers the range.  Chunk c is [c * grain, min(n, (c + 1) * grain)).
+template <class F>
+void parallel_chunks(size_t n, size_t grain, F &&f) {
+    const size_t nch = (n + grain - 1) / grain;
+    if (nch <= 1) {
+        if (n) f((size_t)0, n);
+        return;
+    }
+    const size_t nt = std::min(nch, (size_t)std::max(1u, std::thread::hardware_concurrency()));
+    auto run = [&](size_t t) {
+        for (size_t c = t; c < nch; c += nt) f(c * grain, std::min(n, (c + 1) * grain));
+    };
+    std::vector<std::future<void>> parts;
+    for (size_t t = 1; t < nt; ++t) parts.push_back(std::async(std::launch::async, run, t));
+    run(0);
+    for (auto &p : parts) p.get();
+}
+
 // Host-side prepared scene (FP64 master copy + FP32 device layout sources).
 struct HostScene {
     int npoly = 0, ntri = 0;
-    std::vector<double> tri64;       // [ntri][9]: v0, e1, e2
-    std::vector<int32_t> tri_poly;   // [ntri]
-    std::vector<int32_t> tri_plane;  // [ntri] coplanar group id
-    std::vector<double> normal;      // [npoly][3]
-    std::vector<double> area;        // [npoly]
-    std::vector<double> alpha, scat, trans;  // [npoly][8]
+    hvec<double> tri64;              // [ntri][9]: v0, e1, e2
+    hvec<int32_t> tri_poly;          // [ntri]
+    hvec<int32_t> tri_plane;         // [ntri] coplanar group id
+    hvec<double> normal;             // [npoly][3]
+    hvec<double> area;               // [npoly]
+    hvec<double> alpha, scat, trans;  // [npoly][8]
     bool has_trans = false;
     double bmin[3], bmax[3];
     // BVH: 4-wide, collapsed from an SAH binary tree; triangles above are stored in leaf order.
     // node n = 8 float4 (128 B): lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4], child[4] (int
     // bits), unused; a child >= 0 is an inner node, < 0 the leaf ~(first * 16 + count - 1); an
     // empty slot has an inverted box.
-    std::vector<float> bvh;          // [nodes*32]
-    std::vector<float> bvhq;         // [nodes*16]: the same tree with 8-bit child boxes (64-byte nodes)
+    hvec<float> bvh;                 // [nodes*32]
+    hvec<float> bvhq;                // [nodes*16]: the same tree with 8-bit child boxes (64-byte nodes)
     int bvh_nodes = 0, bvh_leaves = 0, bvh_depth = 0;
     double c = 343, rho = 1.2, rho_c = 411.6, atten[kBands] = {0};
     double scale = 1;                // largest box extent

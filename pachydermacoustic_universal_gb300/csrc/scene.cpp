@@ -7,10 +7,12 @@
 // Voxel_Grid as the nearest-hit structure (any structure that returns the nearest hit with t > eps
 // gives the same answer).  Air properties follow Uniform_Medium (Classes_Medium_Props.cs:286-299).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <future>
 #include <map>
+#include <thread>
 #include <tuple>
 
 #include "engine.h"
@@ -27,18 +29,115 @@ inline D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b
 inline D3 unit(D3 a) { double l = std::sqrt(dot(a, a)); return l > 0 ? mul(a, 1.0 / l) : a; }
 
 // ---- BVH: binned SAH (16 bins, 3 axes), leaves of at most kLeafMax triangles ----
-struct BTri { float lo[3], hi[3], c[3]; };
+// The builder partitions an array of triangle references (box, centroid, triangle id) in place, so
+// every pass over a node's range streams through contiguous memory.
+struct BRef { float lo[3], hi[3], c[3]; int id; };
 struct BNode { double lo[3], hi[3]; int left = -1, right = -1, first = 0, count = 0; };
 
 // Subtrees of at least this many triangles, in the top levels, are built on their own threads (each
 // into a builder of its own, appended in left-right order: the result equals the sequential build).
 constexpr int kParallelBuildMin = 16384;
 constexpr int kParallelBuildDepth = 5;
+// Ranges of at least this many triangles are boxed and binned in parallel chunks.
+constexpr int kParallelBinMin = 131072;
+constexpr int kBins = 16;
+
+// Node box and centroid box of a range (float min/max: exact in any order).
+struct RangeBoxes {
+    float lo[3], hi[3], clo[3], chi[3];
+    void clear() {
+        for (int k = 0; k < 3; ++k) { lo[k] = clo[k] = INFINITY; hi[k] = chi[k] = -INFINITY; }
+    }
+    void add(const RangeBoxes &o) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], o.lo[k]); hi[k] = std::max(hi[k], o.hi[k]);
+            clo[k] = std::min(clo[k], o.clo[k]); chi[k] = std::max(chi[k], o.chi[k]);
+        }
+    }
+};
+
+// Per axis and bin: triangle count and the union of the triangles' boxes.
+struct Bins {
+    int cnt[3][kBins];
+    float lo[3][kBins][3], hi[3][kBins][3];
+    void clear() {
+        for (int a = 0; a < 3; ++a)
+            for (int q = 0; q < kBins; ++q) {
+                cnt[a][q] = 0;
+                for (int k = 0; k < 3; ++k) { lo[a][q][k] = INFINITY; hi[a][q][k] = -INFINITY; }
+            }
+    }
+    void add(const Bins &o) {
+        for (int a = 0; a < 3; ++a)
+            for (int q = 0; q < kBins; ++q) {
+                cnt[a][q] += o.cnt[a][q];
+                for (int k = 0; k < 3; ++k) {
+                    lo[a][q][k] = std::min(lo[a][q][k], o.lo[a][q][k]);
+                    hi[a][q][k] = std::max(hi[a][q][k], o.hi[a][q][k]);
+                }
+            }
+    }
+};
+
+inline int bin_of(float c, double clo, double ext) {
+    return std::min(kBins - 1, (int)(((double)c - clo) / ext * kBins));
+}
+
+void range_boxes(const BRef *r, int b, int e, RangeBoxes &out) {
+    out.clear();
+    for (int i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k) {
+            out.lo[k] = std::min(out.lo[k], r[i].lo[k]); out.hi[k] = std::max(out.hi[k], r[i].hi[k]);
+            out.clo[k] = std::min(out.clo[k], r[i].c[k]); out.chi[k] = std::max(out.chi[k], r[i].c[k]);
+        }
+}
+
+// Bins [b, e) along every axis with a positive centroid extent, in one sweep.
+void range_bins(const BRef *r, int b, int e, const double clo[3], const double ext[3], Bins &out) {
+    out.clear();
+    bool live[3];
+    for (int a = 0; a < 3; ++a) live[a] = ext[a] > 0;
+    for (int i = b; i < e; ++i) {
+        const BRef &x = r[i];
+        for (int a = 0; a < 3; ++a) {
+            if (!live[a]) continue;
+            const int q = bin_of(x.c[a], clo[a], ext[a]);
+            ++out.cnt[a][q];
+            for (int k = 0; k < 3; ++k) {
+                out.lo[a][q][k] = std::min(out.lo[a][q][k], x.lo[k]);
+                out.hi[a][q][k] = std::max(out.hi[a][q][k], x.hi[k]);
+            }
+        }
+    }
+}
+
+// f over [b, e) split into chunks run in parallel, merged with T::add (exact: min/max and counts).
+template <class T, class F>
+void reduce_range(int b, int e, T &out, F &&f) {
+    const int n = e - b;
+    if (n < kParallelBinMin) {
+        f(b, e, out);
+        return;
+    }
+    const int nt = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+    const int step = (n + nt - 1) / nt;
+    std::vector<T> part((size_t)nt);
+    std::vector<std::future<void>> fut;
+    for (int t = 1; t < nt; ++t) {
+        const int c0 = b + t * step, c1 = std::min(e, c0 + step);
+        fut.push_back(std::async(std::launch::async, [&, t, c0, c1] {
+            if (c0 < c1) f(c0, c1, part[(size_t)t]);
+            else part[(size_t)t].clear();
+        }));
+    }
+    f(b, std::min(e, b + step), part[0]);
+    for (auto &x : fut) x.get();
+    out = part[0];
+    for (int t = 1; t < nt; ++t) out.add(part[(size_t)t]);
+}
 
 struct BvhBuilder {
-    std::vector<BTri> t;            // the root builder's; subtree builders read it through src
-    std::vector<int> idx;
-    const BvhBuilder *src = nullptr;
+    BRef *r = nullptr;              // shared by every builder of one tree (disjoint ranges)
     std::vector<BNode> nodes;
     std::vector<int> order;
     int max_depth = 0, leaves = 0;
@@ -49,25 +148,15 @@ struct BvhBuilder {
         return 2 * (e0 * e1 + e1 * e2 + e2 * e0);
     }
 
-    const BTri &tri(int i) const { return src ? src->t[i] : t[i]; }
-    int &id(int i) { return src ? const_cast<BvhBuilder *>(src)->idx[i] : idx[i]; }
-    int id(int i) const { return src ? src->idx[i] : idx[i]; }
-
-    int make_leaf(int b, int e) {
+    int make_leaf(int b, int e, const RangeBoxes &bx) {
         BNode n;
-        bounds(b, e, n.lo, n.hi);
+        for (int k = 0; k < 3; ++k) { n.lo[k] = bx.lo[k]; n.hi[k] = bx.hi[k]; }
         n.first = (int)order.size();
         n.count = e - b;
-        for (int i = b; i < e; ++i) order.push_back(id(i));
+        for (int i = b; i < e; ++i) order.push_back(r[i].id);
         nodes.push_back(n);
         ++leaves;
         return (int)nodes.size() - 1;
-    }
-
-    void bounds(int b, int e, double lo[3], double hi[3]) const {
-        for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
-        for (int i = b; i < e; ++i)
-            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], (double)tri(id(i)).lo[k]); hi[k] = std::max(hi[k], (double)tri(id(i)).hi[k]); }
     }
 
     // appends a subtree builder's nodes and leaf order; returns its root's index here
@@ -87,63 +176,59 @@ struct BvhBuilder {
     int build(int b, int e, int depth) {
         max_depth = std::max(max_depth, depth);
         const int n = e - b;
+        RangeBoxes bx;
+        reduce_range(b, e, bx, [this](int c0, int c1, RangeBoxes &o) { range_boxes(r, c0, c1, o); });
         if (n <= 2 || depth >= 56) {
-            if (n <= leaf_max) return make_leaf(b, e);
+            if (n <= leaf_max) return make_leaf(b, e, bx);
         }
-        double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
-        for (int i = b; i < e; ++i)
-            for (int k = 0; k < 3; ++k) { clo[k] = std::min(clo[k], (double)tri(id(i)).c[k]); chi[k] = std::max(chi[k], (double)tri(id(i)).c[k]); }
-        double nlo[3], nhi[3];
-        bounds(b, e, nlo, nhi);
+        double clo[3], ext[3], nlo[3], nhi[3];
+        for (int k = 0; k < 3; ++k) {
+            clo[k] = bx.clo[k];
+            ext[k] = (double)bx.chi[k] - clo[k];
+            nlo[k] = bx.lo[k];
+            nhi[k] = bx.hi[k];
+        }
         const double parea = area(nlo, nhi);
-        constexpr int NB = 16;
+        Bins bins;
+        reduce_range(b, e, bins, [this, &clo, &ext](int c0, int c1, Bins &o) { range_bins(r, c0, c1, clo, ext, o); });
         double best = 1e300;
         int best_axis = -1, best_split = -1;
         for (int ax = 0; ax < 3; ++ax) {
-            const double ext = chi[ax] - clo[ax];
-            if (!(ext > 0)) continue;
-            int cnt[NB] = {0};
-            double blo[NB][3], bhi[NB][3];
-            for (int q = 0; q < NB; ++q)
-                for (int k = 0; k < 3; ++k) { blo[q][k] = 1e300; bhi[q][k] = -1e300; }
-            for (int i = b; i < e; ++i) {
-                const BTri &x = tri(id(i));
-                int q = std::min(NB - 1, (int)((x.c[ax] - clo[ax]) / ext * NB));
-                ++cnt[q];
-                for (int k = 0; k < 3; ++k) { blo[q][k] = std::min(blo[q][k], (double)x.lo[k]); bhi[q][k] = std::max(bhi[q][k], (double)x.hi[k]); }
-            }
-            double rarea[NB];
-            int rcnt[NB];
+            if (!(ext[ax] > 0)) continue;
+            double rarea[kBins];
+            int rcnt[kBins];
             double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
             int c = 0;
-            for (int q = NB - 1; q > 0; --q) {
-                c += cnt[q];
-                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], blo[q][k]); hi[k] = std::max(hi[k], bhi[q][k]); }
+            for (int q = kBins - 1; q > 0; --q) {
+                c += bins.cnt[ax][q];
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = std::min(lo[k], (double)bins.lo[ax][q][k]);
+                    hi[k] = std::max(hi[k], (double)bins.hi[ax][q][k]);
+                }
                 rarea[q] = area(lo, hi);
                 rcnt[q] = c;
             }
             for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
             c = 0;
-            for (int q = 0; q < NB - 1; ++q) {
-                c += cnt[q];
-                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], blo[q][k]); hi[k] = std::max(hi[k], bhi[q][k]); }
+            for (int q = 0; q < kBins - 1; ++q) {
+                c += bins.cnt[ax][q];
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = std::min(lo[k], (double)bins.lo[ax][q][k]);
+                    hi[k] = std::max(hi[k], (double)bins.hi[ax][q][k]);
+                }
                 if (c == 0 || rcnt[q + 1] == 0) continue;
                 const double cost = 1.0 + (area(lo, hi) * c + rarea[q + 1] * rcnt[q + 1]) / parea;
                 if (cost < best) { best = cost; best_axis = ax; best_split = q; }
             }
         }
-        if (n <= leaf_max && (best_axis < 0 || best >= (double)n)) return make_leaf(b, e);
+        if (n <= leaf_max && (best_axis < 0 || best >= (double)n)) return make_leaf(b, e, bx);
         int mid;
         if (best_axis < 0) {
             mid = b + n / 2;  // coincident centroids: split the list
         } else {
-            const double ext = chi[best_axis] - clo[best_axis];
-            std::vector<int> &ix = src ? const_cast<BvhBuilder *>(src)->idx : idx;
-            auto it = std::partition(ix.begin() + b, ix.begin() + e, [&](int i) {
-                int q = std::min(NB - 1, (int)((tri(i).c[best_axis] - clo[best_axis]) / ext * NB));
-                return q <= best_split;
-            });
-            mid = (int)(it - ix.begin());
+            const double c0 = clo[best_axis], ex = ext[best_axis];
+            BRef *it = std::partition(r + b, r + e, [&](const BRef &x) { return bin_of(x.c[best_axis], c0, ex) <= best_split; });
+            mid = (int)(it - r);
             if (mid == b || mid == e) mid = b + n / 2;
         }
         BNode node;
@@ -151,23 +236,23 @@ struct BvhBuilder {
         nodes.push_back(node);
         const int me = (int)nodes.size() - 1;
         if (n >= kParallelBuildMin && depth < kParallelBuildDepth) {
-            // both halves on their own builders (disjoint ranges of the shared index array)
+            // both halves on their own builders (disjoint ranges of the shared reference array)
             BvhBuilder L, R;
-            L.src = R.src = src ? src : this;
+            L.r = R.r = r;
             L.leaf_max = R.leaf_max = leaf_max;
             auto fl = std::async(std::launch::async, [&] { return L.build(b, mid, depth + 1); });
             const int rr = R.build(mid, e, depth + 1);
             const int lr = fl.get();
             const int l = append(L, lr);
-            const int r = append(R, rr);
+            const int rt = append(R, rr);
             nodes[me].left = l;
-            nodes[me].right = r;
+            nodes[me].right = rt;
             return me;
         }
         const int l = build(b, mid, depth + 1);
-        const int r = build(mid, e, depth + 1);
+        const int rt = build(mid, e, depth + 1);
         nodes[me].left = l;
-        nodes[me].right = r;
+        nodes[me].right = rt;
         return me;
     }
 };
@@ -176,18 +261,21 @@ struct BvhBuilder {
 void build_bvh(HostScene &hs, int leaf_max) {
     BvhBuilder B;
     B.leaf_max = (leaf_max >= 1 && leaf_max <= kLeafMax) ? leaf_max : kLeafDefault;
-    B.t.resize(hs.ntri);
-    for (int i = 0; i < hs.ntri; ++i) {
-        const double *q = &hs.tri64[9 * (size_t)i];
-        for (int k = 0; k < 3; ++k) {
-            const double a = q[k], b = q[k] + q[3 + k], c = q[k] + q[6 + k];
-            B.t[i].lo[k] = (float)std::min({a, b, c});
-            B.t[i].hi[k] = (float)std::max({a, b, c});
-            B.t[i].c[k] = (float)((a + b + c) / 3.0);
+    std::vector<BRef> refs((size_t)hs.ntri);
+    parallel_chunks((size_t)hs.ntri, 65536, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i) {
+            const double *q = &hs.tri64[9 * i];
+            BRef &x = refs[i];
+            for (int k = 0; k < 3; ++k) {
+                const double a = q[k], b = q[k] + q[3 + k], c = q[k] + q[6 + k];
+                x.lo[k] = (float)std::min({a, b, c});
+                x.hi[k] = (float)std::max({a, b, c});
+                x.c[k] = (float)((a + b + c) / 3.0);
+            }
+            x.id = (int)i;
         }
-    }
-    B.idx.resize(hs.ntri);
-    for (int i = 0; i < hs.ntri; ++i) B.idx[i] = i;
+    });
+    B.r = refs.data();
     int root = B.build(0, hs.ntri, 0);
     // The device walk starts at an inner node: wrap a leaf root.
     if (B.nodes[root].left < 0) {
@@ -221,59 +309,67 @@ void build_bvh(HostScene &hs, int leaf_max) {
         }
     };
     std::vector<int> order4{root};            // binary ids of the 4-wide inner nodes, BFS order
-    std::vector<std::vector<int>> kids4;
-    for (size_t q = 0; q < order4.size(); ++q) {
-        std::vector<int> kids;
-        open(order4[q], kids);
-        for (int k : kids)
-            if (B.nodes[k].left >= 0) order4.push_back(k);
-        kids4.push_back(kids);
-    }
+    std::vector<int> depth4{0};               // their depths
+    std::vector<std::array<int, 4>> kids4;    // their children (binary ids), nkids4 of them
+    std::vector<int> nkids4;
     std::vector<int> id4(B.nodes.size(), -1);
-    for (size_t q = 0; q < order4.size(); ++q) id4[order4[q]] = (int)q;
+    id4[root] = 0;
+    std::vector<int> kids;
+    for (size_t q = 0; q < order4.size(); ++q) {
+        open(order4[q], kids);
+        std::array<int, 4> a{-1, -1, -1, -1};
+        for (size_t k = 0; k < kids.size(); ++k) {
+            a[k] = kids[k];
+            if (B.nodes[kids[k]].left >= 0) {
+                id4[kids[k]] = (int)order4.size();
+                order4.push_back(kids[k]);
+                depth4.push_back(depth4[q] + 1);
+            }
+        }
+        kids4.push_back(a);
+        nkids4.push_back((int)kids.size());
+    }
+    const int max_depth4 = depth4.back();
     const double pad = 2e-6 * hs.scale;
     auto lo_f = [&](double v) { return v > 1e299 ? INFINITY : (float)(v - pad); };
     auto hi_f = [&](double v) { return v < -1e299 ? -INFINITY : (float)(v + pad); };
-    hs.bvh.assign(order4.size() * kBvhNodeFloats, 0.f);
-    int max_depth4 = 0;
-    std::vector<int> depth4(order4.size(), 0);
-    for (size_t q = 0; q < order4.size(); ++q) {
-        float *f = &hs.bvh[kBvhNodeFloats * q];
-        const std::vector<int> &kids = kids4[q];
-        for (int k = 0; k < 4; ++k) {
-            int code;
-            if (k < (int)kids.size()) {
-                const BNode &x = B.nodes[kids[k]];
-                f[0 + k] = lo_f(x.lo[0]); f[4 + k] = hi_f(x.hi[0]);
-                f[8 + k] = lo_f(x.lo[1]); f[12 + k] = hi_f(x.hi[1]);
-                f[16 + k] = lo_f(x.lo[2]); f[20 + k] = hi_f(x.hi[2]);
-                if (x.left >= 0) {
-                    code = id4[kids[k]];
-                    depth4[code] = depth4[q] + 1;
-                    max_depth4 = std::max(max_depth4, depth4[code]);
-                } else {
-                    code = ~(x.first * 16 + (x.count - 1));
+    hs.bvh.resize(order4.size() * kBvhNodeFloats);
+    parallel_chunks(order4.size(), 16384, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q) {
+            float *f = &hs.bvh[kBvhNodeFloats * q];
+            const std::array<int, 4> &kq = kids4[q];
+            for (int k = 0; k < 4; ++k) {
+                int code;
+                if (k < nkids4[q]) {
+                    const BNode &x = B.nodes[kq[k]];
+                    f[0 + k] = lo_f(x.lo[0]); f[4 + k] = hi_f(x.hi[0]);
+                    f[8 + k] = lo_f(x.lo[1]); f[12 + k] = hi_f(x.hi[1]);
+                    f[16 + k] = lo_f(x.lo[2]); f[20 + k] = hi_f(x.hi[2]);
+                    code = x.left >= 0 ? id4[kq[k]] : ~(x.first * 16 + (x.count - 1));
+                } else {  // empty slot: flagged by its code (a slab test cannot reject an inverted box)
+                    f[0 + k] = f[4 + k] = f[8 + k] = f[12 + k] = f[16 + k] = f[20 + k] = 0.f;
+                    code = (int)0x80000000;
                 }
-            } else {  // empty slot: flagged by its code (a slab test cannot reject an inverted box)
-                f[0 + k] = f[4 + k] = f[8 + k] = f[12 + k] = f[16 + k] = f[20 + k] = 0.f;
-                code = (int)0x80000000;
+                std::memcpy(&f[24 + k], &code, 4);
+                f[28 + k] = 0.f;
             }
-            std::memcpy(&f[24 + k], &code, 4);
         }
-    }
+    });
     B.max_depth = max_depth4 + 1;
     hs.bvh_nodes = (int)order4.size();
     hs.bvh_leaves = B.leaves;
     hs.bvh_depth = B.max_depth;
     // reorder triangles into leaf order
-    std::vector<double> t64(hs.tri64.size());
-    std::vector<int32_t> tp(hs.ntri), tl(hs.ntri);
-    for (int i = 0; i < hs.ntri; ++i) {
-        const int s = B.order[i];
-        std::copy(&hs.tri64[9 * (size_t)s], &hs.tri64[9 * (size_t)s] + 9, &t64[9 * (size_t)i]);
-        tp[i] = hs.tri_poly[s];
-        tl[i] = hs.tri_plane[s];
-    }
+    hvec<double> t64(hs.tri64.size());
+    hvec<int32_t> tp(hs.ntri), tl(hs.ntri);
+    parallel_chunks((size_t)hs.ntri, 65536, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i) {
+            const int s = B.order[i];
+            std::copy(&hs.tri64[9 * (size_t)s], &hs.tri64[9 * (size_t)s] + 9, &t64[9 * i]);
+            tp[i] = hs.tri_poly[s];
+            tl[i] = hs.tri_plane[s];
+        }
+    });
     hs.tri64.swap(t64);
     hs.tri_poly.swap(tp);
     hs.tri_plane.swap(tl);
@@ -290,20 +386,9 @@ static void quantize_nodes(HostScene &hs, size_t q0, size_t q1);
 
 void quantize_bvh(HostScene &hs) {
     const size_t nodes = hs.bvh.size() / kBvhNodeFloats;
-    hs.bvhq.assign(nodes * kBvhQNodeFloats, 0.f);
+    hs.bvhq.resize(nodes * kBvhQNodeFloats);  // every float of every node is written
     // nodes are independent: large trees are quantised in chunks on several threads
-    const size_t chunk = 8192;
-    const size_t nchunks = (nodes + chunk - 1) / chunk;
-    if (nchunks > 1) {
-        std::vector<std::future<void>> parts;
-        for (size_t c = 0; c < nchunks; ++c)
-            parts.push_back(std::async(std::launch::async, [&hs, c, chunk, nodes] {
-                quantize_nodes(hs, c * chunk, std::min(nodes, (c + 1) * chunk));
-            }));
-        for (auto &p : parts) p.get();
-    } else {
-        quantize_nodes(hs, 0, nodes);
-    }
+    parallel_chunks(nodes, 8192, [&hs](size_t q0, size_t q1) { quantize_nodes(hs, q0, q1); });
 }
 
 // Quantised copy of nodes [q0, q1) (see quantize_bvh).
@@ -589,62 +674,124 @@ bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err)
     for (int i = 0; i < 3 * nv; ++i)
         if (!std::isfinite(d->vertices[i])) { err = "scene: non-finite vertex coordinate"; return false; }
     auto V = [&](int i) { return D3{d->vertices[3 * i], d->vertices[3 * i + 1], d->vertices[3 * i + 2]}; };
-    hs.alpha.assign(d->absorption, d->absorption + 8 * (size_t)hs.npoly);
-    hs.scat.assign(d->scattering, d->scattering + 8 * (size_t)hs.npoly);
-    if (d->transmission) hs.trans.assign(d->transmission, d->transmission + 8 * (size_t)hs.npoly);
-    else hs.trans.assign(8 * (size_t)hs.npoly, 0.0);
-    for (size_t i = 0; i < hs.alpha.size(); ++i) {
-        if (!(hs.alpha[i] >= 0 && hs.alpha[i] <= 1) || !(hs.scat[i] >= 0 && hs.scat[i] <= 1) ||
-            !(hs.trans[i] >= 0 && hs.trans[i] <= 1)) {
+    hs.alpha.resize(8 * (size_t)hs.npoly);
+    hs.scat.resize(8 * (size_t)hs.npoly);
+    hs.trans.resize(8 * (size_t)hs.npoly);
+    hs.normal.resize(3 * (size_t)hs.npoly);
+    hs.area.resize(hs.npoly);
+
+    // Polygons in parallel chunks: coefficient ranges, vertex indices, Newell normal and area, and the
+    // count of non-degenerate fan pieces.  A coefficient out of range is reported first, else the first
+    // failing polygon in polygon order names the error.
+    constexpr size_t kPolyGrain = 16384;
+    const size_t nchunk = ((size_t)hs.npoly + kPolyGrain - 1) / kPolyGrain;
+    struct PolyChunk {
+        bool bad_coef = false;
+        int bad = -1;
+        std::string msg;
+        bool trans = false;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    };
+    std::vector<PolyChunk> pc(nchunk);
+    std::vector<int> fan(hs.npoly + 1, 0);
+    parallel_chunks((size_t)hs.npoly, kPolyGrain, [&](size_t p0, size_t p1) {
+        PolyChunk &c = pc[p0 / kPolyGrain];
+        std::copy(d->absorption + 8 * p0, d->absorption + 8 * p1, hs.alpha.begin() + 8 * p0);
+        std::copy(d->scattering + 8 * p0, d->scattering + 8 * p1, hs.scat.begin() + 8 * p0);
+        if (d->transmission) std::copy(d->transmission + 8 * p0, d->transmission + 8 * p1, hs.trans.begin() + 8 * p0);
+        else std::fill(hs.trans.begin() + 8 * p0, hs.trans.begin() + 8 * p1, 0.0);
+        for (size_t i = 8 * p0; i < 8 * p1; ++i) {
+            if (!(hs.alpha[i] >= 0 && hs.alpha[i] <= 1) || !(hs.scat[i] >= 0 && hs.scat[i] <= 1) ||
+                !(hs.trans[i] >= 0 && hs.trans[i] <= 1)) {
+                c.bad_coef = true;
+                break;
+            }
+            if (hs.trans[i] > 0) c.trans = true;
+        }
+        for (int p = (int)p0; p < (int)p1; ++p) {
+            int b = d->poly_offsets[p], e = d->poly_offsets[p + 1];
+            if (e - b < 3 || b < 0) {
+                c.bad = p;
+                c.msg = "scene: polygon " + std::to_string(p) + " has fewer than 3 vertices";
+                return;
+            }
+            for (int k = b; k < e; ++k)
+                if (d->poly_indices[k] < 0 || d->poly_indices[k] >= nv) {
+                    c.bad = p;
+                    c.msg = "scene: vertex index out of range";
+                    return;
+                }
+            D3 n{0, 0, 0};
+            for (int k = b; k < e; ++k) {  // Newell
+                D3 p0v = V(d->poly_indices[k]), p1v = V(d->poly_indices[k + 1 < e ? k + 1 : b]);
+                n.x += (p0v.y - p1v.y) * (p0v.z + p1v.z);
+                n.y += (p0v.z - p1v.z) * (p0v.x + p1v.x);
+                n.z += (p0v.x - p1v.x) * (p0v.y + p1v.y);
+            }
+            hs.area[p] = 0.5 * std::sqrt(dot(n, n));
+            if (!(hs.area[p] > 0)) {
+                c.bad = p;
+                c.msg = "scene: degenerate polygon " + std::to_string(p);
+                return;
+            }
+            D3 u = unit(n);
+            hs.normal[3 * p] = u.x; hs.normal[3 * p + 1] = u.y; hs.normal[3 * p + 2] = u.z;
+            D3 a = V(d->poly_indices[b]);
+            int cnt = 0;
+            for (int k = b + 1; k + 1 < e; ++k) {
+                D3 e1 = sub(V(d->poly_indices[k]), a), e2 = sub(V(d->poly_indices[k + 1]), a);
+                if (dot(cross(e1, e2), cross(e1, e2)) != 0) ++cnt;  // zero-area fan pieces are dropped
+            }
+            fan[p + 1] = cnt;
+            for (int k = b; k < e; ++k) {
+                D3 q = V(d->poly_indices[k]);
+                c.lo[0] = std::min(c.lo[0], q.x); c.lo[1] = std::min(c.lo[1], q.y); c.lo[2] = std::min(c.lo[2], q.z);
+                c.hi[0] = std::max(c.hi[0], q.x); c.hi[1] = std::max(c.hi[1], q.y); c.hi[2] = std::max(c.hi[2], q.z);
+            }
+        }
+    });
+    for (const PolyChunk &c : pc)
+        if (c.bad_coef) {
             err = "scene: absorption, scattering and transmission must lie in [0, 1]";
             return false;
         }
-        if (hs.trans[i] > 0) hs.has_trans = true;
-    }
-    hs.normal.resize(3 * (size_t)hs.npoly);
-    hs.area.resize(hs.npoly);
     for (int k = 0; k < 3; ++k) { hs.bmin[k] = 1e300; hs.bmax[k] = -1e300; }
-    for (int p = 0; p < hs.npoly; ++p) {
-        int b = d->poly_offsets[p], e = d->poly_offsets[p + 1];
-        if (e - b < 3 || b < 0) { err = "scene: polygon " + std::to_string(p) + " has fewer than 3 vertices"; return false; }
-        for (int k = b; k < e; ++k)
-            if (d->poly_indices[k] < 0 || d->poly_indices[k] >= nv) { err = "scene: vertex index out of range"; return false; }
-        D3 n{0, 0, 0};
-        for (int k = b; k < e; ++k) {  // Newell
-            D3 p0 = V(d->poly_indices[k]), p1 = V(d->poly_indices[k + 1 < e ? k + 1 : b]);
-            n.x += (p0.y - p1.y) * (p0.z + p1.z);
-            n.y += (p0.z - p1.z) * (p0.x + p1.x);
-            n.z += (p0.x - p1.x) * (p0.y + p1.y);
-        }
-        hs.area[p] = 0.5 * std::sqrt(dot(n, n));
-        if (!(hs.area[p] > 0)) { err = "scene: degenerate polygon " + std::to_string(p); return false; }
-        D3 u = unit(n);
-        hs.normal[3 * p] = u.x; hs.normal[3 * p + 1] = u.y; hs.normal[3 * p + 2] = u.z;
-        D3 a = V(d->poly_indices[b]);
-        for (int k = b + 1; k + 1 < e; ++k) {
-            D3 pb = V(d->poly_indices[k]), pc = V(d->poly_indices[k + 1]);
-            D3 e1 = sub(pb, a), e2 = sub(pc, a);
-            if (dot(cross(e1, e2), cross(e1, e2)) == 0) continue;  // zero-area fan piece
-            const double t9[9] = {a.x, a.y, a.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z};
-            hs.tri64.insert(hs.tri64.end(), t9, t9 + 9);
-            hs.tri_poly.push_back(p);
-        }
-        for (int k = b; k < e; ++k) {
-            D3 q = V(d->poly_indices[k]);
-            hs.bmin[0] = std::min(hs.bmin[0], q.x); hs.bmin[1] = std::min(hs.bmin[1], q.y); hs.bmin[2] = std::min(hs.bmin[2], q.z);
-            hs.bmax[0] = std::max(hs.bmax[0], q.x); hs.bmax[1] = std::max(hs.bmax[1], q.y); hs.bmax[2] = std::max(hs.bmax[2], q.z);
-        }
+    for (const PolyChunk &c : pc) {
+        if (c.bad >= 0) { err = c.msg; return false; }
+        hs.has_trans = hs.has_trans || c.trans;
+        for (int k = 0; k < 3; ++k) { hs.bmin[k] = std::min(hs.bmin[k], c.lo[k]); hs.bmax[k] = std::max(hs.bmax[k], c.hi[k]); }
     }
-    hs.ntri = (int)hs.tri_poly.size();
+    for (int p = 0; p < hs.npoly; ++p) fan[p + 1] += fan[p];
+    hs.ntri = fan[hs.npoly];
     if (hs.ntri == 0) { err = "scene: no triangles"; return false; }
+    hs.tri64.resize(9 * (size_t)hs.ntri);
+    hs.tri_poly.resize(hs.ntri);
+    parallel_chunks((size_t)hs.npoly, kPolyGrain, [&](size_t p0, size_t p1) {
+        for (int p = (int)p0; p < (int)p1; ++p) {
+            const int b = d->poly_offsets[p], e = d->poly_offsets[p + 1];
+            int t = fan[p];
+            D3 a = V(d->poly_indices[b]);
+            for (int k = b + 1; k + 1 < e; ++k) {
+                D3 e1 = sub(V(d->poly_indices[k]), a), e2 = sub(V(d->poly_indices[k + 1]), a);
+                if (dot(cross(e1, e2), cross(e1, e2)) == 0) continue;
+                double *t9 = &hs.tri64[9 * (size_t)t];
+                t9[0] = a.x; t9[1] = a.y; t9[2] = a.z;
+                t9[3] = e1.x; t9[4] = e1.y; t9[5] = e1.z;
+                t9[6] = e2.x; t9[7] = e2.y; t9[8] = e2.z;
+                hs.tri_poly[t++] = p;
+            }
+        }
+    });
     double ext[3];
     for (int k = 0; k < 3; ++k) ext[k] = hs.bmax[k] - hs.bmin[k];
     hs.scale = std::max({ext[0], ext[1], ext[2], 1e-3});
     const double pad = 1e-5 * hs.scale;
     for (int k = 0; k < 3; ++k) { hs.bmin[k] -= pad; hs.bmax[k] += pad; ext[k] = hs.bmax[k] - hs.bmin[k]; }
 
-    // Coplanar groups: quantised (canonical normal, offset) of each triangle's own plane.
-    // (flat open-addressing table; ids in order of first appearance)
+    // Coplanar groups: quantised (canonical normal, offset) of each triangle's own plane; ids in order
+    // of first appearance.  Keys are computed in parallel; large scenes are grouped in shards (by the
+    // top bits of the key's hash, one open-addressing table per shard), each triangle pointing at the
+    // first triangle of its group, and the ids are then numbered in triangle order.
     struct PlaneKey {
         long long v[4];
         bool operator==(const PlaneKey &o) const { return v[0] == o.v[0] && v[1] == o.v[1] && v[2] == o.v[2] && v[3] == o.v[3]; }
@@ -654,27 +801,41 @@ bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err)
         for (long long x : k.v) h = (h ^ (uint64_t)x) * 0xBF58476D1CE4E5B9ull + (h >> 29);
         return h ^ (h >> 31);
     };
-    size_t cap = 16;
-    while (cap < 2 * (size_t)hs.ntri) cap <<= 1;
-    std::vector<PlaneKey> slot_key(cap);
-    std::vector<int> slot_id(cap, -1);
-    int n_planes = 0;
-    hs.tri_plane.resize(hs.ntri);
-    for (int i = 0; i < hs.ntri; ++i) {
-        const double *t = &hs.tri64[9 * (size_t)i];
-        D3 n = unit(cross(D3{t[3], t[4], t[5]}, D3{t[6], t[7], t[8]}));
-        if (n.x < 0 || (n.x == 0 && (n.y < 0 || (n.y == 0 && n.z < 0)))) n = mul(n, -1);
-        double off = dot(n, D3{t[0], t[1], t[2]}) / hs.scale;
-        const PlaneKey key{{std::llround(n.x * 1e6), std::llround(n.y * 1e6), std::llround(n.z * 1e6),
-                            std::llround(off * 1e6)}};
-        size_t h = (size_t)hash(key) & (cap - 1);
-        while (slot_id[h] >= 0 && !(slot_key[h] == key)) h = (h + 1) & (cap - 1);
-        if (slot_id[h] < 0) {
-            slot_key[h] = key;
-            slot_id[h] = n_planes++;
+    std::vector<PlaneKey> keys((size_t)hs.ntri);
+    std::vector<uint64_t> khash((size_t)hs.ntri);
+    parallel_chunks((size_t)hs.ntri, 65536, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i) {
+            const double *t = &hs.tri64[9 * i];
+            D3 n = unit(cross(D3{t[3], t[4], t[5]}, D3{t[6], t[7], t[8]}));
+            if (n.x < 0 || (n.x == 0 && (n.y < 0 || (n.y == 0 && n.z < 0)))) n = mul(n, -1);
+            double off = dot(n, D3{t[0], t[1], t[2]}) / hs.scale;
+            keys[i] = PlaneKey{{std::llround(n.x * 1e6), std::llround(n.y * 1e6), std::llround(n.z * 1e6),
+                                std::llround(off * 1e6)}};
+            khash[i] = hash(keys[i]);
         }
-        hs.tri_plane[i] = slot_id[h];
-    }
+    });
+    const int shards = hs.ntri >= 65536 ? 16 : 1;
+    std::vector<int> first((size_t)hs.ntri);
+    parallel_chunks((size_t)shards, 1, [&](size_t s0, size_t s1) {
+        for (size_t s = s0; s < s1; ++s) {
+            auto mine = [&](size_t i) { return shards == 1 || (khash[i] >> 60) == s; };
+            size_t count = 0;
+            for (size_t i = 0; i < (size_t)hs.ntri; ++i) count += mine(i);
+            size_t cap = 16;
+            while (cap < 2 * count) cap <<= 1;
+            std::vector<int> slot(cap, -1);  // first triangle of the slot's group
+            for (size_t i = 0; i < (size_t)hs.ntri; ++i) {
+                if (!mine(i)) continue;
+                size_t h = (size_t)khash[i] & (cap - 1);
+                while (slot[h] >= 0 && !(keys[(size_t)slot[h]] == keys[i])) h = (h + 1) & (cap - 1);
+                if (slot[h] < 0) slot[h] = (int)i;
+                first[i] = slot[h];
+            }
+        }
+    });
+    hs.tri_plane.resize(hs.ntri);
+    int n_planes = 0;
+    for (int i = 0; i < hs.ntri; ++i) hs.tri_plane[i] = first[i] == i ? n_planes++ : hs.tri_plane[first[i]];
 
     build_bvh(hs, d->bvh_leaf_max);
     quantize_bvh(hs);
