@@ -54,7 +54,41 @@ struct RangeBoxes {
             clo[k] = std::min(clo[k], o.clo[k]); chi[k] = std::max(chi[k], o.chi[k]);
         }
     }
+    void add(const BRef &x) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], x.lo[k]); hi[k] = std::max(hi[k], x.hi[k]);
+            clo[k] = std::min(clo[k], x.c[k]); chi[k] = std::max(chi[k], x.c[k]);
+        }
+    }
 };
+
+// Two-ended partition (each element tested once: from the front while it passes, from the back while
+// it fails, then one swap), accumulating the boxes of both sides so that the children need no pass
+// of their own for them.
+template <class P>
+BRef *partition_boxes(BRef *first, BRef *last, P pred, RangeBoxes &L, RangeBoxes &R) {
+    L.clear();
+    R.clear();
+    for (;;) {
+        for (;;) {
+            if (first == last) return first;
+            if (!pred(*first)) break;
+            L.add(*first);
+            ++first;
+        }
+        R.add(*first);  // fails: ends on the right (returned position or swapped to the back)
+        --last;
+        for (;;) {
+            if (first == last) return first;
+            if (pred(*last)) break;
+            R.add(*last);
+            --last;
+        }
+        L.add(*last);
+        std::swap(*first, *last);
+        ++first;
+    }
+}
 
 // Per axis and bin: triangle count and the union of the triangles' boxes.
 struct Bins {
@@ -173,11 +207,13 @@ struct BvhBuilder {
         return root + noff;
     }
 
-    int build(int b, int e, int depth) {
+    // known: the boxes of [b, e) when the parent's partition accumulated them
+    int build(int b, int e, int depth, const RangeBoxes *known = nullptr) {
         max_depth = std::max(max_depth, depth);
         const int n = e - b;
         RangeBoxes bx;
-        reduce_range(b, e, bx, [this](int c0, int c1, RangeBoxes &o) { range_boxes(r, c0, c1, o); });
+        if (known) bx = *known;
+        else reduce_range(b, e, bx, [this](int c0, int c1, RangeBoxes &o) { range_boxes(r, c0, c1, o); });
         if (n <= 2 || depth >= 56) {
             if (n <= leaf_max) return make_leaf(b, e, bx);
         }
@@ -223,14 +259,22 @@ struct BvhBuilder {
         }
         if (n <= leaf_max && (best_axis < 0 || best >= (double)n)) return make_leaf(b, e, bx);
         int mid;
+        RangeBoxes lbx, rbx;
+        bool split_boxes = false;
         if (best_axis < 0) {
             mid = b + n / 2;  // coincident centroids: split the list
         } else {
             const double c0 = clo[best_axis], ex = ext[best_axis];
-            BRef *it = std::partition(r + b, r + e, [&](const BRef &x) { return bin_of(x.c[best_axis], c0, ex) <= best_split; });
+            BRef *it = partition_boxes(r + b, r + e, [&](const BRef &x) { return bin_of(x.c[best_axis], c0, ex) <= best_split; },
+                                       lbx, rbx);
             mid = (int)(it - r);
-            if (mid == b || mid == e) mid = b + n / 2;
+            split_boxes = true;
+            if (mid == b || mid == e) {
+                mid = b + n / 2;
+                split_boxes = false;
+            }
         }
+        const RangeBoxes *lk = split_boxes ? &lbx : nullptr, *rk = split_boxes ? &rbx : nullptr;
         BNode node;
         for (int k = 0; k < 3; ++k) { node.lo[k] = nlo[k]; node.hi[k] = nhi[k]; }
         nodes.push_back(node);
@@ -240,8 +284,8 @@ struct BvhBuilder {
             BvhBuilder L, R;
             L.r = R.r = r;
             L.leaf_max = R.leaf_max = leaf_max;
-            auto fl = std::async(std::launch::async, [&] { return L.build(b, mid, depth + 1); });
-            const int rr = R.build(mid, e, depth + 1);
+            auto fl = std::async(std::launch::async, [&] { return L.build(b, mid, depth + 1, lk); });
+            const int rr = R.build(mid, e, depth + 1, rk);
             const int lr = fl.get();
             const int l = append(L, lr);
             const int rt = append(R, rr);
@@ -249,8 +293,8 @@ struct BvhBuilder {
             nodes[me].right = rt;
             return me;
         }
-        const int l = build(b, mid, depth + 1);
-        const int rt = build(mid, e, depth + 1);
+        const int l = build(b, mid, depth + 1, lk);
+        const int rt = build(mid, e, depth + 1, rk);
         nodes[me].left = l;
         nodes[me].right = rt;
         return me;
