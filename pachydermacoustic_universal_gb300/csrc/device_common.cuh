@@ -104,10 +104,11 @@ __device__ __noinline__ bool retest64(const DevScene &S, int i, float3 of, float
     return true;
 }
 
-// Traversal work of one thread: FP64 re-tests, inner BVH nodes visited, triangles tested.
+// Traversal work of one thread in one launch: FP64 re-tests, inner BVH nodes visited, triangles
+// tested (32-bit: a thread walks a few thousand rays per launch at most; launches sum them in 64 bits).
 struct TraceWork {
-    unsigned long long retests = 0;
-    unsigned long long nodes = 0, tris = 0;
+    unsigned retests = 0;
+    unsigned nodes = 0, tris = 0;
 };
 
 // One candidate triangle: FP32 Moller-Trumbore, FP64 re-test inside the epsilon band.

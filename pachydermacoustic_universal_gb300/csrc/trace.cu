@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     const int lane = threadIdx.x & 31;
     TraceWork w;
     bool have = false, exhausted = false;
-    unsigned long long j = 0;
+    unsigned j = 0;  // index in the wave (a wave holds at most half the ring: < 2^31 items)
     float3 o = make_float3(0.f, 0.f, 0.f), d = o;
     float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f, best = FLT_MAX;
     int skip = -1, node = 0, sp = 0, bi = -1, leaf = 0;
@@ -392,8 +392,9 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             if (lane == leader) base = atomicAdd(&c->trace_next, (unsigned long long)__popc(need));
             base = __shfl_sync(FULL, base, leader);
             if (!have && !exhausted) {
-                j = base + __popc(need & ((1u << lane) - 1u));
-                if (j < m) {
+                const unsigned long long jj = base + __popc(need & ((1u << lane) - 1u));
+                j = (unsigned)jj;
+                if (jj < m) {
                     const float4 *q = reinterpret_cast<const float4 *>(wave_item(r, head, j));
                     const float4 P = __ldcs(q), D = __ldcs(q + 1), X = __ldcs(q + 3);
                     o = f3(P);
