@@ -284,7 +284,24 @@ bool room_setup(RoomSpec &rm, const pach_trace_params &p, std::string &err) {
 // (k_cond) ends the loop when the run is done; progress and cancellation go through mapped host
 // memory.  With kernel_timing = 1 the host launches batches of iterations instead, with CUDA events
 // around every kernel.
+void run_worker_body(pach_run *run);
+
+// The run's host thread: a C++ exception (a failed host allocation) ends the run as failed instead of
+// ending the process.
 void run_worker(pach_run *run) {
+    try {
+        run_worker_body(run);
+    } catch (const std::exception &ex) {
+        std::lock_guard<std::mutex> lk(run->mu);
+        run->status = PACH_ERR_OUT_OF_MEMORY;
+        run->err = std::string("host resources exhausted: ") + ex.what();
+        run->state = PACH_RUN_FAILED;
+        run->finished = true;
+        run->cv.notify_all();
+    }
+}
+
+void run_worker_body(pach_run *run) {
     auto finish = [&](pach_status s, const std::string &msg, int st) {
         std::lock_guard<std::mutex> lk(run->mu);
         run->status = s;
@@ -855,446 +872,488 @@ int pach_device_count(void) {
 
 pach_status pach_medium_properties(double temp_c, double hr, double pa_hpa, int32_t air_choice, int32_t edge,
                                    double atten[PACH_BANDS], double *c, double *rho) {
-    if (!atten) return fail(PACH_ERR_INVALID_ARGUMENT, "atten is null");
-    if (!(pa_hpa > 0) || !(hr > 0) || air_choice < 0 || air_choice > 2)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "medium: pressure and humidity must be positive, air_choice 0..2");
-    medium_properties(temp_c, hr, pa_hpa, air_choice, edge, atten, c, rho);
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!atten) return fail(PACH_ERR_INVALID_ARGUMENT, "atten is null");
+        if (!(pa_hpa > 0) || !(hr > 0) || air_choice < 0 || air_choice > 2)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "medium: pressure and humidity must be positive, air_choice 0..2");
+        medium_properties(temp_c, hr, pa_hpa, air_choice, edge, atten, c, rho);
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_medium_attenuation_third_octave(double temp_c, double hr, double pa_hpa, int32_t air_choice,
                                                  int32_t edge, double *atten, double *centres_hz) {
-    if (!atten) return fail(PACH_ERR_INVALID_ARGUMENT, "atten is null");
-    if (!(pa_hpa > 0) || !(hr > 0) || air_choice < 0 || air_choice > 2)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "medium: pressure and humidity must be positive, air_choice 0..2");
-    medium_attenuation_third_octave(temp_c, hr, pa_hpa, air_choice, edge, atten);
-    if (centres_hz) for (int i = 0; i < kThirdOctaveBands; ++i) centres_hz[i] = kThirdOctaveCentres[i];
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!atten) return fail(PACH_ERR_INVALID_ARGUMENT, "atten is null");
+        if (!(pa_hpa > 0) || !(hr > 0) || air_choice < 0 || air_choice > 2)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "medium: pressure and humidity must be positive, air_choice 0..2");
+        medium_attenuation_third_octave(temp_c, hr, pa_hpa, air_choice, edge, atten);
+        if (centres_hz) for (int i = 0; i < kThirdOctaveBands; ++i) centres_hz[i] = kThirdOctaveCentres[i];
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
-    if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
-    *out = nullptr;
-    if (!desc) return fail(PACH_ERR_INVALID_ARGUMENT, "desc is null");
-    if (!(desc->pressure_hpa > 0) || !(desc->rel_humidity > 0) || desc->air_choice < 0 || desc->air_choice > 2)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "scene: pressure and humidity must be positive, air_choice 0..2");
-    auto *sc = new pach_scene();
-    std::string err;
-    if (!build_host_scene(desc, sc->hs, err)) {
-        delete sc;
-        return fail(PACH_ERR_INVALID_ARGUMENT, err);
-    }
-    if (pach_device_count() <= 0) {
-        delete sc;
-        return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
-    }
-    cudaGetDevice(&sc->device);
-    SceneArrays A;
-    append_scene(sc->hs, A);
-    const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->bvhq, sc->dev);
-    if (e != cudaSuccess) {
-        delete sc;
-        return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
-    }
-    *out = sc;
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
+        *out = nullptr;
+        if (!desc) return fail(PACH_ERR_INVALID_ARGUMENT, "desc is null");
+        if (!(desc->pressure_hpa > 0) || !(desc->rel_humidity > 0) || desc->air_choice < 0 || desc->air_choice > 2)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "scene: pressure and humidity must be positive, air_choice 0..2");
+        std::unique_ptr<pach_scene> sc(new pach_scene());
+        std::string err;
+        if (!build_host_scene(desc, sc->hs, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
+        if (pach_device_count() <= 0)
+            return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
+        cudaGetDevice(&sc->device);
+        SceneArrays A;
+        append_scene(sc->hs, A);
+        const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->bvhq, sc->dev);
+        if (e != cudaSuccess)
+            return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
+        *out = sc.release();
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_scenes_create(const pach_scene_desc *descs, int32_t n, pach_scene **out, int32_t threads) {
-    if (!out || (n > 0 && !descs) || n < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "scenes: bad arguments");
-    for (int i = 0; i < n; ++i) out[i] = nullptr;
-    for (int i = 0; i < n; ++i)
-        if (!(descs[i].pressure_hpa > 0) || !(descs[i].rel_humidity > 0) || descs[i].air_choice < 0 ||
-            descs[i].air_choice > 2)
-            return fail(PACH_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) +
-                                                       ": pressure and humidity must be positive, air_choice 0..2");
-    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
-    int device = 0;
-    cudaGetDevice(&device);
-    // host builds (BVH, quantised nodes, materials) on worker threads, largest scenes first
-    std::vector<std::unique_ptr<pach_scene>> sc((size_t)n);
-    std::vector<std::string> errs((size_t)n);
-    std::vector<int> order((size_t)n);
-    for (int i = 0; i < n; ++i) order[(size_t)i] = i;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return descs[a].n_polys > descs[b].n_polys; });
-    std::atomic<int> next{0};
-    const int nt = std::max(1, std::min(n, threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency())));
-    auto work = [&] {
-        for (int j; (j = next.fetch_add(1)) < n;) {
-            const int i = order[(size_t)j];
-            sc[(size_t)i].reset(new pach_scene());
-            if (!build_host_scene(&descs[i], sc[(size_t)i]->hs, errs[(size_t)i])) sc[(size_t)i].reset();
+    return guarded([&]() -> pach_status {
+        if (!out || (n > 0 && !descs) || n < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "scenes: bad arguments");
+        for (int i = 0; i < n; ++i) out[i] = nullptr;
+        for (int i = 0; i < n; ++i)
+            if (!(descs[i].pressure_hpa > 0) || !(descs[i].rel_humidity > 0) || descs[i].air_choice < 0 ||
+                descs[i].air_choice > 2)
+                return fail(PACH_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) +
+                                                           ": pressure and humidity must be positive, air_choice 0..2");
+        if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
+        int device = 0;
+        cudaGetDevice(&device);
+        // host builds (BVH, quantised nodes, materials) on worker threads, largest scenes first
+        std::vector<std::unique_ptr<pach_scene>> sc((size_t)n);
+        std::vector<std::string> errs((size_t)n);
+        std::vector<int> order((size_t)n);
+        for (int i = 0; i < n; ++i) order[(size_t)i] = i;
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return descs[a].n_polys > descs[b].n_polys; });
+        std::atomic<int> next{0};
+        const int nt = std::max(1, std::min(n, threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency())));
+        std::vector<char> oom((size_t)n, 0);
+        auto work = [&] {
+            for (int j; (j = next.fetch_add(1)) < n;) {
+                const int i = order[(size_t)j];
+                try {  // nothing may leave a worker thread
+                    sc[(size_t)i].reset(new pach_scene());
+                    if (!build_host_scene(&descs[i], sc[(size_t)i]->hs, errs[(size_t)i])) sc[(size_t)i].reset();
+                } catch (const std::exception &ex) {
+                    sc[(size_t)i].reset();
+                    oom[(size_t)i] = 1;
+                    errs[(size_t)i] = std::string("host resources exhausted: ") + ex.what();
+                }
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) {
+            try {
+                pool.emplace_back(work);
+            } catch (const std::exception &) {
+                break;  // fewer threads: the calling thread takes the rest
+            }
         }
-    };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
-    work();
-    for (std::thread &t : pool) t.join();
-    for (int i = 0; i < n; ++i)
-        if (!sc[(size_t)i]) return fail(PACH_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) + ": " + errs[(size_t)i]);
-    // device copies on the caller's device
-    for (int i = 0; i < n; ++i) {
-        pach_scene *s = sc[(size_t)i].get();
-        s->device = device;
-        SceneArrays A;
-        append_scene(s->hs, A);
-        const cudaError_t e = upload_scene(A, s->tri, s->tri64, s->norm, s->mat, s->trans, s->bvh, s->bvhq, s->dev);
-        if (e != cudaSuccess)
-            return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
-    }
-    for (int i = 0; i < n; ++i) out[i] = sc[(size_t)i].release();
-    return PACH_OK;
+        work();
+        for (std::thread &t : pool) t.join();
+        for (int i = 0; i < n; ++i)
+            if (!sc[(size_t)i])
+                return fail(oom[(size_t)i] ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_INVALID_ARGUMENT,
+                            "scene " + std::to_string(i) + ": " + errs[(size_t)i]);
+        // device copies on the caller's device
+        for (int i = 0; i < n; ++i) {
+            pach_scene *s = sc[(size_t)i].get();
+            s->device = device;
+            SceneArrays A;
+            append_scene(s->hs, A);
+            const cudaError_t e = upload_scene(A, s->tri, s->tri64, s->norm, s->mat, s->trans, s->bvh, s->bvhq, s->dev);
+            if (e != cudaSuccess)
+                return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
+        }
+        for (int i = 0; i < n; ++i) out[i] = sc[(size_t)i].release();
+        return PACH_OK;
+    }, fail);
 }
 
 void pach_scene_destroy(pach_scene *scene) { delete scene; }
 
 pach_status pach_scene_info(const pach_scene *scene, int32_t *n_polys, int32_t *n_triangles, double *sound_speed,
                             double *rho_c, double atten[PACH_BANDS], double *poly_area) {
-    if (!scene) return fail(PACH_ERR_INVALID_ARGUMENT, "null scene");
-    const HostScene &hs = scene->hs;
-    if (n_polys) *n_polys = hs.npoly;
-    if (n_triangles) *n_triangles = hs.ntri;
-    if (sound_speed) *sound_speed = hs.c;
-    if (rho_c) *rho_c = hs.rho_c;
-    if (atten) for (int o = 0; o < kBands; ++o) atten[o] = hs.atten[o];
-    if (poly_area) for (int p = 0; p < hs.npoly; ++p) poly_area[p] = hs.area[p];
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!scene) return fail(PACH_ERR_INVALID_ARGUMENT, "null scene");
+        const HostScene &hs = scene->hs;
+        if (n_polys) *n_polys = hs.npoly;
+        if (n_triangles) *n_triangles = hs.ntri;
+        if (sound_speed) *sound_speed = hs.c;
+        if (rho_c) *rho_c = hs.rho_c;
+        if (atten) for (int o = 0; o < kBands; ++o) atten[o] = hs.atten[o];
+        if (poly_area) for (int p = 0; p < hs.npoly; ++p) poly_area[p] = hs.area[p];
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
                              const pach_receiver_desc *receivers, int32_t n_receivers, const pach_trace_params *params,
                              pach_run **out) {
-    if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
-    *out = nullptr;
-    if (!scene || !params) return fail(PACH_ERR_INVALID_ARGUMENT, "null scene or params");
-    if (pach_status st = check_room(sources, n_sources, receivers, n_receivers, "")) return st;
-    if (n_receivers > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers per run");
-    const pach_trace_params &p = *params;
-    if (p.ray_count < 1 || p.ray_begin < 0 || p.ray_begin + p.ray_count > (1ll << 32))
-        return fail(PACH_ERR_INVALID_ARGUMENT,
-                    "ray_count must be >= 1 and ray_begin + ray_count <= 2^32 (convergence mode is not supported)");
-    if (pach_status st = check_common(p)) return st;
-    if (!(p.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, "cutoff_length_m must be positive");
-    if (p.proposal) {
-        if (p.n_proposal < 1 || p.n_proposal > 256)
-            return fail(PACH_ERR_INVALID_ARGUMENT, "n_proposal must be 1..256 when proposal is given");
-        if (p.prim_dirs) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal and prim_dirs exclude each other");
-        if (p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "capture records uniform-emission runs only");
-        if (!(p.proposal_mix >= 0 && p.proposal_mix <= 1))
-            return fail(PACH_ERR_INVALID_ARGUMENT, "proposal_mix must lie in [0, 1] (0 = default)");
-        for (long long i = 0; i < (long long)p.n_proposal * PACH_MLP_OUT; ++i)
-            if (!std::isfinite(p.proposal[i])) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal holds a non-finite value");
-    }
-    if (p.capture && (p.capture < 0 || p.capture > 2 || n_receivers < 1))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0, 1 or 2 and needs receivers");
-    if (p.capture == 2 && (double)p.ray_count * n_receivers * kCaptureWindows * 4 > 16e9)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "per-primary capture larger than 16 GB");
-    std::unique_ptr<pach_run> run(new pach_run());
-    run->scene = scene;
-    run->p = p;
-    if (p.map) {
+    return guarded([&]() -> pach_status {
+        if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
+        *out = nullptr;
+        if (!scene || !params) return fail(PACH_ERR_INVALID_ARGUMENT, "null scene or params");
+        if (pach_status st = check_room(sources, n_sources, receivers, n_receivers, "")) return st;
+        if (n_receivers > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers per run");
+        const pach_trace_params &p = *params;
+        if (p.ray_count < 1 || p.ray_begin < 0 || p.ray_begin + p.ray_count > (1ll << 32))
+            return fail(PACH_ERR_INVALID_ARGUMENT,
+                        "ray_count must be >= 1 and ray_begin + ray_count <= 2^32 (convergence mode is not supported)");
+        if (pach_status st = check_common(p)) return st;
+        if (!(p.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, "cutoff_length_m must be positive");
+        if (p.proposal) {
+            if (p.n_proposal < 1 || p.n_proposal > 256)
+                return fail(PACH_ERR_INVALID_ARGUMENT, "n_proposal must be 1..256 when proposal is given");
+            if (p.prim_dirs) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal and prim_dirs exclude each other");
+            if (p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "capture records uniform-emission runs only");
+            if (!(p.proposal_mix >= 0 && p.proposal_mix <= 1))
+                return fail(PACH_ERR_INVALID_ARGUMENT, "proposal_mix must lie in [0, 1] (0 = default)");
+            for (long long i = 0; i < (long long)p.n_proposal * PACH_MLP_OUT; ++i)
+                if (!std::isfinite(p.proposal[i])) return fail(PACH_ERR_INVALID_ARGUMENT, "proposal holds a non-finite value");
+        }
+        if (p.capture && (p.capture < 0 || p.capture > 2 || n_receivers < 1))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "capture must be 0, 1 or 2 and needs receivers");
+        if (p.capture == 2 && (double)p.ray_count * n_receivers * kCaptureWindows * 4 > 16e9)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "per-primary capture larger than 16 GB");
+        std::unique_ptr<pach_run> run(new pach_run());
+        run->scene = scene;
+        run->p = p;
+        if (p.map) {
+            std::string err;
+            if (!build_map_grid(*p.map, sources[0].origin, n_sources, scene->hs.c, run->mg, err))
+                return fail(PACH_ERR_INVALID_ARGUMENT, err);
+            if ((double)run->mg.M * kBands * run->mg.T * 16 > 200e9)
+                return fail(PACH_ERR_INVALID_ARGUMENT, "map histograms larger than 200 GB");
+            run->map_org.assign(p.map->origins, p.map->origins + 3 * (size_t)p.map->n_receivers);
+            run->has_map = true;
+        }
+        run->p.map = nullptr;
+        if (p.proposal) proposal_lobes(p.proposal, p.n_proposal, run->prop);
+        if (p.prim_dirs) run->prim_dirs.assign(p.prim_dirs, p.prim_dirs + 3 * p.ray_count);
+        if (p.prim_weights) run->prim_weights.assign(p.prim_weights, p.prim_weights + p.ray_count);
+        run->p.proposal = nullptr;
+        run->p.prim_dirs = nullptr;
+        run->p.prim_weights = nullptr;
+        RoomSpec rm;
+        rm.scene = scene;
+        rm.src.assign(sources, sources + n_sources);
+        rm.rec.assign(receivers, receivers + n_receivers);
+        rm.rays = p.ray_count;
+        rm.prim_begin = p.ray_begin;
+        rm.cutoff_len = p.cutoff_length_m;  // TaskAll:83 -- the ctor's cutoff argument is a length
         std::string err;
-        if (!build_map_grid(*p.map, sources[0].origin, n_sources, scene->hs.c, run->mg, err))
-            return fail(PACH_ERR_INVALID_ARGUMENT, err);
-        if ((double)run->mg.M * kBands * run->mg.T * 16 > 200e9)
-            return fail(PACH_ERR_INVALID_ARGUMENT, "map histograms larger than 200 GB");
-        run->map_org.assign(p.map->origins, p.map->origins + 3 * (size_t)p.map->n_receivers);
-        run->has_map = true;
-    }
-    run->p.map = nullptr;
-    if (p.proposal) proposal_lobes(p.proposal, p.n_proposal, run->prop);
-    if (p.prim_dirs) run->prim_dirs.assign(p.prim_dirs, p.prim_dirs + 3 * p.ray_count);
-    if (p.prim_weights) run->prim_weights.assign(p.prim_weights, p.prim_weights + p.ray_count);
-    run->p.proposal = nullptr;
-    run->p.prim_dirs = nullptr;
-    run->p.prim_weights = nullptr;
-    RoomSpec rm;
-    rm.scene = scene;
-    rm.src.assign(sources, sources + n_sources);
-    rm.rec.assign(receivers, receivers + n_receivers);
-    rm.rays = p.ray_count;
-    rm.prim_begin = p.ray_begin;
-    rm.cutoff_len = p.cutoff_length_m;  // TaskAll:83 -- the ctor's cutoff argument is a length
-    std::string err;
-    if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
-    run->rooms.push_back(std::move(rm));
-    run->R = n_receivers;
-    run->nsrc = n_sources;
-    run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
-    run->worker = std::thread(run_worker, run.get());
-    *out = run.release();
-    return PACH_OK;
+        if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
+        run->rooms.push_back(std::move(rm));
+        run->R = n_receivers;
+        run->nsrc = n_sources;
+        run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
+        run->worker = std::thread(run_worker, run.get());
+        *out = run.release();
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_batch_begin(const pach_room_desc *rooms, int32_t n_rooms, const pach_trace_params *params,
                              pach_run **out) {
-    if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
-    *out = nullptr;
-    if (!rooms || !params || n_rooms < 1 || n_rooms > kMaxRooms)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "need 1.." + std::to_string(kMaxRooms) + " rooms and params");
-    const pach_trace_params &p = *params;
-    if (pach_status st = check_common(p)) return st;
-    if (p.proposal || p.prim_dirs || p.prim_weights)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "a batch emits from its sources: no proposal or emission overrides");
-    if (p.map) return fail(PACH_ERR_INVALID_ARGUMENT, "mapping receivers need a single-room run (pach_trace_begin)");
-    if (p.ray_begin < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin must be >= 0");
-    std::unique_ptr<pach_run> run(new pach_run());
-    run->p = p;
-    run->p.map = nullptr;
-    long long prim = p.ray_begin;
-    int R = 0, nsrc = 0;
-    for (int i = 0; i < n_rooms; ++i) {
-        const pach_room_desc &d = rooms[i];
-        const std::string who = "room " + std::to_string(i) + ": ";
-        if (!d.scene) return fail(PACH_ERR_INVALID_ARGUMENT, who + "null scene");
-        if (d.scene->device != rooms[0].scene->device) return fail(PACH_ERR_INVALID_ARGUMENT, who + "scenes on different devices");
-        if (pach_status st = check_room(d.sources, d.n_sources, d.receivers, d.n_receivers, who)) return st;
-        if (d.ray_count < 1) return fail(PACH_ERR_INVALID_ARGUMENT, who + "ray_count must be >= 1");
-        if (!(d.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, who + "cutoff_length_m must be positive");
-        RoomSpec rm;
-        rm.scene = const_cast<pach_scene *>(d.scene);
-        rm.src.assign(d.sources, d.sources + d.n_sources);
-        rm.rec.assign(d.receivers, d.receivers + d.n_receivers);
-        rm.rays = d.ray_count;
-        rm.prim_begin = prim;
-        rm.cutoff_len = d.cutoff_length_m;
-        std::string err;
-        if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, who + err);
-        prim += d.ray_count;
-        R += d.n_receivers;
-        nsrc += d.n_sources;
-        run->rooms.push_back(std::move(rm));
-    }
-    if (prim > (1ll << 32)) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin + the rooms' rays must be <= 2^32");
-    if (R > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers over the rooms of a batch");
-    if (p.capture && (p.capture != 1 || R < 1))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "a batch captures per direction bin only (capture 1) and needs receivers");
-    run->scene = run->rooms[0].scene;
-    run->p.ray_count = prim - p.ray_begin;
-    run->p.cutoff_length_m = run->rooms[0].cutoff_len;
-    run->R = R;
-    run->nsrc = nsrc;
-    run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
-    run->worker = std::thread(run_worker, run.get());
-    *out = run.release();
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!out) return fail(PACH_ERR_INVALID_ARGUMENT, "out is null");
+        *out = nullptr;
+        if (!rooms || !params || n_rooms < 1 || n_rooms > kMaxRooms)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "need 1.." + std::to_string(kMaxRooms) + " rooms and params");
+        const pach_trace_params &p = *params;
+        if (pach_status st = check_common(p)) return st;
+        if (p.proposal || p.prim_dirs || p.prim_weights)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "a batch emits from its sources: no proposal or emission overrides");
+        if (p.map) return fail(PACH_ERR_INVALID_ARGUMENT, "mapping receivers need a single-room run (pach_trace_begin)");
+        if (p.ray_begin < 0) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin must be >= 0");
+        std::unique_ptr<pach_run> run(new pach_run());
+        run->p = p;
+        run->p.map = nullptr;
+        long long prim = p.ray_begin;
+        int R = 0, nsrc = 0;
+        for (int i = 0; i < n_rooms; ++i) {
+            const pach_room_desc &d = rooms[i];
+            const std::string who = "room " + std::to_string(i) + ": ";
+            if (!d.scene) return fail(PACH_ERR_INVALID_ARGUMENT, who + "null scene");
+            if (d.scene->device != rooms[0].scene->device) return fail(PACH_ERR_INVALID_ARGUMENT, who + "scenes on different devices");
+            if (pach_status st = check_room(d.sources, d.n_sources, d.receivers, d.n_receivers, who)) return st;
+            if (d.ray_count < 1) return fail(PACH_ERR_INVALID_ARGUMENT, who + "ray_count must be >= 1");
+            if (!(d.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, who + "cutoff_length_m must be positive");
+            RoomSpec rm;
+            rm.scene = const_cast<pach_scene *>(d.scene);
+            rm.src.assign(d.sources, d.sources + d.n_sources);
+            rm.rec.assign(d.receivers, d.receivers + d.n_receivers);
+            rm.rays = d.ray_count;
+            rm.prim_begin = prim;
+            rm.cutoff_len = d.cutoff_length_m;
+            std::string err;
+            if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, who + err);
+            prim += d.ray_count;
+            R += d.n_receivers;
+            nsrc += d.n_sources;
+            run->rooms.push_back(std::move(rm));
+        }
+        if (prim > (1ll << 32)) return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin + the rooms' rays must be <= 2^32");
+        if (R > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers over the rooms of a batch");
+        if (p.capture && (p.capture != 1 || R < 1))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "a batch captures per direction bin only (capture 1) and needs receivers");
+        run->scene = run->rooms[0].scene;
+        run->p.ray_count = prim - p.ray_begin;
+        run->p.cutoff_length_m = run->rooms[0].cutoff_len;
+        run->R = R;
+        run->nsrc = nsrc;
+        run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
+        run->worker = std::thread(run_worker, run.get());
+        *out = run.release();
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_poll(pach_run *run, pach_progress *pr) {
-    if (pach_status s = check_run(run)) return s;
-    if (!pr) return fail(PACH_ERR_INVALID_ARGUMENT, "progress is null");
-    pr->state = run->state.load();
-    {
-        std::lock_guard<std::mutex> lk(run->mu);
-        pr->last_status = run->status;
-    }
-    pr->rays_done = run->rays_done.load();
-    pr->rays_total = run->p.ray_count;
-    pr->end_traces = run->end_traces.load();
-    pr->segments = run->segments.load();
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        if (!pr) return fail(PACH_ERR_INVALID_ARGUMENT, "progress is null");
+        pr->state = run->state.load();
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            pr->last_status = run->status;
+        }
+        pr->rays_done = run->rays_done.load();
+        pr->rays_total = run->p.ray_count;
+        pr->end_traces = run->end_traces.load();
+        pr->segments = run->segments.load();
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_cancel(pach_run *run) {
-    if (pach_status s = check_run(run)) return s;
-    run->cancel = true;
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        run->cancel = true;
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_wait(pach_run *run, int64_t timeout_ms) {
-    if (pach_status s = check_run(run)) return s;
-    std::unique_lock<std::mutex> lk(run->mu);
-    if (timeout_ms < 0) {
-        run->cv.wait(lk, [&] { return run->finished; });
-    } else if (!run->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return run->finished; })) {
-        return fail(PACH_ERR_TIMEOUT, "run still in progress");
-    }
-    lk.unlock();
-    if (run->worker.joinable()) run->worker.join();
-    if (run->status != PACH_OK) return fail(run->status, run->err);
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        std::unique_lock<std::mutex> lk(run->mu);
+        if (timeout_ms < 0) {
+            run->cv.wait(lk, [&] { return run->finished; });
+        } else if (!run->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return run->finished; })) {
+            return fail(PACH_ERR_TIMEOUT, "run still in progress");
+        }
+        lk.unlock();
+        if (run->worker.joinable()) run->worker.join();
+        if (run->status != PACH_OK) return fail(run->status, run->err);
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_get_histograms(pach_run *run, int32_t scaled, double *energy, double *pressure, double *dir_pos,
                                       double *dir_neg, double *analysis, size_t cap_bins) {
-    if (pach_status s = check_run(run)) return s;
-    {
-        std::lock_guard<std::mutex> lk(run->mu);
-        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
-        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
-    }
-    const size_t nE = (size_t)run->R * kBands * run->T, nD = nE * 3;
-    if (cap_bins < nE) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < receivers * 8 * bins");
-    cudaSetDevice(run->scene->device);
-    struct Item { double *dst; DevMem *src; size_t n; int lanes; bool pressure; };
-    const Item items[5] = {{energy, &run->hE, nE, 1, false}, {pressure, &run->hP, nE, 1, true},
-                           {dir_pos, &run->hDp, nD, 3, false}, {dir_neg, &run->hDn, nD, 3, false},
-                           {analysis, &run->hAn, nD, 3, false}};
-    const long long done = run->rays_done.load();
-    for (const Item &it : items) {
-        if (!it.dst || it.n == 0) continue;
-        cudaError_t e = cudaMemcpy(it.dst, it.src->p, it.n * sizeof(double), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "histogram copy"));
-        if (!scaled) continue;
-        // Receiver_Bank.Scale(N) then, for a cluster, Scale(1/n_sources) (TaskAll:770-771), with N the
-        // primaries the receiver's room completed (rooms are fed in order)
-        const size_t per_rec = (size_t)it.lanes * kBands * run->T;
-        double *dst = it.dst;
-        for (const RoomSpec &rm : run->rooms) {
-            const long long off = rm.prim_begin - run->rooms[0].prim_begin;
-            const double N = (double)std::max(1ll, std::min(rm.rays, done - off));
-            const double ns = (double)rm.src.size();
-            const double f = it.pressure ? std::sqrt(ns) / std::sqrt(N) : ns / N;
-            for (size_t i = 0; i < rm.rec.size() * per_rec; ++i) dst[i] *= f;
-            dst += rm.rec.size() * per_rec;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+            if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
         }
-    }
-    return PACH_OK;
+        const size_t nE = (size_t)run->R * kBands * run->T, nD = nE * 3;
+        if (cap_bins < nE) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < receivers * 8 * bins");
+        cudaSetDevice(run->scene->device);
+        struct Item { double *dst; DevMem *src; size_t n; int lanes; bool pressure; };
+        const Item items[5] = {{energy, &run->hE, nE, 1, false}, {pressure, &run->hP, nE, 1, true},
+                               {dir_pos, &run->hDp, nD, 3, false}, {dir_neg, &run->hDn, nD, 3, false},
+                               {analysis, &run->hAn, nD, 3, false}};
+        const long long done = run->rays_done.load();
+        for (const Item &it : items) {
+            if (!it.dst || it.n == 0) continue;
+            cudaError_t e = cudaMemcpy(it.dst, it.src->p, it.n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "histogram copy"));
+            if (!scaled) continue;
+            // Receiver_Bank.Scale(N) then, for a cluster, Scale(1/n_sources) (TaskAll:770-771), with N the
+            // primaries the receiver's room completed (rooms are fed in order)
+            const size_t per_rec = (size_t)it.lanes * kBands * run->T;
+            double *dst = it.dst;
+            for (const RoomSpec &rm : run->rooms) {
+                const long long off = rm.prim_begin - run->rooms[0].prim_begin;
+                const double N = (double)std::max(1ll, std::min(rm.rays, done - off));
+                const double ns = (double)rm.src.size();
+                const double f = it.pressure ? std::sqrt(ns) / std::sqrt(N) : ns / N;
+                for (size_t i = 0; i < rm.rec.size() * per_rec; ++i) dst[i] *= f;
+                dst += rm.rec.size() * per_rec;
+            }
+        }
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_get_capture(pach_run *run, float *out, size_t cap) {
-    if (pach_status s = check_run(run)) return s;
-    {
-        std::lock_guard<std::mutex> lk(run->mu);
-        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
-        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
-    }
-    if (!run->p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "the run was made without capture");
-    const size_t per = run->p.capture == 2 ? (size_t)rprim_total(run) : (size_t)kDirBins;
-    const size_t n = (size_t)run->R * kCaptureWindows * per;
-    if (!out || cap < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap < receivers * 4 * (1536 bins or primaries)");
-    cudaSetDevice(run->scene->device);
-    cudaError_t e = cudaMemcpy(out, run->dcap.p, n * sizeof(float), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "capture copy"));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+            if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+        }
+        if (!run->p.capture) return fail(PACH_ERR_INVALID_ARGUMENT, "the run was made without capture");
+        const size_t per = run->p.capture == 2 ? (size_t)rprim_total(run) : (size_t)kDirBins;
+        const size_t n = (size_t)run->R * kCaptureWindows * per;
+        if (!out || cap < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap < receivers * 4 * (1536 bins or primaries)");
+        cudaSetDevice(run->scene->device);
+        cudaError_t e = cudaMemcpy(out, run->dcap.p, n * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "capture copy"));
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_get_map(pach_run *run, int32_t scaled, double *energy, double *pressure, double *direct_time,
                                int32_t *sizes, size_t cap_bins) {
-    if (pach_status s = check_run(run)) return s;
-    if (!run->has_map) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no mapping receivers");
-    const MapGrid &g = run->mg;
-    if (sizes) { sizes[0] = g.M; sizes[1] = g.T; }
-    if (direct_time) std::memcpy(direct_time, g.direct.data(), g.direct.size() * sizeof(double));
-    if (!energy && !pressure) return PACH_OK;
-    {
-        std::lock_guard<std::mutex> lk(run->mu);
-        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
-        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
-    }
-    const size_t n = (size_t)g.M * kBands * g.T;
-    if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 8 * bins");
-    cudaSetDevice(run->scene->device);
-    // Histogram.Scale(N) divides energy and pressure by N (Directional_Histogram.Scale: pressure by
-    // sqrt(N)); a cluster's Scale(1 / n_sources) multiplies back
-    const double N = (double)std::max(1ll, run->rays_done.load());
-    const double f = (double)run->nsrc / N;
-    const double fp = g.directional ? std::sqrt((double)run->nsrc / N) : f;
-    for (auto [dst, src, k] : {std::tuple<double *, DevMem *, double>{energy, &run->mE, f}, {pressure, &run->mP, fp}}) {
-        if (!dst) continue;
-        cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map copy"));
-        if (scaled)
-            for (size_t i = 0; i < n; ++i) dst[i] *= k;
-    }
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        if (!run->has_map) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no mapping receivers");
+        const MapGrid &g = run->mg;
+        if (sizes) { sizes[0] = g.M; sizes[1] = g.T; }
+        if (direct_time) std::memcpy(direct_time, g.direct.data(), g.direct.size() * sizeof(double));
+        if (!energy && !pressure) return PACH_OK;
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+            if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+        }
+        const size_t n = (size_t)g.M * kBands * g.T;
+        if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 8 * bins");
+        cudaSetDevice(run->scene->device);
+        // Histogram.Scale(N) divides energy and pressure by N (Directional_Histogram.Scale: pressure by
+        // sqrt(N)); a cluster's Scale(1 / n_sources) multiplies back
+        const double N = (double)std::max(1ll, run->rays_done.load());
+        const double f = (double)run->nsrc / N;
+        const double fp = g.directional ? std::sqrt((double)run->nsrc / N) : f;
+        for (auto [dst, src, k] : {std::tuple<double *, DevMem *, double>{energy, &run->mE, f}, {pressure, &run->mP, fp}}) {
+            if (!dst) continue;
+            cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map copy"));
+            if (scaled)
+                for (size_t i = 0; i < n; ++i) dst[i] *= k;
+        }
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_get_map_directions(pach_run *run, int32_t scaled, double *dir_pos, double *dir_neg,
                                           size_t cap_bins) {
-    if (pach_status s = check_run(run)) return s;
-    if (!run->has_map || !run->mg.directional) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no directional map");
-    {
-        std::lock_guard<std::mutex> lk(run->mu);
-        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
-        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
-    }
-    const MapGrid &g = run->mg;
-    const size_t n = (size_t)g.M * 3 * kBands * g.T;
-    if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 3 * 8 * bins");
-    cudaSetDevice(run->scene->device);
-    const double f = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
-    for (auto [dst, src] : {std::pair<double *, DevMem *>{dir_pos, &run->mDp}, {dir_neg, &run->mDn}}) {
-        if (!dst) continue;
-        cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map direction copy"));
-        if (scaled)
-            for (size_t i = 0; i < n; ++i) dst[i] *= f;
-    }
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        if (!run->has_map || !run->mg.directional) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no directional map");
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+            if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+        }
+        const MapGrid &g = run->mg;
+        const size_t n = (size_t)g.M * 3 * kBands * g.T;
+        if (cap_bins < n) return fail(PACH_ERR_INVALID_ARGUMENT, "cap_bins < map receivers * 3 * 8 * bins");
+        cudaSetDevice(run->scene->device);
+        const double f = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
+        for (auto [dst, src] : {std::pair<double *, DevMem *>{dir_pos, &run->mDp}, {dir_neg, &run->mDn}}) {
+            if (!dst) continue;
+            cudaError_t e = cudaMemcpy(dst, src->p, n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "map direction copy"));
+            if (scaled)
+                for (size_t i = 0; i < n; ++i) dst[i] *= f;
+        }
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_map_parameters(pach_run *run, int32_t decay_depth, int32_t clarity_ms, double *t_x, double *edt,
                                 double *clarity, double *definition, double *energy_sum) {
-    if (pach_status s = check_run(run)) return s;
-    if (!run->has_map) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no mapping receivers");
-    {
-        std::lock_guard<std::mutex> lk(run->mu);
-        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
-        if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
-    }
-    const MapGrid &g = run->mg;
-    const int n = g.M * kBands;
-    cudaSetDevice(run->scene->device);
-    DevMem out;
-    struct Release {
-        DevMem &m;
-        ~Release() { m.release(); }
-    } release_out{out};
-    cudaError_t e = out.alloc((size_t)5 * n * sizeof(double));
-    if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "parameter map buffers"));
-    double *d = out.as<double>();
-    const double scale = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
-    e = launch_map_params(run->mE.as<double>(), n, g.T, 1000.0, scale, decay_depth, clarity_ms / 1000.0, d, d + n,
-                          d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map kernel"));
-    double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
-    for (int i = 0; i < 5; ++i) {
-        if (!dst[i]) continue;
-        e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map copy"));
-    }
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        if (!run->has_map) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no mapping receivers");
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+            if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+        }
+        const MapGrid &g = run->mg;
+        const int n = g.M * kBands;
+        cudaSetDevice(run->scene->device);
+        DevMem out;
+        struct Release {
+            DevMem &m;
+            ~Release() { m.release(); }
+        } release_out{out};
+        cudaError_t e = out.alloc((size_t)5 * n * sizeof(double));
+        if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "parameter map buffers"));
+        double *d = out.as<double>();
+        const double scale = (double)run->nsrc / (double)std::max(1ll, run->rays_done.load());
+        e = launch_map_params(run->mE.as<double>(), n, g.T, 1000.0, scale, decay_depth, clarity_ms / 1000.0, d, d + n,
+                              d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map kernel"));
+        double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
+        for (int i = 0; i < 5; ++i) {
+            if (!dst[i]) continue;
+            e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "parameter map copy"));
+        }
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_etc_parameters(const double *etc, int32_t n, int32_t T, int32_t sample_rate, int32_t decay_depth,
                                 double clarity_s, double *t_x, double *edt, double *clarity, double *definition,
                                 double *energy_sum) {
-    if (n < 0 || T < 1 || sample_rate < 1 || (n > 0 && !etc))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "etc_parameters: need n >= 0 curves of T >= 1 bins at a positive rate");
-    if (n == 0) return PACH_OK;
-    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
-    DevMem in, out;
-    struct Release {
-        DevMem &a, &b;
-        ~Release() { a.release(); b.release(); }
-    } release_bufs{in, out};
-    const size_t bytes = (size_t)n * T * sizeof(double);
-    cudaError_t e = upload(in, etc, bytes);
-    if (e == cudaSuccess) e = out.alloc((size_t)5 * n * sizeof(double));
-    if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "etc_parameters buffers"));
-    double *d = out.as<double>();
-    e = launch_map_params(in.as<double>(), n, T, (double)sample_rate, 1.0, decay_depth, clarity_s, d, d + n,
-                          d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "etc_parameters kernel"));
-    double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
-    for (int i = 0; i < 5; ++i) {
-        if (!dst[i]) continue;
-        e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "etc_parameters copy"));
-    }
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (n < 0 || T < 1 || sample_rate < 1 || (n > 0 && !etc))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "etc_parameters: need n >= 0 curves of T >= 1 bins at a positive rate");
+        if (n == 0) return PACH_OK;
+        if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
+        DevMem in, out;
+        struct Release {
+            DevMem &a, &b;
+            ~Release() { a.release(); b.release(); }
+        } release_bufs{in, out};
+        const size_t bytes = (size_t)n * T * sizeof(double);
+        cudaError_t e = upload(in, etc, bytes);
+        if (e == cudaSuccess) e = out.alloc((size_t)5 * n * sizeof(double));
+        if (e != cudaSuccess) return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "etc_parameters buffers"));
+        double *d = out.as<double>();
+        e = launch_map_params(in.as<double>(), n, T, (double)sample_rate, 1.0, decay_depth, clarity_s, d, d + n,
+                              d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, nullptr);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "etc_parameters kernel"));
+        double *dst[5] = {t_x, edt, clarity, definition, energy_sum};
+        for (int i = 0; i < 5; ++i) {
+            if (!dst[i]) continue;
+            e = cudaMemcpy(dst[i], d + (size_t)i * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return fail(PACH_ERR_CUDA, cuda_msg(e, "etc_parameters copy"));
+        }
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_trace_get_stats(pach_run *run, pach_stats *stats) {
-    if (pach_status s = check_run(run)) return s;
-    if (!stats) return fail(PACH_ERR_INVALID_ARGUMENT, "stats is null");
-    std::lock_guard<std::mutex> lk(run->mu);
-    if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
-    *stats = run->stats;
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        if (!stats) return fail(PACH_ERR_INVALID_ARGUMENT, "stats is null");
+        std::lock_guard<std::mutex> lk(run->mu);
+        if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+        *stats = run->stats;
+        return PACH_OK;
+    }, fail);
 }
 
 void pach_run_destroy(pach_run *run) { delete run; }
@@ -1303,90 +1362,98 @@ pach_status pach_trace_run(pach_scene *scene, const pach_source_desc *sources, i
                            const pach_receiver_desc *receivers, int32_t n_receivers, const pach_trace_params *params,
                            int32_t scaled, double *energy, double *pressure, double *dir_pos, double *dir_neg,
                            double *analysis, size_t cap_bins, pach_stats *stats) {
-    pach_run *run = nullptr;
-    pach_status s = pach_trace_begin(scene, sources, n_sources, receivers, n_receivers, params, &run);
-    if (s) return s;
-    s = pach_trace_wait(run, -1);
-    if (!s) s = pach_trace_get_histograms(run, scaled, energy, pressure, dir_pos, dir_neg, analysis, cap_bins);
-    if (!s && stats) s = pach_trace_get_stats(run, stats);
-    std::string keep = g_err;
-    pach_run_destroy(run);
-    g_err = keep;
-    return s;
+    return guarded([&]() -> pach_status {
+        pach_run *run = nullptr;
+        pach_status s = pach_trace_begin(scene, sources, n_sources, receivers, n_receivers, params, &run);
+        if (s) return s;
+        s = pach_trace_wait(run, -1);
+        if (!s) s = pach_trace_get_histograms(run, scaled, energy, pressure, dir_pos, dir_neg, analysis, cap_bins);
+        if (!s && stats) s = pach_trace_get_stats(run, stats);
+        std::string keep = g_err;
+        pach_run_destroy(run);
+        g_err = keep;
+        return s;
+    }, fail);
 }
 
 pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double *origins, const double *dirs,
                                       int32_t max_bounces, int32_t *poly_out, double *t_out, double *pts_out) {
-    if (!scene || n < 0 || max_bounces < 1 || !origins || !dirs || !poly_out || !t_out || !pts_out)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    if (n == 0) return PACH_OK;
-    cudaSetDevice(scene->device);
-    DevMem o, d, pl, t, pt;
-    const size_t k = (size_t)n * max_bounces;
-    cudaError_t e;
-    if ((e = upload(o, origins, sizeof(double) * 3 * n)) || (e = upload(d, dirs, sizeof(double) * 3 * n)) ||
-        (e = pl.alloc(sizeof(int32_t) * k)) || (e = t.alloc(sizeof(double) * k)) || (e = pt.alloc(sizeof(double) * 3 * k)) ||
-        (e = launch_paths(scene->dev, n, o.as<double>(), d.as<double>(), max_bounces, pl.as<int>(), t.as<double>(),
-                          pt.as<double>(), 0)) ||
-        (e = cudaMemcpy(poly_out, pl.p, sizeof(int32_t) * k, cudaMemcpyDeviceToHost)) ||
-        (e = cudaMemcpy(t_out, t.p, sizeof(double) * k, cudaMemcpyDeviceToHost)) ||
-        (e = cudaMemcpy(pts_out, pt.p, sizeof(double) * 3 * k, cudaMemcpyDeviceToHost)))
-        return fail(PACH_ERR_CUDA, cuda_msg(e, "specular paths"));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!scene || n < 0 || max_bounces < 1 || !origins || !dirs || !poly_out || !t_out || !pts_out)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        if (n == 0) return PACH_OK;
+        cudaSetDevice(scene->device);
+        DevMem o, d, pl, t, pt;
+        const size_t k = (size_t)n * max_bounces;
+        cudaError_t e;
+        if ((e = upload(o, origins, sizeof(double) * 3 * n)) || (e = upload(d, dirs, sizeof(double) * 3 * n)) ||
+            (e = pl.alloc(sizeof(int32_t) * k)) || (e = t.alloc(sizeof(double) * k)) || (e = pt.alloc(sizeof(double) * 3 * k)) ||
+            (e = launch_paths(scene->dev, n, o.as<double>(), d.as<double>(), max_bounces, pl.as<int>(), t.as<double>(),
+                              pt.as<double>(), 0)) ||
+            (e = cudaMemcpy(poly_out, pl.p, sizeof(int32_t) * k, cudaMemcpyDeviceToHost)) ||
+            (e = cudaMemcpy(t_out, t.p, sizeof(double) * k, cudaMemcpyDeviceToHost)) ||
+            (e = cudaMemcpy(pts_out, pt.p, sizeof(double) * 3 * k, cudaMemcpyDeviceToHost)))
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "specular paths"));
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_scene_shoot_host(const pach_scene_desc *desc, int32_t n, const double *origins, const double *dirs,
                                   int32_t *poly_out, double *t_out) {
-    if (n < 0 || (n > 0 && (!origins || !dirs || !poly_out || !t_out))) return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    HostScene hs;
-    std::string err;
-    if (!build_host_scene(desc, hs, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
-    for (int i = 0; i < n; ++i) {
-        const double o[3] = {origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]};
-        double d[3] = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
-        const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        for (double &x : d) x /= l;
-        int tri = -1;
-        double t = 0;
-        if (bvh_shoot_host(hs, o, d, 1e-10, tri, t)) {
-            poly_out[i] = hs.tri_poly[tri];
-            t_out[i] = t;
-        } else {
-            poly_out[i] = -1;
-            t_out[i] = 0;
+    return guarded([&]() -> pach_status {
+        if (n < 0 || (n > 0 && (!origins || !dirs || !poly_out || !t_out))) return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        HostScene hs;
+        std::string err;
+        if (!build_host_scene(desc, hs, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
+        for (int i = 0; i < n; ++i) {
+            const double o[3] = {origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]};
+            double d[3] = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+            const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            for (double &x : d) x /= l;
+            int tri = -1;
+            double t = 0;
+            if (bvh_shoot_host(hs, o, d, 1e-10, tri, t)) {
+                poly_out[i] = hs.tri_poly[tri];
+                t_out[i] = t;
+            } else {
+                poly_out[i] = -1;
+                t_out[i] = 0;
+            }
         }
-    }
-    return PACH_OK;
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, int32_t n_sources, int32_t kind,
                                  double *dirs_out) {
-    if (n < 0 || n_sources < 1 || n_sources > kMaxSources || kind < 0 || kind > 2 || !dirs_out)
-        return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    if (n == 0) return PACH_OK;
-    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
-    std::vector<float4> src(n_sources, make_float4(0, 0, 0, (float)kind));
-    std::vector<double> gf;
-    geodesic_faces(gf);
-    std::vector<float4> geo(kGeoFaces * 3);
-    for (int i = 0; i < kGeoFaces * 3; ++i) geo[i] = make_float4((float)gf[3 * i], (float)gf[3 * i + 1], (float)gf[3 * i + 2], 0.f);
-    DevMem ds, dg, dout, droom;
-    cudaError_t e;
-    DevRun r{};
-    r.seed = seed;
-    RoomParams room{};
-    room.nsrc = n_sources;
-    if ((e = upload(ds, src.data(), src.size() * sizeof(float4))) || (e = upload(dg, geo.data(), geo.size() * sizeof(float4))) ||
-        (e = upload(droom, &room, sizeof(room))) || (e = dout.alloc(sizeof(double) * 3 * n)))
-        return fail(PACH_ERR_CUDA, cuda_msg(e, "emit setup"));
-    r.src = ds.as<float4>();
-    r.geo = dg.as<float4>();
-    r.rooms = droom.as<RoomParams>();
-    r.n_rooms = 1;
-    if ((e = launch_emit(r, ray_begin, n, dout.as<double>(), 0)) ||
-        (e = cudaMemcpy(dirs_out, dout.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost)))
-        return fail(PACH_ERR_CUDA, cuda_msg(e, "emit"));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (n < 0 || n_sources < 1 || n_sources > kMaxSources || kind < 0 || kind > 2 || !dirs_out)
+            return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        if (n == 0) return PACH_OK;
+        if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
+        std::vector<float4> src(n_sources, make_float4(0, 0, 0, (float)kind));
+        std::vector<double> gf;
+        geodesic_faces(gf);
+        std::vector<float4> geo(kGeoFaces * 3);
+        for (int i = 0; i < kGeoFaces * 3; ++i) geo[i] = make_float4((float)gf[3 * i], (float)gf[3 * i + 1], (float)gf[3 * i + 2], 0.f);
+        DevMem ds, dg, dout, droom;
+        cudaError_t e;
+        DevRun r{};
+        r.seed = seed;
+        RoomParams room{};
+        room.nsrc = n_sources;
+        if ((e = upload(ds, src.data(), src.size() * sizeof(float4))) || (e = upload(dg, geo.data(), geo.size() * sizeof(float4))) ||
+            (e = upload(droom, &room, sizeof(room))) || (e = dout.alloc(sizeof(double) * 3 * n)))
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "emit setup"));
+        r.src = ds.as<float4>();
+        r.geo = dg.as<float4>();
+        r.rooms = droom.as<RoomParams>();
+        r.n_rooms = 1;
+        if ((e = launch_emit(r, ray_begin, n, dout.as<double>(), 0)) ||
+            (e = cudaMemcpy(dirs_out, dout.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost)))
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "emit"));
+        return PACH_OK;
+    }, fail);
 }
 
 int32_t pach_direction_bin(double x, double y, double z) { return dir_bin((float)x, (float)y, (float)z); }
@@ -1394,69 +1461,73 @@ int32_t pach_direction_bin(double x, double y, double z) { return dir_bin((float
 pach_status pach_direct_sound(pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
                               const pach_receiver_desc *receivers, int32_t n_receivers, int32_t *valid,
                               double *distance, double *energy) {
-    if (!scene || !sources || n_sources < 1 || n_receivers < 0 || (n_receivers > 0 && (!receivers || !valid)))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    if ((long long)n_sources * n_receivers > (1ll << 30)) return fail(PACH_ERR_INVALID_ARGUMENT, "too many pairs");
-    if (n_receivers == 0) return PACH_OK;
-    cudaSetDevice(scene->device);
-    const HostScene &hs = scene->hs;
-    std::vector<double> s3(3 * (size_t)n_sources), r3(3 * (size_t)n_receivers);
-    for (int s = 0; s < n_sources; ++s)
-        for (int a = 0; a < 3; ++a) s3[3 * s + a] = sources[s].origin[a];
-    for (int k = 0; k < n_receivers; ++k)
-        for (int a = 0; a < 3; ++a) r3[3 * k + a] = receivers[k].origin[a];
-    const size_t npair = (size_t)n_sources * n_receivers;
-    DevMem ds, dr, dv, dt;
-    std::vector<int> v(npair);
-    std::vector<double> tm(npair * kBands);
-    cudaError_t e;
-    if ((e = upload(ds, s3.data(), s3.size() * sizeof(double))) || (e = upload(dr, r3.data(), r3.size() * sizeof(double))) ||
-        (e = dv.alloc(npair * sizeof(int))) || (e = dt.alloc(npair * kBands * sizeof(double))) ||
-        (e = launch_direct(scene->dev, ds.as<double>(), n_sources, dr.as<double>(), n_receivers, 64, dv.as<int>(),
-                           dt.as<double>(), 0)) ||
-        (e = cudaMemcpy(v.data(), dv.p, npair * sizeof(int), cudaMemcpyDeviceToHost)) ||
-        (e = cudaMemcpy(tm.data(), dt.p, npair * kBands * sizeof(double), cudaMemcpyDeviceToHost)))
-        return fail(PACH_ERR_CUDA, cuda_msg(e, "direct sound"));
-    for (int k = 0; k < n_receivers; ++k)
-        for (int s = 0; s < n_sources; ++s) {
-            const size_t p = (size_t)k * n_sources + s;
-            const double dx = r3[3 * k] - s3[3 * s], dy = r3[3 * k + 1] - s3[3 * s + 1], dz = r3[3 * k + 2] - s3[3 * s + 2];
-            const double L = std::sqrt(dx * dx + dy * dy + dz * dz);
-            valid[p] = v[p];
-            if (distance) distance[p] = L;
-            if (energy)
-                for (int o = 0; o < kBands; ++o) {
-                    const double P = 1e-12 * std::pow(10.0, .1 * sources[s].power_db[o]);
-                    energy[p * kBands + o] = P * std::pow(10.0, -.1 * hs.atten[o] * L) * tm[p * kBands + o] / (4 * M_PI * L * L);
-                }
-        }
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!scene || !sources || n_sources < 1 || n_receivers < 0 || (n_receivers > 0 && (!receivers || !valid)))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        if ((long long)n_sources * n_receivers > (1ll << 30)) return fail(PACH_ERR_INVALID_ARGUMENT, "too many pairs");
+        if (n_receivers == 0) return PACH_OK;
+        cudaSetDevice(scene->device);
+        const HostScene &hs = scene->hs;
+        std::vector<double> s3(3 * (size_t)n_sources), r3(3 * (size_t)n_receivers);
+        for (int s = 0; s < n_sources; ++s)
+            for (int a = 0; a < 3; ++a) s3[3 * s + a] = sources[s].origin[a];
+        for (int k = 0; k < n_receivers; ++k)
+            for (int a = 0; a < 3; ++a) r3[3 * k + a] = receivers[k].origin[a];
+        const size_t npair = (size_t)n_sources * n_receivers;
+        DevMem ds, dr, dv, dt;
+        std::vector<int> v(npair);
+        std::vector<double> tm(npair * kBands);
+        cudaError_t e;
+        if ((e = upload(ds, s3.data(), s3.size() * sizeof(double))) || (e = upload(dr, r3.data(), r3.size() * sizeof(double))) ||
+            (e = dv.alloc(npair * sizeof(int))) || (e = dt.alloc(npair * kBands * sizeof(double))) ||
+            (e = launch_direct(scene->dev, ds.as<double>(), n_sources, dr.as<double>(), n_receivers, 64, dv.as<int>(),
+                               dt.as<double>(), 0)) ||
+            (e = cudaMemcpy(v.data(), dv.p, npair * sizeof(int), cudaMemcpyDeviceToHost)) ||
+            (e = cudaMemcpy(tm.data(), dt.p, npair * kBands * sizeof(double), cudaMemcpyDeviceToHost)))
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "direct sound"));
+        for (int k = 0; k < n_receivers; ++k)
+            for (int s = 0; s < n_sources; ++s) {
+                const size_t p = (size_t)k * n_sources + s;
+                const double dx = r3[3 * k] - s3[3 * s], dy = r3[3 * k + 1] - s3[3 * s + 1], dz = r3[3 * k + 2] - s3[3 * s + 2];
+                const double L = std::sqrt(dx * dx + dy * dy + dz * dz);
+                valid[p] = v[p];
+                if (distance) distance[p] = L;
+                if (energy)
+                    for (int o = 0; o < kBands; ++o) {
+                        const double P = 1e-12 * std::pow(10.0, .1 * sources[s].power_db[o]);
+                        energy[p * kBands + o] = P * std::pow(10.0, -.1 * hs.atten[o] * L) * tm[p * kBands + o] / (4 * M_PI * L * L);
+                    }
+            }
+        return PACH_OK;
+    }, fail);
 }
 
 pach_status pach_proposal_sample(const float *proposal, int32_t n_prop, double mix, uint64_t seed, int64_t ray_begin,
                                  int32_t n, float *dirs, float *weights) {
-    if (!proposal || n_prop < 1 || n_prop > 256 || !(mix >= 0 && mix <= 1) || n < 0 || ray_begin < 0 ||
-        ray_begin + n > (1ll << 32) || (n > 0 && (!dirs || !weights)))
-        return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    if (n == 0) return PACH_OK;
-    if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
-    std::vector<float> lobes;
-    proposal_lobes(proposal, n_prop, lobes);
-    DevMem dl, dd, dw;
-    cudaError_t e;
-    if ((e = upload(dl, lobes.data(), lobes.size() * sizeof(float))) || (e = dd.alloc(sizeof(float) * 3 * n)) ||
-        (e = dw.alloc(sizeof(float) * n)))
-        return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample setup"));
-    DevRun r{};
-    r.seed = seed;
-    r.prop = dl.as<float4>();
-    r.n_prop = n_prop;
-    r.prop_mix = (float)(mix > 0 ? mix : 0.3);
-    if ((e = launch_prop_sample(r, ray_begin, n, dd.as<float>(), dw.as<float>(), 0)) ||
-        (e = cudaMemcpy(dirs, dd.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost)) ||
-        (e = cudaMemcpy(weights, dw.p, sizeof(float) * n, cudaMemcpyDeviceToHost)))
-        return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample"));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!proposal || n_prop < 1 || n_prop > 256 || !(mix >= 0 && mix <= 1) || n < 0 || ray_begin < 0 ||
+            ray_begin + n > (1ll << 32) || (n > 0 && (!dirs || !weights)))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        if (n == 0) return PACH_OK;
+        if (pach_device_count() <= 0) return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible");
+        std::vector<float> lobes;
+        proposal_lobes(proposal, n_prop, lobes);
+        DevMem dl, dd, dw;
+        cudaError_t e;
+        if ((e = upload(dl, lobes.data(), lobes.size() * sizeof(float))) || (e = dd.alloc(sizeof(float) * 3 * n)) ||
+            (e = dw.alloc(sizeof(float) * n)))
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample setup"));
+        DevRun r{};
+        r.seed = seed;
+        r.prop = dl.as<float4>();
+        r.n_prop = n_prop;
+        r.prop_mix = (float)(mix > 0 ? mix : 0.3);
+        if ((e = launch_prop_sample(r, ray_begin, n, dd.as<float>(), dw.as<float>(), 0)) ||
+            (e = cudaMemcpy(dirs, dd.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost)) ||
+            (e = cudaMemcpy(weights, dw.p, sizeof(float) * n, cudaMemcpyDeviceToHost)))
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "proposal sample"));
+        return PACH_OK;
+    }, fail);
 }
 
 }  // extern "C"

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <exception>
 #include <future>
 #include <memory>
 #include <new>
@@ -39,6 +40,22 @@ struct UninitAlloc : std::allocator<T> {
 };
 template <class T>
 using hvec = std::vector<T, UninitAlloc<T>>;
+
+// Runs an entry point's body so that no C++ exception crosses the C ABI: a failed host allocation or
+// thread creation becomes PACH_ERR_OUT_OF_MEMORY with a message stored by `report` (the entry
+// point's last-error setter).
+template <class F, class R>
+pach_status guarded(F &&body, R &&report) noexcept {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        return report(PACH_ERR_OUT_OF_MEMORY, std::string("out of host memory"));
+    } catch (const std::exception &e) {
+        return report(PACH_ERR_OUT_OF_MEMORY, std::string("host resources exhausted: ") + e.what());
+    } catch (...) {
+        return report(PACH_ERR_OUT_OF_MEMORY, std::string("host resources exhausted"));
+    }
+}
 
 // Runs f(c0, c1) over [0, n) in chunks of `grain` elements on up to hardware_concurrency() threads;
 // inline when one chunk covers the range.  Chunk c is [c * grain, min(n, (c + 1) * grain)).

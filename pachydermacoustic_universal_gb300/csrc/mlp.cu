@@ -812,268 +812,286 @@ extern "C" {
 int64_t pach_mlp_param_count(void) { return public_count(); }
 
 pach_status pach_mlp_create(uint64_t seed, int32_t max_rows, pach_mlp **out) {
-    if (!out) return mfail(PACH_ERR_INVALID_ARGUMENT, "out is null");
-    *out = nullptr;
-    if (max_rows < 1 || max_rows > kMaxRows) return mfail(PACH_ERR_INVALID_ARGUMENT, "max_rows must be 1..65536");
-    int nd = 0;
-    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd < 1) return mfail(PACH_ERR_NO_DEVICE, "no CUDA device");
-    pach_mlp *m = new pach_mlp();
-    std::unique_ptr<pach_mlp> guard(m);
-    MTRY(cudaGetDevice(&m->device));
-    m->max_rows = max_rows;
-    m->Mp_max = round_up(max_rows, kTile);
-    const int Mp = m->Mp_max;
-    MTRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
-    m->n_dev = padded_offset(3, true) + kOut;
-    for (int l = 0; l < 4; ++l) {
-        Layer &L = m->L[l];
-        L.n = kLayerN[l];
-        L.k = kLayerKPad[l];
-        L.w = padded_offset(l, false);
-        L.b = padded_offset(l, true);
-        MTRY(m->wb[l].alloc((size_t)round_up(L.n, kTile) * L.k * 2));
-        L.wb = m->wb[l].as<__nv_bfloat16>();
-        if (l > 0) {
-            MTRY(m->wt[l].alloc((size_t)round_up(L.k, kTile) * L.n * 2));
-            L.wt = m->wt[l].as<__nv_bfloat16>();
-        } else {
-            L.wt = nullptr;
+    return guarded([&]() -> pach_status {
+        if (!out) return mfail(PACH_ERR_INVALID_ARGUMENT, "out is null");
+        *out = nullptr;
+        if (max_rows < 1 || max_rows > kMaxRows) return mfail(PACH_ERR_INVALID_ARGUMENT, "max_rows must be 1..65536");
+        int nd = 0;
+        if (cudaGetDeviceCount(&nd) != cudaSuccess || nd < 1) return mfail(PACH_ERR_NO_DEVICE, "no CUDA device");
+        pach_mlp *m = new pach_mlp();
+        std::unique_ptr<pach_mlp> guard(m);
+        MTRY(cudaGetDevice(&m->device));
+        m->max_rows = max_rows;
+        m->Mp_max = round_up(max_rows, kTile);
+        const int Mp = m->Mp_max;
+        MTRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+        m->n_dev = padded_offset(3, true) + kOut;
+        for (int l = 0; l < 4; ++l) {
+            Layer &L = m->L[l];
+            L.n = kLayerN[l];
+            L.k = kLayerKPad[l];
+            L.w = padded_offset(l, false);
+            L.b = padded_offset(l, true);
+            MTRY(m->wb[l].alloc((size_t)round_up(L.n, kTile) * L.k * 2));
+            L.wb = m->wb[l].as<__nv_bfloat16>();
+            if (l > 0) {
+                MTRY(m->wt[l].alloc((size_t)round_up(L.k, kTile) * L.n * 2));
+                L.wt = m->wt[l].as<__nv_bfloat16>();
+            } else {
+                L.wt = nullptr;
+            }
         }
-    }
-    const size_t F = sizeof(float);
-    MTRY(m->w.alloc(m->n_dev * F));
-    MTRY(m->m1.alloc(m->n_dev * F));
-    MTRY(m->m2.alloc(m->n_dev * F));
-    MTRY(m->g.alloc(m->n_dev * F));
-    MTRY(m->decay.alloc(m->n_dev));
-    MTRY(m->step.alloc(sizeof(int)));
-    MTRY(m->err.alloc(sizeof(int)));
-    MTRY(m->xb.alloc((size_t)Mp * kInPad * 2));
-    MTRY(m->xt.alloc((size_t)kTile * Mp * 2));
-    for (int i = 0; i < 3; ++i) {
-        MTRY(m->hb[i].alloc((size_t)Mp * kHid * 2));
-        MTRY(m->ht[i].alloc((size_t)kHid * Mp * 2));
-        MTRY(m->pre[i].alloc((size_t)Mp * kHid * F));
-        MTRY(m->dzb[i].alloc((size_t)Mp * kHid * 2));
-        MTRY(m->dzt[i].alloc((size_t)kHid * Mp * 2));
-    }
-    MTRY(m->out.alloc((size_t)Mp * kOut * F));
-    MTRY(m->dob.alloc((size_t)Mp * kOut * 2));
-    MTRY(m->dobt.alloc((size_t)round_up(kOut, kTile) * Mp * 2));
-    MTRY(m->target.alloc((size_t)max_rows * kBins * F));
-    MTRY(m->loss.alloc((size_t)Mp * F));
-    MTRY(m->losses.alloc((size_t)1024 * F));
-    MTRY(m->cond_in.alloc((size_t)max_rows * kIn * F));
-    MTRY(m->cond_train.alloc((size_t)max_rows * kIn * F));
-    {
-        std::vector<float> d, om;
-        direction_bins_host(d, om);
-        std::vector<float4> b(kBins);
-        for (int i = 0; i < kBins; ++i) b[i] = make_float4(d[3 * i], d[3 * i + 1], d[3 * i + 2], om[i]);
-        MTRY(m->bins.alloc(kBins * sizeof(float4)));
-        MTRY(cudaMemcpy(m->bins.p, b.data(), kBins * sizeof(float4), cudaMemcpyHostToDevice));
-    }
-    // seeded initialisation (public order): uniform(+-sqrt(6 / fan_in)) hidden weights, small output
-    // weights, zero biases except log kappa = 1 (kappa e), so the first mixture is broad
-    std::vector<float> pub((size_t)public_count());
-    Rng rng{seed ^ 0x6D6C7050726F70ull};
-    size_t p = 0;
-    for (int l = 0; l < 4; ++l) {
-        const double a = (l < 3) ? std::sqrt(6.0 / kLayerK[l]) : 0.5 / std::sqrt((double)kLayerK[l]);
-        for (int i = 0; i < kLayerN[l] * kLayerK[l]; ++i) pub[p++] = (float)(a * rng.sym());
-        for (int n = 0; n < kLayerN[l]; ++n) pub[p++] = (l == 3 && n % 5 == 3) ? 1.f : 0.f;
-    }
-    std::vector<float> dev;
-    to_padded(pub.data(), dev, m->n_dev);
-    MTRY(cudaMemcpy(m->w.p, dev.data(), m->n_dev * F, cudaMemcpyHostToDevice));
-    std::vector<unsigned char> dec(m->n_dev, 0);
-    for (int l = 0; l < 4; ++l)
-        for (size_t i = 0; i < (size_t)kLayerN[l] * kLayerKPad[l]; ++i) dec[padded_offset(l, false) + i] = 1;
-    MTRY(cudaMemcpy(m->decay.p, dec.data(), m->n_dev, cudaMemcpyHostToDevice));
-    MTRY(pack_weights(m));
-    MTRY(cudaStreamSynchronize(m->stream));
-    *out = guard.release();
-    return PACH_OK;
+        const size_t F = sizeof(float);
+        MTRY(m->w.alloc(m->n_dev * F));
+        MTRY(m->m1.alloc(m->n_dev * F));
+        MTRY(m->m2.alloc(m->n_dev * F));
+        MTRY(m->g.alloc(m->n_dev * F));
+        MTRY(m->decay.alloc(m->n_dev));
+        MTRY(m->step.alloc(sizeof(int)));
+        MTRY(m->err.alloc(sizeof(int)));
+        MTRY(m->xb.alloc((size_t)Mp * kInPad * 2));
+        MTRY(m->xt.alloc((size_t)kTile * Mp * 2));
+        for (int i = 0; i < 3; ++i) {
+            MTRY(m->hb[i].alloc((size_t)Mp * kHid * 2));
+            MTRY(m->ht[i].alloc((size_t)kHid * Mp * 2));
+            MTRY(m->pre[i].alloc((size_t)Mp * kHid * F));
+            MTRY(m->dzb[i].alloc((size_t)Mp * kHid * 2));
+            MTRY(m->dzt[i].alloc((size_t)kHid * Mp * 2));
+        }
+        MTRY(m->out.alloc((size_t)Mp * kOut * F));
+        MTRY(m->dob.alloc((size_t)Mp * kOut * 2));
+        MTRY(m->dobt.alloc((size_t)round_up(kOut, kTile) * Mp * 2));
+        MTRY(m->target.alloc((size_t)max_rows * kBins * F));
+        MTRY(m->loss.alloc((size_t)Mp * F));
+        MTRY(m->losses.alloc((size_t)1024 * F));
+        MTRY(m->cond_in.alloc((size_t)max_rows * kIn * F));
+        MTRY(m->cond_train.alloc((size_t)max_rows * kIn * F));
+        {
+            std::vector<float> d, om;
+            direction_bins_host(d, om);
+            std::vector<float4> b(kBins);
+            for (int i = 0; i < kBins; ++i) b[i] = make_float4(d[3 * i], d[3 * i + 1], d[3 * i + 2], om[i]);
+            MTRY(m->bins.alloc(kBins * sizeof(float4)));
+            MTRY(cudaMemcpy(m->bins.p, b.data(), kBins * sizeof(float4), cudaMemcpyHostToDevice));
+        }
+        // seeded initialisation (public order): uniform(+-sqrt(6 / fan_in)) hidden weights, small output
+        // weights, zero biases except log kappa = 1 (kappa e), so the first mixture is broad
+        std::vector<float> pub((size_t)public_count());
+        Rng rng{seed ^ 0x6D6C7050726F70ull};
+        size_t p = 0;
+        for (int l = 0; l < 4; ++l) {
+            const double a = (l < 3) ? std::sqrt(6.0 / kLayerK[l]) : 0.5 / std::sqrt((double)kLayerK[l]);
+            for (int i = 0; i < kLayerN[l] * kLayerK[l]; ++i) pub[p++] = (float)(a * rng.sym());
+            for (int n = 0; n < kLayerN[l]; ++n) pub[p++] = (l == 3 && n % 5 == 3) ? 1.f : 0.f;
+        }
+        std::vector<float> dev;
+        to_padded(pub.data(), dev, m->n_dev);
+        MTRY(cudaMemcpy(m->w.p, dev.data(), m->n_dev * F, cudaMemcpyHostToDevice));
+        std::vector<unsigned char> dec(m->n_dev, 0);
+        for (int l = 0; l < 4; ++l)
+            for (size_t i = 0; i < (size_t)kLayerN[l] * kLayerKPad[l]; ++i) dec[padded_offset(l, false) + i] = 1;
+        MTRY(cudaMemcpy(m->decay.p, dec.data(), m->n_dev, cudaMemcpyHostToDevice));
+        MTRY(pack_weights(m));
+        MTRY(cudaStreamSynchronize(m->stream));
+        *out = guard.release();
+        return PACH_OK;
+    }, mfail);
 }
 
 void pach_mlp_destroy(pach_mlp *m) { delete m; }
 
 pach_status pach_mlp_get_params(pach_mlp *m, float *params, int64_t n) {
-    if (!m || !params || n < public_count()) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    std::lock_guard<std::mutex> lk(m->mu);
-    std::vector<float> dev(m->n_dev);
-    MTRY(cudaMemcpy(dev.data(), m->w.p, m->n_dev * sizeof(float), cudaMemcpyDeviceToHost));
-    from_padded(dev, params);
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!m || !params || n < public_count()) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        std::lock_guard<std::mutex> lk(m->mu);
+        std::vector<float> dev(m->n_dev);
+        MTRY(cudaMemcpy(dev.data(), m->w.p, m->n_dev * sizeof(float), cudaMemcpyDeviceToHost));
+        from_padded(dev, params);
+        return PACH_OK;
+    }, mfail);
 }
 
 pach_status pach_mlp_set_params(pach_mlp *m, const float *params, int64_t n) {
-    if (!m || !params || n != public_count()) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    std::lock_guard<std::mutex> lk(m->mu);
-    std::vector<float> dev;
-    to_padded(params, dev, m->n_dev);
-    MTRY(cudaMemcpy(m->w.p, dev.data(), m->n_dev * sizeof(float), cudaMemcpyHostToDevice));
-    MTRY(cudaMemset(m->m1.p, 0, m->n_dev * sizeof(float)));
-    MTRY(cudaMemset(m->m2.p, 0, m->n_dev * sizeof(float)));
-    MTRY(cudaMemset(m->step.p, 0, sizeof(int)));
-    MTRY(pack_weights(m));
-    MTRY(cudaStreamSynchronize(m->stream));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!m || !params || n != public_count()) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        std::lock_guard<std::mutex> lk(m->mu);
+        std::vector<float> dev;
+        to_padded(params, dev, m->n_dev);
+        MTRY(cudaMemcpy(m->w.p, dev.data(), m->n_dev * sizeof(float), cudaMemcpyHostToDevice));
+        MTRY(cudaMemset(m->m1.p, 0, m->n_dev * sizeof(float)));
+        MTRY(cudaMemset(m->m2.p, 0, m->n_dev * sizeof(float)));
+        MTRY(cudaMemset(m->step.p, 0, sizeof(int)));
+        MTRY(pack_weights(m));
+        MTRY(cudaStreamSynchronize(m->stream));
+        return PACH_OK;
+    }, mfail);
 }
 
 pach_status pach_mlp_set_data(pach_mlp *m, const float *cond, const float *target, int32_t rows) {
-    if (!m || !cond || !target || rows < 1 || rows > m->max_rows) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    std::lock_guard<std::mutex> lk(m->mu);
-    for (int64_t i = 0; i < (int64_t)rows * kIn; ++i)
-        if (!std::isfinite(cond[i])) return mfail(PACH_ERR_INVALID_ARGUMENT, "cond holds a non-finite value");
-    for (int64_t i = 0; i < (int64_t)rows * kBins; ++i)
-        if (!(target[i] >= 0.f) || !std::isfinite(target[i]))
-            return mfail(PACH_ERR_INVALID_ARGUMENT, "target must be finite and non-negative");
-    MTRY(cudaMemcpyAsync(m->cond_train.p, cond, (size_t)rows * kIn * sizeof(float), cudaMemcpyHostToDevice, m->stream));
-    MTRY(cudaMemcpyAsync(m->target.p, target, (size_t)rows * kBins * sizeof(float), cudaMemcpyHostToDevice, m->stream));
-    MTRY(cudaStreamSynchronize(m->stream));
-    m->rows = rows;
-    m->x_train = false;
-    if (m->exec) {  // the captured step holds the old row count
-        cudaGraphExecDestroy(m->exec);
-        cudaGraphDestroy(m->graph);
-        m->exec = nullptr;
-        m->graph = nullptr;
-    }
-    return PACH_OK;
-}
-
-pach_status pach_mlp_loss_grad(pach_mlp *m, float *loss, float *grad) {
-    if (!m || !loss) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    std::lock_guard<std::mutex> lk(m->mu);
-    if (m->rows < 1) return mfail(PACH_ERR_NOT_READY, "no training data (pach_mlp_set_data)");
-    const int Mp = round_up(m->rows, kTile);
-    MTRY(load_train_inputs(m));
-    MTRY(forward(m, m->rows, Mp));
-    MTRY(backward(m, m->rows, Mp));
-    k_loss_sum<<<1, 256, 0, m->stream>>>(m->loss.as<float>(), m->rows, 1.f / m->rows, m->losses.as<float>(), 0);
-    MTRY(cudaGetLastError());
-    MTRY(cudaStreamSynchronize(m->stream));
-    pach_status st = check_err(m);
-    if (st != PACH_OK) return st;
-    MTRY(cudaMemcpy(loss, m->losses.p, sizeof(float), cudaMemcpyDeviceToHost));
-    if (grad) {
-        std::vector<float> dev(m->n_dev);
-        MTRY(cudaMemcpy(dev.data(), m->g.p, m->n_dev * sizeof(float), cudaMemcpyDeviceToHost));
-        from_padded(dev, grad);
-    }
-    return PACH_OK;
-}
-
-pach_status pach_mlp_train(pach_mlp *m, int32_t steps, float lr, float weight_decay, float *loss_curve) {
-    if (!m || steps < 0 || !(lr > 0.f) || !(weight_decay >= 0.f)) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    std::lock_guard<std::mutex> lk(m->mu);
-    if (m->rows < 1) return mfail(PACH_ERR_NOT_READY, "no training data (pach_mlp_set_data)");
-    const int Mp = round_up(m->rows, kTile);
-    MTRY(load_train_inputs(m));
-    if (!m->exec || m->graph_lr != lr || m->graph_wd != weight_decay) {
-        if (m->exec) {
+    return guarded([&]() -> pach_status {
+        if (!m || !cond || !target || rows < 1 || rows > m->max_rows) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        std::lock_guard<std::mutex> lk(m->mu);
+        for (int64_t i = 0; i < (int64_t)rows * kIn; ++i)
+            if (!std::isfinite(cond[i])) return mfail(PACH_ERR_INVALID_ARGUMENT, "cond holds a non-finite value");
+        for (int64_t i = 0; i < (int64_t)rows * kBins; ++i)
+            if (!(target[i] >= 0.f) || !std::isfinite(target[i]))
+                return mfail(PACH_ERR_INVALID_ARGUMENT, "target must be finite and non-negative");
+        MTRY(cudaMemcpyAsync(m->cond_train.p, cond, (size_t)rows * kIn * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+        MTRY(cudaMemcpyAsync(m->target.p, target, (size_t)rows * kBins * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+        MTRY(cudaStreamSynchronize(m->stream));
+        m->rows = rows;
+        m->x_train = false;
+        if (m->exec) {  // the captured step holds the old row count
             cudaGraphExecDestroy(m->exec);
             cudaGraphDestroy(m->graph);
             m->exec = nullptr;
             m->graph = nullptr;
         }
-        // warm the GEMM attribute outside capture
+        return PACH_OK;
+    }, mfail);
+}
+
+pach_status pach_mlp_loss_grad(pach_mlp *m, float *loss, float *grad) {
+    return guarded([&]() -> pach_status {
+        if (!m || !loss) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        std::lock_guard<std::mutex> lk(m->mu);
+        if (m->rows < 1) return mfail(PACH_ERR_NOT_READY, "no training data (pach_mlp_set_data)");
+        const int Mp = round_up(m->rows, kTile);
+        MTRY(load_train_inputs(m));
         MTRY(forward(m, m->rows, Mp));
+        MTRY(backward(m, m->rows, Mp));
+        k_loss_sum<<<1, 256, 0, m->stream>>>(m->loss.as<float>(), m->rows, 1.f / m->rows, m->losses.as<float>(), 0);
+        MTRY(cudaGetLastError());
         MTRY(cudaStreamSynchronize(m->stream));
-        MTRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = forward(m, m->rows, Mp);
-        if (e == cudaSuccess) e = backward(m, m->rows, Mp);
-        if (e == cudaSuccess) {
-            k_loss_sum<<<1, 256, 0, m->stream>>>(m->loss.as<float>(), m->rows, 1.f / m->rows, m->losses.as<float>(), 0);
-            k_adam<<<(unsigned)((m->n_dev + 255) / 256), 256, 0, m->stream>>>(
-                m->w.as<float>(), m->m1.as<float>(), m->m2.as<float>(), m->g.as<float>(), m->decay.as<unsigned char>(),
-                m->n_dev, m->step.as<int>(), lr, weight_decay);
-            k_step<<<1, 1, 0, m->stream>>>(m->step.as<int>());
-            e = cudaGetLastError();
-            if (e == cudaSuccess) e = pack_weights(m);
+        pach_status st = check_err(m);
+        if (st != PACH_OK) return st;
+        MTRY(cudaMemcpy(loss, m->losses.p, sizeof(float), cudaMemcpyDeviceToHost));
+        if (grad) {
+            std::vector<float> dev(m->n_dev);
+            MTRY(cudaMemcpy(dev.data(), m->g.p, m->n_dev * sizeof(float), cudaMemcpyDeviceToHost));
+            from_padded(dev, grad);
         }
-        cudaGraph_t gr = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(m->stream, &gr);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            if (gr) cudaGraphDestroy(gr);
-            return mfail(PACH_ERR_CUDA, cu_msg(e != cudaSuccess ? e : e2, "capturing the training step"));
+        return PACH_OK;
+    }, mfail);
+}
+
+pach_status pach_mlp_train(pach_mlp *m, int32_t steps, float lr, float weight_decay, float *loss_curve) {
+    return guarded([&]() -> pach_status {
+        if (!m || steps < 0 || !(lr > 0.f) || !(weight_decay >= 0.f)) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        std::lock_guard<std::mutex> lk(m->mu);
+        if (m->rows < 1) return mfail(PACH_ERR_NOT_READY, "no training data (pach_mlp_set_data)");
+        const int Mp = round_up(m->rows, kTile);
+        MTRY(load_train_inputs(m));
+        if (!m->exec || m->graph_lr != lr || m->graph_wd != weight_decay) {
+            if (m->exec) {
+                cudaGraphExecDestroy(m->exec);
+                cudaGraphDestroy(m->graph);
+                m->exec = nullptr;
+                m->graph = nullptr;
+            }
+            // warm the GEMM attribute outside capture
+            MTRY(forward(m, m->rows, Mp));
+            MTRY(cudaStreamSynchronize(m->stream));
+            MTRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = forward(m, m->rows, Mp);
+            if (e == cudaSuccess) e = backward(m, m->rows, Mp);
+            if (e == cudaSuccess) {
+                k_loss_sum<<<1, 256, 0, m->stream>>>(m->loss.as<float>(), m->rows, 1.f / m->rows, m->losses.as<float>(), 0);
+                k_adam<<<(unsigned)((m->n_dev + 255) / 256), 256, 0, m->stream>>>(
+                    m->w.as<float>(), m->m1.as<float>(), m->m2.as<float>(), m->g.as<float>(), m->decay.as<unsigned char>(),
+                    m->n_dev, m->step.as<int>(), lr, weight_decay);
+                k_step<<<1, 1, 0, m->stream>>>(m->step.as<int>());
+                e = cudaGetLastError();
+                if (e == cudaSuccess) e = pack_weights(m);
+            }
+            cudaGraph_t gr = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(m->stream, &gr);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (gr) cudaGraphDestroy(gr);
+                return mfail(PACH_ERR_CUDA, cu_msg(e != cudaSuccess ? e : e2, "capturing the training step"));
+            }
+            m->graph = gr;
+            MTRY(cudaGraphInstantiate(&m->exec, m->graph, 0));
+            m->graph_lr = lr;
+            m->graph_wd = weight_decay;
         }
-        m->graph = gr;
-        MTRY(cudaGraphInstantiate(&m->exec, m->graph, 0));
-        m->graph_lr = lr;
-        m->graph_wd = weight_decay;
-    }
-    for (int s = 0; s < steps; ++s) {
-        MTRY(cudaGraphLaunch(m->exec, m->stream));
-        if (loss_curve) {
-            MTRY(cudaMemcpyAsync(loss_curve + s, m->losses.p, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+        for (int s = 0; s < steps; ++s) {
+            MTRY(cudaGraphLaunch(m->exec, m->stream));
+            if (loss_curve) {
+                MTRY(cudaMemcpyAsync(loss_curve + s, m->losses.p, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+            }
         }
-    }
-    MTRY(cudaStreamSynchronize(m->stream));
-    return check_err(m);
+        MTRY(cudaStreamSynchronize(m->stream));
+        return check_err(m);
+    }, mfail);
 }
 
 pach_status pach_mlp_forward(pach_mlp *m, const float *cond, int32_t rows, float *out) {
-    if (!m || !cond || !out || rows < 1 || rows > m->max_rows) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
-    std::lock_guard<std::mutex> lk(m->mu);
-    const int Mp = round_up(rows, kTile);
-    MTRY(cudaMemcpyAsync(m->cond_in.p, cond, (size_t)rows * kIn * sizeof(float), cudaMemcpyHostToDevice, m->stream));
-    k_pack_input<<<(Mp * kInPad + 255) / 256, 256, 0, m->stream>>>(m->cond_in.as<float>(), rows, Mp,
-                                                                    m->xb.as<__nv_bfloat16>(), m->xt.as<__nv_bfloat16>());
-    MTRY(cudaGetLastError());
-    MTRY(forward(m, rows, Mp));
-    MTRY(cudaMemcpyAsync(out, m->out.p, (size_t)rows * kOut * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
-    MTRY(cudaStreamSynchronize(m->stream));
-    m->x_train = false;
-    return check_err(m);
+    return guarded([&]() -> pach_status {
+        if (!m || !cond || !out || rows < 1 || rows > m->max_rows) return mfail(PACH_ERR_INVALID_ARGUMENT, "bad arguments");
+        std::lock_guard<std::mutex> lk(m->mu);
+        const int Mp = round_up(rows, kTile);
+        MTRY(cudaMemcpyAsync(m->cond_in.p, cond, (size_t)rows * kIn * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+        k_pack_input<<<(Mp * kInPad + 255) / 256, 256, 0, m->stream>>>(m->cond_in.as<float>(), rows, Mp,
+                                                                        m->xb.as<__nv_bfloat16>(), m->xt.as<__nv_bfloat16>());
+        MTRY(cudaGetLastError());
+        MTRY(forward(m, rows, Mp));
+        MTRY(cudaMemcpyAsync(out, m->out.p, (size_t)rows * kOut * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+        MTRY(cudaStreamSynchronize(m->stream));
+        m->x_train = false;
+        return check_err(m);
+    }, mfail);
 }
 
 pach_status pach_mlp_gemm(const float *A, const float *B, int32_t M, int32_t N, int32_t K, float *C) {
-    if (!A || !B || !C || M < 1 || N < 16 || K < 16 || M > 4096 || N > 4096 || K > 4096 || N % 16 || K % 16)
-        return mfail(PACH_ERR_INVALID_ARGUMENT, "gemm: M, N, K must be 1..4096, N and K multiples of 16");
-    int nd = 0;
-    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd < 1) return mfail(PACH_ERR_NO_DEVICE, "no CUDA device");
-    const int Mp = round_up(M, kTile), Np = round_up(N, kTile);
-    std::vector<__nv_bfloat16> a((size_t)Mp * K, __float2bfloat16_rn(0.f)), b((size_t)Np * K, __float2bfloat16_rn(0.f));
-    for (int i = 0; i < M; ++i)
-        for (int k = 0; k < K; ++k) a[blk(i, k, K)] = __float2bfloat16_rn(A[(size_t)i * K + k]);
-    for (int i = 0; i < N; ++i)
-        for (int k = 0; k < K; ++k) b[blk(i, k, K)] = __float2bfloat16_rn(B[(size_t)i * K + k]);
-    Buf da, db, dc, de;
-    MTRY(da.alloc(a.size() * 2));
-    MTRY(db.alloc(b.size() * 2));
-    MTRY(dc.alloc((size_t)M * N * sizeof(float)));
-    MTRY(de.alloc(sizeof(int)));
-    MTRY(cudaMemcpy(da.p, a.data(), a.size() * 2, cudaMemcpyHostToDevice));
-    MTRY(cudaMemcpy(db.p, b.data(), b.size() * 2, cudaMemcpyHostToDevice));
-    Gemm g{};
-    g.A = da.as<__nv_bfloat16>();
-    g.B = db.as<__nv_bfloat16>();
-    g.Mp = Mp;
-    g.N = N;
-    g.K = K;
-    g.epi = EPI_F32;
-    g.m_valid = M;
-    g.out = dc.as<float>();
-    g.ld_out = N;
-    g.err = de.as<int>();
-    MTRY(launch_gemm(g, 0));
-    MTRY(cudaDeviceSynchronize());
-    int h = 0;
-    MTRY(cudaMemcpy(&h, de.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) return mfail(PACH_ERR_GAVE_UP, "tensor-core GEMM: a bounded barrier wait ran out");
-    MTRY(cudaMemcpy(C, dc.p, (size_t)M * N * sizeof(float), cudaMemcpyDeviceToHost));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!A || !B || !C || M < 1 || N < 16 || K < 16 || M > 4096 || N > 4096 || K > 4096 || N % 16 || K % 16)
+            return mfail(PACH_ERR_INVALID_ARGUMENT, "gemm: M, N, K must be 1..4096, N and K multiples of 16");
+        int nd = 0;
+        if (cudaGetDeviceCount(&nd) != cudaSuccess || nd < 1) return mfail(PACH_ERR_NO_DEVICE, "no CUDA device");
+        const int Mp = round_up(M, kTile), Np = round_up(N, kTile);
+        std::vector<__nv_bfloat16> a((size_t)Mp * K, __float2bfloat16_rn(0.f)), b((size_t)Np * K, __float2bfloat16_rn(0.f));
+        for (int i = 0; i < M; ++i)
+            for (int k = 0; k < K; ++k) a[blk(i, k, K)] = __float2bfloat16_rn(A[(size_t)i * K + k]);
+        for (int i = 0; i < N; ++i)
+            for (int k = 0; k < K; ++k) b[blk(i, k, K)] = __float2bfloat16_rn(B[(size_t)i * K + k]);
+        Buf da, db, dc, de;
+        MTRY(da.alloc(a.size() * 2));
+        MTRY(db.alloc(b.size() * 2));
+        MTRY(dc.alloc((size_t)M * N * sizeof(float)));
+        MTRY(de.alloc(sizeof(int)));
+        MTRY(cudaMemcpy(da.p, a.data(), a.size() * 2, cudaMemcpyHostToDevice));
+        MTRY(cudaMemcpy(db.p, b.data(), b.size() * 2, cudaMemcpyHostToDevice));
+        Gemm g{};
+        g.A = da.as<__nv_bfloat16>();
+        g.B = db.as<__nv_bfloat16>();
+        g.Mp = Mp;
+        g.N = N;
+        g.K = K;
+        g.epi = EPI_F32;
+        g.m_valid = M;
+        g.out = dc.as<float>();
+        g.ld_out = N;
+        g.err = de.as<int>();
+        MTRY(launch_gemm(g, 0));
+        MTRY(cudaDeviceSynchronize());
+        int h = 0;
+        MTRY(cudaMemcpy(&h, de.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) return mfail(PACH_ERR_GAVE_UP, "tensor-core GEMM: a bounded barrier wait ran out");
+        MTRY(cudaMemcpy(C, dc.p, (size_t)M * N * sizeof(float), cudaMemcpyDeviceToHost));
+        return PACH_OK;
+    }, mfail);
 }
 
 pach_status pach_direction_bins(float *dirs, float *solid_angle, int32_t cap) {
-    if (!dirs || !solid_angle || cap < kBins) return mfail(PACH_ERR_INVALID_ARGUMENT, "need room for 1536 bins");
-    std::vector<float> d, om;
-    direction_bins_host(d, om);
-    std::memcpy(dirs, d.data(), d.size() * sizeof(float));
-    std::memcpy(solid_angle, om.data(), om.size() * sizeof(float));
-    return PACH_OK;
+    return guarded([&]() -> pach_status {
+        if (!dirs || !solid_angle || cap < kBins) return mfail(PACH_ERR_INVALID_ARGUMENT, "need room for 1536 bins");
+        std::vector<float> d, om;
+        direction_bins_host(d, om);
+        std::memcpy(dirs, d.data(), d.size() * sizeof(float));
+        std::memcpy(solid_angle, om.data(), om.size() * sizeof(float));
+        return PACH_OK;
+    }, mfail);
 }
 
 }  // extern "C"
