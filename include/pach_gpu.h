@@ -25,7 +25,8 @@
  *                            Get_Definition_Map without coherent superposition (Pach_Map_Receiver.cs:925-1270)
  *
  * Error behaviour: every entry point returns a pach_status; the message of the last failure on
- * the calling thread is available from pach_last_error.  No callbacks cross the ABI.
+ * the calling thread is available from pach_last_error.  No callbacks and no C++ exceptions cross
+ * the ABI (a failed host allocation returns PACH_ERR_OUT_OF_MEMORY).
  */
 #ifndef PACH_GPU_H
 #define PACH_GPU_H
