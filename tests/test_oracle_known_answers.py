@@ -101,10 +101,13 @@ def test_oracle_grid_equals_brute_force_in_irregular_hall():
 
 @pytest.mark.parametrize("make", [lambda: rooms.shoebox_c1().scene,
                                   lambda: rooms.irregular_hall_c2().scene,
-                                  lambda: rooms.batched_rooms_c3(n_rooms=3)[2].scene])
+                                  lambda: rooms.batched_rooms_c3(n_rooms=3)[2].scene,
+                                  lambda: rooms.irregular_hall_c2(target_tris=150_000).scene])
 def test_engine_bvh_finds_the_nearest_hit(make):
     """The engine's BVH (built and walked on the host with the device's FP32 box tests) returns the
-    same nearest polygon as the oracle's brute force over every polygon."""
+    same nearest polygon as the oracle's brute force over every polygon.  The 150k-triangle hall takes
+    the build's parallel paths (polygon chunks, sharded coplanar groups, chunked binning of ranges
+    above 128k triangles, subtrees on threads)."""
     sc = make()
     lo, hi = sc.bounds()
     rng = np.random.default_rng(17)
