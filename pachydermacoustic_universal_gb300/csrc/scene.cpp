@@ -36,7 +36,7 @@ struct BNode { double lo[3], hi[3]; int left = -1, right = -1, first = 0, count 
 
 // Subtrees of at least this many triangles, in the top levels, are built on their own threads (each
 // into a builder of its own, appended in left-right order: the result equals the sequential build).
-constexpr int kParallelBuildMin = 16384;
+constexpr int kParallelBuildMin = 4096;
 constexpr int kParallelBuildDepth = 5;
 // Ranges of at least this many triangles are boxed and binned in parallel chunks.
 constexpr int kParallelBinMin = 131072;
