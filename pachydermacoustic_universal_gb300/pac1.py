@@ -103,16 +103,17 @@ class _Reader:
         return self._unpack("<?", 1)
 
 
-def write_pac1(filename, sources, direct, banks, cutoff_ms=None):
+def write_pac1(filename, sources, direct, banks, cutoff_ms=None, date=None):
     """Write one .pac1 file.  sources: the simulation Source objects (one per result set); direct: a
     Direct_Sound per source (simulation.Direct_Sound, computed); banks: a Receiver_Bank per source
-    (filled by SplitRayTracer.Combine_ThreadLocal_Results)."""
+    (filled by SplitRayTracer.Combine_ThreadLocal_Results); date: the date string written first
+    (default: now, as DateTime.Now.ToString() writes it in the en-US culture)."""
     if not banks:
         raise ValueError("There is no simulated data to save.")
     rb = banks[0]
     with open(filename, "wb") as f:
         w = _Writer(f)
-        w.string(datetime.datetime.now().strftime("%m/%d/%Y %I:%M:%S %p"))
+        w.string(date if date is not None else datetime.datetime.now().strftime("%m/%d/%Y %I:%M:%S %p"))
         w.string(VERSION)
         w.double(rb.CutOffTime if cutoff_ms is None else cutoff_ms)
         w.int32(rb.SampleRate)
