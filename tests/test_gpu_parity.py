@@ -3,8 +3,9 @@
 Tolerances, stated per test:
 * emission directions: |d_gpu - d_oracle| < 2e-6 (FP32 vs FP64 of the same uniforms);
 * pure-specular shoebox paths: same wall sequence, legs within 1e-4 relative (FP32 geometry);
-* pure-specular ETC (oracle (a)): band totals within 1e-4 relative, 99 % of occupied bins within
-  1e-3 relative -- the rest are 1 ms bin-edge straddles and grazing sphere hits, reported;
+* pure-specular ETC (oracle (a), the shoebox configuration's 100k primaries): band totals within 1e-4
+  relative, 99 % of occupied bins within 1e-3 relative -- the rest are 1 ms bin-edge straddles and
+  grazing sphere hits; direction components within 2e-4 of their band's energy total;
 * stochastic mode (oracle (b)): both sides draw the same Philox streams, so in the shoebox the
   totals agree within 5e-3 and T30/EDT/C80/D50 within a tenth of a JND (JND: 5 % T30/EDT,
   1 dB C80, 0.05 D50); in the chaotic jittered hall within one JND.
@@ -94,28 +95,54 @@ def test_specular_paths_follow_the_image_lattice():
         np.testing.assert_allclose(pts[i], r["points"][:nb], atol=2e-3)
 
 
+def _edge_distance(scene, poly, x):
+    """Distance of point x to the boundary of polygon `poly`."""
+    V = scene.vertices[scene.poly_indices[scene.poly_offsets[poly]:scene.poly_offsets[poly + 1]]]
+    best = np.inf
+    for k in range(len(V)):
+        a, b = V[k], V[(k + 1) % len(V)]
+        ab = b - a
+        t = np.clip(np.dot(x - a, ab) / np.dot(ab, ab), 0.0, 1.0)
+        best = min(best, float(np.linalg.norm(x - (a + t * ab))))
+    return best
+
+
 def test_specular_paths_in_jittered_hall_match_oracle():
+    """Per-ray hit sequences of the FP32 walk (with its FP64 re-test) against the FP64 oracle over 8
+    bounces: each sequence must match, except certified ties -- a ray whose first differing hit lies
+    within TIE_M of an edge of the polygon either side hit (where the two engines' accumulated position
+    difference can put the rays on different sides), or whose two candidate hits are equidistant."""
+    TIE_M = 5e-3
     w = rooms.irregular_hall_c2(target_tris=20_000)
     ds = tracer.DeviceScene(w.scene)
     rng = np.random.default_rng(9)
-    n = 1024
+    n = 4096
     o = np.repeat(np.array(w.sources[0].origin)[None], n, axis=0)
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
-    nb = 6
-    pg, tg, _ = tracer.specular_paths(ds, o, d, nb)
-    po, to, _ = O.specular_paths(w.scene, o, d, nb, grid_domain=31)
-    same = np.all(pg == po, axis=1)
-    assert same.mean() >= 0.98, same.mean()
-    np.testing.assert_allclose(tg[same], to[same], rtol=2e-3, atol=2e-4)
+    nb = 8
+    pg, tg, xg = tracer.specular_paths(ds, o, d, nb)
+    po, to, xo = O.specular_paths(w.scene, o, d, nb, grid_domain=31)
     # first leg from the source: always identical
     assert np.all(pg[:, 0] == po[:, 0])
+    same = np.all(pg == po, axis=1)
+    assert same.mean() >= 0.995, same.mean()
+    for i in np.where(~same)[0]:
+        b = int(np.argmax(pg[i] != po[i]))
+        tie = abs(tg[i, b] - to[i, b]) <= 1e-4 * max(to[i, b], 1.0)
+        for poly, x in ((pg[i, b], xg[i, b]), (po[i, b], xo[i, b])):
+            tie = tie or (poly >= 0 and _edge_distance(w.scene, poly, x) <= TIE_M)
+        assert tie, ("divergent hit sequence that is not an edge tie", i, b, pg[i, b], po[i, b])
+    # hit points of the matching sequences: FP32 drift stays below 2 mm over 8 bounces
+    assert np.linalg.norm(xg[same] - xo[same], axis=2).max() < 2e-3
+    np.testing.assert_allclose(tg[same], to[same], rtol=2e-3, atol=5e-4)
 
 
 # ---------------------------------------------------------------- oracle (a): pure specular
 def test_pure_specular_etc_matches_oracle():
+    """Oracle (a) at the shoebox configuration's full 100k primaries."""
     w = rooms.shoebox_c1()
-    n = 2000
+    n = 100_000
     hg, sg = tracer.trace(w, rays=n, seed=5, pure_specular=True)
     ho, so = O.trace(w, rays=n, seed=5, pure_specular=True, threads=0)
     assert sg["primaries"] == n and sg["queue_overflows"] == 0 and sg["capped"] == 0
@@ -126,8 +153,13 @@ def test_pure_specular_etc_matches_oracle():
     occ = Eo > 1e-12 * Eo.max()
     rel = np.abs(Eg[occ] - Eo[occ]) / Eo[occ]
     assert np.mean(rel < 1e-3) >= 0.99, np.mean(rel < 1e-3)
-    for k in ("pressure", "dir_pos", "dir_neg", "analysis"):
+    for k in ("pressure", "analysis"):
         np.testing.assert_allclose(hg[k].sum(axis=-1), ho[k].sum(axis=-1), rtol=2e-4, atol=1e-30)
+    # a direction component holds one sign of d.x E (a fraction of the band's energy), so its error is
+    # bounded by the band's energy total: within 2e-4 of it
+    for k in ("dir_pos", "dir_neg"):
+        d = np.abs(hg[k].sum(axis=-1) - ho[k].sum(axis=-1)) / tot_o[:, None, :]
+        assert d.max() <= 2e-4, (k, d.max())
 
 
 # ---------------------------------------------------------------- oracle (b): stochastic
@@ -204,8 +236,11 @@ def test_invalid_runs_are_rejected():
     w = rooms.shoebox_c1()
     ds = tracer.DeviceScene(w.scene)
     with pytest.raises(_capi.PachError) as ei:
-        tracer.trace(w, dscene=ds, rays=0)
+        tracer.trace(w, dscene=ds, rays=10, ray_begin=-1)
     assert ei.value.status == 1
+    with pytest.raises(_capi.PachError) as ei:  # convergence mode takes no emission overrides
+        tracer.trace(w, dscene=ds, rays=0, prim_dirs=np.zeros((1, 3)))
+    assert ei.value.status == 1 and "convergence mode" in str(ei.value)
     with pytest.raises(_capi.PachError):
         tracer.trace(w, dscene=ds, rays=10, oct_range=(3, 9))
     bad = rooms.Workload(w.name, w.scene, w.sources, [rooms.ReceiverSpec((1, 1, 1), -0.5)], 10, 2.0)
