@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define PACH_ABI_VERSION 1
+#define PACH_ABI_VERSION 2
 #define PACH_BANDS 8
 
 typedef enum {
@@ -96,7 +96,11 @@ typedef struct {
 
 typedef struct {
     uint64_t seed;                 /* Philox key; a run is reproducible for a fixed seed */
-    int64_t ray_count;             /* primary rays (SplitRayTracer rayCount > 0) */
+    int64_t ray_count;             /* primary rays (SplitRayTracer rayCount > 0); < 1: convergence mode as
+                                      the reference's rayCount < 1 (TaskAll:111-176, 300-330): revolutions of
+                                      80 primaries per source until the convergence checks of two receivers
+                                      (the farthest the source sees, the farthest it does not) agree --
+                                      0: SpecMin_Convergence_Check, < 0: Minimum_Convergence_Check */
     int64_t ray_begin;             /* index of the first primary: a shard [ray_begin, ray_begin+ray_count)
                                       draws the same random streams as in an unsharded run */
     double cutoff_length_m;        /* SplitRayTracer "cutoffTime" argument: a LENGTH, COTime = L / c */
@@ -133,6 +137,8 @@ typedef struct {
     double proposal_mix;           /* weight of uniform emission in the proposal, (0, 1]; 0 = 0.3 */
     double capture_edges_ms[3];    /* capture windows, ms after the direct arrival; zeros = 80, 400, 1200 */
     const struct pach_map_desc *map; /* optional mapping receivers (single-room runs), else NULL */
+    int64_t max_rays;              /* convergence mode (ray_count < 1): primaries traced at most before the run
+                                      stops unconverged (0 = 2^24) */
 } pach_trace_params;
 
 /* Mapping receivers (PachMapReceiver, Pach_Map_Receiver.cs:34-1834): many small spheres, typically one
@@ -212,6 +218,10 @@ typedef struct {
     double wall_ms;
     int32_t accel[3];              /* BVH inner nodes, leaves, depth */
     int32_t walk;                  /* the walk used: BVH node bytes (64 or 128) + 1000 x traversal (1-3) */
+    int64_t revolutions;           /* convergence mode: revolutions traced (primaries = revolutions x period) */
+    int32_t converged;             /* convergence mode: 1 when the checks agreed, 0 when max_rays stopped it */
+    int32_t check_receivers[2];    /* convergence mode: receivers of the two checks (-1: none) */
+    int32_t reserved2;
 } pach_stats;
 
 typedef struct pach_scene pach_scene;
@@ -324,19 +334,36 @@ pach_status pach_trace_run(pach_scene *scene, const pach_source_desc *sources, i
  * trace time -- a host tracing from an audio or plug-in processing callback, or code whose device
  * memory belongs to another framework's allocator: it creates the scene at set-up, then calls this
  * per run with its own device buffers (energy/pressure R*8*T doubles, dir_pos/dir_neg/analysis
- * R*24*T doubles; all five required; cleared by the call).  The call allocates nothing: its working
- * memory is a fixed ~4.6 MB device array inside the library, resident on every GPU that loads the
- * library until the process exits.  Limits: 16 sources, 256 receivers, 65536 octave rays in flight
- * (a scene whose phase-A bound or split trees need more is rejected with PACH_ERR_INVALID_ARGUMENT
- * or PACH_ERR_BOUNDS), no emission overrides.  The scene's device must be current.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress): make that first call before
- * any stream capture.  Runs on `stream` (a cudaStream_t, NULL = default stream) and returns when done.
- * Every call shares the one array, so calls that overlap on the GPU (other threads or streams) race. */
+ * R*24*T doubles; all five required; cleared by the call).  Its working memory is a fixed ~4.7 MB
+ * device array inside the library, resident on every GPU that loads the library until the process
+ * exits.  Limits: 16 sources, 256 receivers, 65536 octave rays in flight (a scene whose phase-A bound
+ * or split trees need more is rejected with PACH_ERR_INVALID_ARGUMENT or PACH_ERR_BOUNDS), no
+ * emission overrides; otherwise it rejects what pach_trace_begin rejects, with the same messages.
+ * The scene's device must be current.
+ * Set-up: the first call on a device looks up the array's device address (cudaGetSymbolAddress) and
+ * may load the library's device code, which allocates device memory once -- make that first call at
+ * set-up, before any stream capture, not from the thread that must not allocate.  Later calls
+ * allocate nothing.  The address stays cached for the process: after a cudaDeviceReset of that device
+ * (which also invalidates its scene handles) this entry point must not be called again.
+ * The call is synchronous: it runs on `stream` (a cudaStream_t, NULL = default stream), synchronising
+ * it every 32 loop iterations, and returns when the run is done.  Its time grows with ray_count; it
+ * returns PACH_ERR_GAVE_UP if the device loop stops making progress for 2048 iterations.  Every call
+ * shares the one array, so calls that overlap on the GPU (other threads or streams) race. */
 pach_status pach_trace_run_noalloc(const pach_scene *scene, const pach_source_desc *sources, int32_t n_sources,
                                    const pach_receiver_desc *receivers, int32_t n_receivers,
                                    const pach_trace_params *params, void *stream, double *d_energy,
                                    double *d_pressure, double *d_dir_pos, double *d_dir_neg, double *d_analysis,
                                    pach_stats *stats);
+
+/* The convergence checks of convergence mode (TaskAll:783-1107) replayed over a caller's per-revolution
+ * histograms, on the host: per_rev [revs][4][T] holds each revolution's raw contribution to one receiver's
+ * band-h_oct energy histogram and its three Reflection_Analysis_Data histograms (0 specular, 1 diffuse,
+ * 2 specular-after-scatter).  mode 0 = SpecMin_Convergence_Check, 1 = Minimum_Convergence_Check
+ * (distance_m / sound_speed = the direct arrival that starts its windows).  *stop_rev = the first
+ * revolution (1-based) after which Check() answered true, 0 if none did; *nmin_out = SpecMin's last
+ * minimum ray count (may be NULL). */
+pach_status pach_convergence_replay(const double *per_rev, int32_t revs, int32_t T, int32_t sample_rate, int32_t mode,
+                                    double distance_m, double sound_speed, int32_t *stop_rev, int64_t *nmin_out);
 
 /* Pure-specular paths (oracle (a)): per bounce the hit polygon (-1 = miss), leg length and hit
  * point, traced by the same device traversal as the tracer. */

@@ -60,7 +60,8 @@ class TraceParams(C.Structure):
                 ("traversal", C.c_int32), ("capture", C.c_int32),
                 ("prim_dirs", _dp), ("prim_weights", _dp),
                 ("proposal", C.POINTER(C.c_float)), ("n_proposal", C.c_int32), ("bvh_format", C.c_int32),
-                ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3), ("map", C.POINTER(MapDesc))]
+                ("proposal_mix", C.c_double), ("capture_edges_ms", C.c_double * 3), ("map", C.POINTER(MapDesc)),
+                ("max_rays", C.c_int64)]
 
 
 class RoomDesc(C.Structure):
@@ -92,7 +93,9 @@ class Stats(C.Structure):
                 ("sort_ms", C.c_double),
                 ("waves", C.c_int64), ("kernel_launches", C.c_int64), ("peak_live_rays", C.c_int64),
                 ("bvh_nodes_visited", C.c_int64), ("tri_tests", C.c_int64),
-                ("wall_ms", C.c_double), ("accel", C.c_int32 * 3), ("walk", C.c_int32)]
+                ("wall_ms", C.c_double), ("accel", C.c_int32 * 3), ("walk", C.c_int32),
+                ("revolutions", C.c_int64), ("converged", C.c_int32), ("check_receivers", C.c_int32 * 2),
+                ("reserved2", C.c_int32)]
 
     def to_dict(self):
         out = {}
@@ -109,7 +112,7 @@ EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_c
            "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_trace_get_map_directions", "pach_map_parameters",
            "pach_etc_parameters",
            "pach_run_destroy", "pach_trace_run",
-           "pach_trace_run_noalloc", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_medium_attenuation_third_octave", "pach_math_schroeder",
+           "pach_trace_run_noalloc", "pach_convergence_replay", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_medium_attenuation_third_octave", "pach_math_schroeder",
            "pach_math_t_x", "pach_math_edt", "pach_math_clarity", "pach_math_definition", "pach_math_center_time",
            "pach_math_strength", "pach_math_sound_speed",
            # include/pach_proposal.h
@@ -157,6 +160,8 @@ def _declare(L):
                                      C.POINTER(Stats)]),
         "pach_trace_run_noalloc": (C.c_int, [vp, C.POINTER(SourceDesc), C.c_int32, C.POINTER(ReceiverDesc), C.c_int32,
                                              C.POINTER(TraceParams), vp, vp, vp, vp, vp, vp, C.POINTER(Stats)]),
+        "pach_convergence_replay": (C.c_int, [_dp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                              C.c_double, _ip, C.POINTER(C.c_int64)]),
         "pach_trace_specular_paths": (C.c_int, [vp, C.c_int32, _dp, _dp, C.c_int32, _ip, _dp, _dp]),
         "pach_scene_shoot_host": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, _dp, _dp, _ip, _dp]),
         "pach_emit_directions": (C.c_int, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _dp]),

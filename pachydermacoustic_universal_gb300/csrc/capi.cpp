@@ -92,6 +92,14 @@ struct pach_run {
     MapGrid mg;
     std::vector<double> map_org;
     DevMem mrec, mdir, mcell, mentry, mE, mP, mDp, mDn, drecid;
+    // convergence mode (ray_count < 1): -1 off, 0 SpecMin, 1 Minimum; the checks, their receivers, the
+    // per-revolution capture and the pre-chunk copies of the histograms and counters
+    int conv_mode = -1;
+    int conv_rows[2] = {-1, -1};
+    long long conv_period = 80, conv_revs = 0;
+    bool conv_converged = false;
+    std::vector<ConvCheck> conv_checks;
+    DevMem conv, bak[6];
     // worker
     std::thread worker;
     std::mutex mu;
@@ -111,7 +119,8 @@ struct pach_run {
         cudaSetDevice(scene ? scene->device : 0);
         for (DevMem *m : {&hE, &hP, &hDp, &hDn, &hAn, &cnt, &qa, &qs0, &qs1, &qctl, &drec, &dsrc, &de0, &dgeo, &ddirs, &dw,
                           &sortbins, &dprop, &dcap, &droom, &droomprim, &btri, &btri64, &bnorm, &bmat, &btrans, &bbvh, &bbvhq,
-                          &mrec, &mdir, &mcell, &mentry, &mE, &mP, &mDp, &mDn, &drecid})
+                          &mrec, &mdir, &mcell, &mentry, &mE, &mP, &mDp, &mDn, &drecid, &conv, &bak[0], &bak[1], &bak[2],
+                          &bak[3], &bak[4], &bak[5]})
             m->release();
     }
 };
@@ -504,7 +513,7 @@ void run_worker_body(pach_run *run) {
             break;
         }
         TRY(run->qa.alloc(ring_cap * sizeof(ORayItem)));
-        TRY(run->qs0.alloc(std::min(max_wave, ring_cap) * sizeof(int2)));
+        TRY(run->qs0.alloc(std::min(max_wave, ring_cap) * sizeof(int4)));
         const bool sorting = run->p.ray_sort > 0;
         if (sorting) {
             TRY(run->qs1.alloc(std::min(max_wave, ring_cap) * sizeof(ORayItem)));
@@ -590,7 +599,7 @@ void run_worker_body(pach_run *run) {
         r.ring = run->qa.as<ORayItem>();
         r.ring_cap = ring_cap;
         r.ctl = run->qctl.as<WaveCtl>();
-        r.hits = run->qs0.as<int2>();
+        r.hits = run->qs0.as<int4>();
         r.wave_buf = sorting ? run->qs1.as<ORayItem>() : nullptr;
         r.bin_count = sorting ? run->sortbins.as<unsigned>() : nullptr;
         r.bin_cursor = sorting ? run->sortbins.as<unsigned>() + kSortBins : nullptr;
@@ -607,15 +616,25 @@ void run_worker_body(pach_run *run) {
         const int bb_threads = 128;
         const int bb_blocks = (int)std::max<long long>(1, std::min<long long>((r.feed_batch + bb_threads - 1) / bb_threads,
                                                                               (long long)dev_sms * 16));
-        // initial schedule
         std::memset(h_ctl, 0, sizeof(WaveCtl));
-        h_ctl->next_prim = rprim[0];
-        h_ctl->prim_end = rprim[0] + N;
-        h_ctl->prim_first = rprim[0];
-        TRY(cudaMemcpyAsync(run->qctl.p, h_ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
         double t_trace = 0, t_shade = 0, t_bb = 0, t_sort = 0;
         long long launches = 0;
         bool cancelled = false;
+        const bool conv_mode = run->conv_mode >= 0;
+        if (conv_mode) {
+            // per-revolution capture of the check receivers, and a copy of the histograms and counters
+            // taken before each chunk (restored when the checks agree inside a chunk)
+            r.conv = nullptr;
+            r.conv_row[0] = run->conv_rows[0];
+            r.conv_row[1] = run->conv_rows[1];
+            r.conv_oct = run->rooms[0].h_oct;
+            r.conv_period = run->conv_period;
+            TRY(run->conv.alloc((size_t)kConvChunk * 2 * kConvKinds * T * sizeof(double)));
+            r.conv = run->conv.as<double>();
+            DevMem *src_[6] = {&run->hE, &run->hP, &run->hDp, &run->hDn, &run->hAn, &run->cnt};
+            for (int i = 0; i < 6; ++i) TRY(run->bak[i].alloc(src_[i]->bytes));
+            if (e) break;
+        }
         auto one_iteration = [&](int k) -> cudaError_t {
             cudaError_t x;
             if ((x = launch_feed(r, stream))) return x;
@@ -632,7 +651,6 @@ void run_worker_body(pach_run *run) {
             if (timing && (x = cudaEventRecord(kev[6 * k + 5], stream))) return x;
             return cudaSuccess;
         };
-        TRY(cudaEventRecord(ev0, stream));
         if (!timing) {
             // the whole loop as one graph launch: while (k_cond says so) { one iteration }
             TRY(cudaGraphCreate(&graph, 0));
@@ -654,87 +672,180 @@ void run_worker_body(pach_run *run) {
             TRY(ce);
             TRY(ee);
             TRY(cudaGraphInstantiate(&gexec, graph, 0));
-            TRY(cudaGraphLaunch(gexec, stream));
-            TRY(cudaEventRecord(ev1, stream));
-            launches = 6;
-            // poll: progress from the mapped mirror, cancellation through the mapped flag (1: stop
-            // feeding; 2, two seconds later: stop the loop without waiting for the fed primaries)
-            auto t_cancel = std::chrono::steady_clock::now();
-            for (;;) {
-                const cudaError_t q = cudaEventQuery(ev1);
-                run->rays_done = std::max(0ll, (long long)h_mirror->next_prim - rprim[0]);
-                run->end_traces = (long long)h_mirror->end_traces;
-                run->segments = (long long)h_mirror->segments;
-                if (q == cudaSuccess) break;
-                if (q != cudaErrorNotReady) { e = q; where = "graph run"; break; }
-                if (run->cancel && !cancelled) {
-                    cancelled = true;
-                    t_cancel = std::chrono::steady_clock::now();
-                    *reinterpret_cast<volatile int *>(h_cancel) = 1;
-                } else if (cancelled && std::chrono::steady_clock::now() - t_cancel > std::chrono::seconds(2)) {
-                    *reinterpret_cast<volatile int *>(h_cancel) = 2;
+        }
+        double dev_ms_total = 0;
+        long long done_before = 0;  // primaries of the ranges already run (progress offset)
+        // Runs the device loop over primaries [p0, p1): the graph launch (progress and cancellation through
+        // mapped host memory) or, with kernel_timing, host-launched batches of iterations with CUDA events
+        // around every kernel.  Returns a CUDA error, or cudaSuccess with `status` set when it gave up.
+#define RTRY(x)                                   \
+    {                                             \
+        const cudaError_t x_ = (x);               \
+        if (x_ != cudaSuccess) { where = #x; return x_; } \
+    }
+        auto run_range = [&](long long p0, long long p1) -> cudaError_t {
+            // the schedule starts afresh; the pilots' per-primary ring footprint carries over
+            const unsigned long long per_prim = h_ctl->per_prim;
+            const int pilot_room = h_ctl->pilot_room;
+            std::memset(h_ctl, 0, sizeof(WaveCtl));
+            h_ctl->next_prim = p0;
+            h_ctl->prim_end = p1;
+            h_ctl->prim_first = p0;
+            h_ctl->per_prim = per_prim;
+            h_ctl->pilot_room = pilot_room;
+            RTRY(cudaMemcpyAsync(run->qctl.p, h_ctl, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
+            if (!timing) {
+                *reinterpret_cast<volatile int *>(h_cancel) = 0;
+                std::memset(h_mirror, 0, sizeof(HostMirror));
+                h_mirror->next_prim = p0;
+                // device time of the loop alone: the host's graph construction is not inside the events
+                RTRY(cudaEventRecord(ev0, stream));
+                RTRY(cudaGraphLaunch(gexec, stream));
+                RTRY(cudaEventRecord(ev1, stream));
+                launches += 6;
+                // poll: progress from the mapped mirror, cancellation through the mapped flag (1: stop
+                // feeding; 2, two seconds later: stop the loop without waiting for the fed primaries)
+                auto t_cancel = std::chrono::steady_clock::now();
+                for (;;) {
+                    const cudaError_t q = cudaEventQuery(ev1);
+                    run->rays_done = done_before + std::max(0ll, (long long)h_mirror->next_prim - p0);
+                    run->end_traces = (long long)h_mirror->end_traces;
+                    run->segments = (long long)h_mirror->segments;
+                    if (q == cudaSuccess) break;
+                    if (q != cudaErrorNotReady) { where = "graph run"; return q; }
+                    if (run->cancel && !cancelled) {
+                        cancelled = true;
+                        t_cancel = std::chrono::steady_clock::now();
+                        *reinterpret_cast<volatile int *>(h_cancel) = 1;
+                    } else if (cancelled && std::chrono::steady_clock::now() - t_cancel > std::chrono::seconds(2)) {
+                        *reinterpret_cast<volatile int *>(h_cancel) = 2;
+                    }
+                    std::this_thread::sleep_for(std::chrono::microseconds(500));
                 }
-                std::this_thread::sleep_for(std::chrono::microseconds(500));
+            } else {
+                RTRY(cudaEventRecord(ev0, stream));
+                int batch = 8;
+                for (long long it = 0;;) {
+                    // one batch of iterations, no host synchronisation inside
+                    while (kev.size() < (size_t)batch * 6) {
+                        cudaEvent_t x;
+                        RTRY(cudaEventCreate(&x));
+                        kev.push_back(x);
+                    }
+                    for (int k = 0; k < batch; ++k, ++it) {
+                        RTRY(one_iteration(k));
+                        launches += (sorting ? 8 : 5) - (fused ? 1 : 0);
+                    }
+                    RTRY(cudaMemcpyAsync(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
+                    RTRY(cudaMemcpyAsync(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost, stream));
+                    RTRY(cudaStreamSynchronize(stream));
+                    for (int k = 0; k < batch; ++k) {
+                        float a = 0, b = 0, c = 0, so = 0;
+                        RTRY(cudaEventElapsedTime(&a, kev[6 * k], kev[6 * k + 1]));
+                        RTRY(cudaEventElapsedTime(&so, kev[6 * k + 2], kev[6 * k + 3]));
+                        RTRY(cudaEventElapsedTime(&b, kev[6 * k + 3], kev[6 * k + 4]));
+                        RTRY(cudaEventElapsedTime(&c, kev[6 * k + 4], kev[6 * k + 5]));
+                        t_bb += a;
+                        t_sort += so;
+                        t_trace += b;
+                        t_shade += c;
+                    }
+                    // progress: primaries whose phase A has run
+                    run->rays_done = done_before + h_ctl->next_prim - p0;
+                    run->end_traces = (long long)h_cnt->end_traces;
+                    run->segments = (long long)(h_cnt->seg_broad + h_cnt->seg_b + h_cnt->seg_c);
+                    if (h_ctl->done) break;
+                    if (run->cancel && !cancelled) {
+                        // stop feeding; the primaries already fed run to completion, so the histograms stay
+                        // a consistent estimate over rays_done primaries
+                        cancelled = true;
+                        const long long stop = h_ctl->next_prim;
+                        RTRY(cudaMemcpyAsync(&run->qctl.as<WaveCtl>()->prim_end, &stop, sizeof(long long),
+                                             cudaMemcpyHostToDevice, stream));
+                        RTRY(cudaStreamSynchronize(stream));
+                    }
+                    if (batch < 64) batch *= 2;
+                    if (it > (1ll << 26)) {
+                        status = PACH_ERR_GAVE_UP;
+                        msg = "wavefront loop did not finish";
+                        final_state = PACH_RUN_FAILED;
+                        return cudaSuccess;
+                    }
+                }
+                RTRY(cudaEventRecord(ev1, stream));
             }
-            if (e) break;
+            RTRY(cudaStreamSynchronize(stream));
+            float ms = 0.f;
+            RTRY(cudaEventElapsedTime(&ms, ev0, ev1));
+            dev_ms_total += ms;
+            RTRY(cudaMemcpy(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost));
+            return cudaSuccess;
+        };
+#undef RTRY
+        if (!conv_mode) {
+            if ((e = run_range(rprim[0], rprim[0] + N)) != cudaSuccess || status) break;
         } else {
-            int batch = 8;
-            for (long long it = 0; !e;) {
-                // one batch of iterations, no host synchronisation inside
-                while (kev.size() < (size_t)batch * 6) {
-                    cudaEvent_t x;
-                    TRY(cudaEventCreate(&x));
-                    kev.push_back(x);
-                }
+            // Convergence mode (TaskAll:300-330): revolutions of conv_period primaries until every check
+            // agrees.  Chunks of revolutions run as one device loop that also records each revolution's
+            // contribution to the two check receivers; the host replays the checks revolution by
+            // revolution.  When they agree inside a chunk, the histograms and counters are restored to
+            // their state before the chunk and the chunk's primaries up to that revolution are traced
+            // again -- the same Philox streams, so the result is the run that stopped there.
+            const long long period = run->conv_period;
+            const long long cap = run->p.max_rays > 0 ? run->p.max_rays : (1ll << 24);
+            std::vector<ConvCheck> &checks = run->conv_checks;
+            std::vector<double> capbuf((size_t)kConvChunk * 2 * kConvKinds * T);
+            DevMem *live[6] = {&run->hE, &run->hP, &run->hDp, &run->hDn, &run->hAn, &run->cnt};
+            long long done = 0, revs = 0;
+            int chunk = 4;
+            bool converged = false;
+            while (!converged && done < cap && !run->cancel) {
+                const long long left = (cap - done + period - 1) / period;
+                const int K = (int)std::min<long long>(chunk, left);
+                for (int i = 0; i < 6; ++i)
+                    TRY(cudaMemcpyAsync(run->bak[i].p, live[i]->p, live[i]->bytes, cudaMemcpyDeviceToDevice, stream));
+                TRY(cudaMemsetAsync(run->conv.p, 0, (size_t)K * 2 * kConvKinds * T * sizeof(double), stream));
                 if (e) break;
-                for (int k = 0; k < batch && !e; ++k, ++it) {
-                    TRY(one_iteration(k));
-                    launches += (sorting ? 8 : 5) - (fused ? 1 : 0);
+                done_before = done;
+                if ((e = run_range(rprim[0] + done, rprim[0] + done + K * period)) != cudaSuccess || status) break;
+                TRY(cudaMemcpy(capbuf.data(), run->conv.p, (size_t)K * 2 * kConvKinds * T * sizeof(double),
+                               cudaMemcpyDeviceToHost));
+                int stop = -1;
+                for (int j = 0; j < K && stop < 0; ++j) {
+                    bool agree = true;
+                    for (int k = 0; k < 2; ++k) {
+                        ConvCheck &c = checks[(size_t)k];
+                        if (c.mode < 0) continue;
+                        const double *h = capbuf.data() + ((size_t)j * 2 + k) * kConvKinds * T;
+                        for (int b = 0; b < T; ++b) {
+                            c.E[(size_t)b] += h[b];
+                            c.A0[(size_t)b] += h[T + b];
+                            c.A1[(size_t)b] += h[2 * T + b];
+                            c.A2[(size_t)b] += h[3 * T + b];
+                        }
+                        agree = c.check() && agree;  // every check runs each revolution (C# &=)
+                    }
+                    if (agree) stop = j;
                 }
-                if (e) break;
-                TRY(cudaMemcpyAsync(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
-                TRY(cudaMemcpyAsync(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost, stream));
-                TRY(cudaStreamSynchronize(stream));
-                for (int k = 0; k < batch; ++k) {
-                    float a = 0, b = 0, c = 0, so = 0;
-                    TRY(cudaEventElapsedTime(&a, kev[6 * k], kev[6 * k + 1]));
-                    TRY(cudaEventElapsedTime(&so, kev[6 * k + 2], kev[6 * k + 3]));
-                    TRY(cudaEventElapsedTime(&b, kev[6 * k + 3], kev[6 * k + 4]));
-                    TRY(cudaEventElapsedTime(&c, kev[6 * k + 4], kev[6 * k + 5]));
-                    t_bb += a;
-                    t_sort += so;
-                    t_trace += b;
-                    t_shade += c;
+                if (stop >= 0 && stop < K - 1) {
+                    for (int i = 0; i < 6; ++i)
+                        TRY(cudaMemcpyAsync(live[i]->p, run->bak[i].p, live[i]->bytes, cudaMemcpyDeviceToDevice, stream));
+                    if (e) break;
+                    if ((e = run_range(rprim[0] + done, rprim[0] + done + (stop + 1) * period)) != cudaSuccess || status)
+                        break;
                 }
-                if (e) break;
-                // progress: primaries whose phase A has run
-                run->rays_done = h_ctl->next_prim - rprim[0];
-                run->end_traces = (long long)h_cnt->end_traces;
-                run->segments = (long long)(h_cnt->seg_broad + h_cnt->seg_b + h_cnt->seg_c);
-                if (h_ctl->done) break;
-                if (run->cancel && !cancelled) {
-                    // stop feeding; the primaries already fed run to completion, so the histograms stay
-                    // a consistent estimate over rays_done primaries
-                    cancelled = true;
-                    const long long stop = h_ctl->next_prim;
-                    TRY(cudaMemcpyAsync(&run->qctl.as<WaveCtl>()->prim_end, &stop, sizeof(long long),
-                                        cudaMemcpyHostToDevice, stream));
-                    TRY(cudaStreamSynchronize(stream));
-                }
-                if (batch < 64) batch *= 2;
-                if (it > (1ll << 26)) {
-                    status = PACH_ERR_GAVE_UP;
-                    msg = "wavefront loop did not finish";
-                    final_state = PACH_RUN_FAILED;
-                    break;
-                }
+                done += (stop >= 0 ? stop + 1 : K) * period;
+                revs = done / period;
+                converged = stop >= 0;
+                chunk = std::min(chunk * 2, kConvChunk);
             }
             if (e || status) break;
-            TRY(cudaEventRecord(ev1, stream));
+            run->rooms[0].rays = done;
+            run->conv_revs = revs;
+            run->conv_converged = converged;
+            if (run->cancel) cancelled = true;
         }
-        TRY(cudaStreamSynchronize(stream));
-        float dev_ms = 0.f;
-        TRY(cudaEventElapsedTime(&dev_ms, ev0, ev1));
+        const float dev_ms = (float)dev_ms_total;
         TRY(cudaMemcpy(h_cnt, run->cnt.p, sizeof(DevCounters), cudaMemcpyDeviceToHost));
         TRY(cudaMemcpy(h_ctl, run->qctl.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost));
         const HostScene &hs = sc->hs;
@@ -774,6 +885,10 @@ void run_worker_body(pach_run *run) {
         s.accel[1] = hs.bvh_leaves;
         s.accel[2] = hs.bvh_depth;
         s.walk = (quant ? 64 : 128) + 1000 * (fused ? 3 : ((tr_variant & 16) ? 2 : 1));
+        s.revolutions = conv_mode ? run->conv_revs : 0;
+        s.converged = conv_mode && run->conv_converged ? 1 : 0;
+        s.check_receivers[0] = conv_mode ? run->conv_rows[0] : -1;
+        s.check_receivers[1] = conv_mode ? run->conv_rows[1] : -1;
         run->rays_done = (long long)h_cnt->primaries;
         run->segments = s.segments;
         run->end_traces = s.end_traces;
@@ -809,7 +924,8 @@ void run_worker_body(pach_run *run) {
     if (h_cancel) cudaFreeHost(h_cancel);
     // release the ring and the batch scene; histograms and counters stay until the run is destroyed
     for (DevMem *m : {&run->qa, &run->qs0, &run->qs1, &run->ddirs, &run->dw, &run->sortbins, &run->btri, &run->btri64,
-                      &run->bnorm, &run->bmat, &run->btrans, &run->bbvh, &run->bbvhq})
+                      &run->bnorm, &run->bmat, &run->btrans, &run->bbvh, &run->bbvhq, &run->conv, &run->bak[0],
+                      &run->bak[1], &run->bak[2], &run->bak[3], &run->bak[4], &run->bak[5]})
         m->release();
     if (e != cudaSuccess) return finish(PACH_ERR_CUDA, cuda_msg(e, where.c_str()), PACH_RUN_FAILED);
     finish(status, msg, final_state);
@@ -820,9 +936,11 @@ pach_status check_run(pach_run *run) {
     return PACH_OK;
 }
 
-// Checks shared by pach_trace_begin and pach_batch_begin: the run-wide parameters and one room's
-// sources and receivers.
-pach_status check_common(const pach_trace_params &p) {
+}  // namespace
+
+// Checks shared by pach_trace_begin, pach_batch_begin and pach_trace_run_noalloc: the run-wide
+// parameters and one room's sources and receivers (the message goes to pach_last_error).
+pach_status pach::check_common(const pach_trace_params &p) {
     if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi) return fail(PACH_ERR_INVALID_ARGUMENT, "octave range must lie in 0..7");
     if (p.sample_rate < 1) return fail(PACH_ERR_INVALID_ARGUMENT, "sample_rate must be positive");
     if (p.traversal < 0 || p.traversal > 3) return fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0..3");
@@ -831,7 +949,7 @@ pach_status check_common(const pach_trace_params &p) {
     return PACH_OK;
 }
 
-pach_status check_room(const pach_source_desc *sources, int32_t n_sources, const pach_receiver_desc *receivers,
+pach_status pach::check_room(const pach_source_desc *sources, int32_t n_sources, const pach_receiver_desc *receivers,
                        int32_t n_receivers, const std::string &who) {
     if (!sources || n_sources < 1 || n_sources > kMaxSources)
         return fail(PACH_ERR_INVALID_ARGUMENT, who + "need 1.." + std::to_string(kMaxSources) + " sources");
@@ -846,7 +964,6 @@ pach_status check_room(const pach_source_desc *sources, int32_t n_sources, const
     return PACH_OK;
 }
 
-}  // namespace
 
 extern "C" {
 
@@ -1006,9 +1123,17 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
         if (pach_status st = check_room(sources, n_sources, receivers, n_receivers, "")) return st;
         if (n_receivers > 2048) return fail(PACH_ERR_INVALID_ARGUMENT, "at most 2048 receivers per run");
         const pach_trace_params &p = *params;
-        if (p.ray_count < 1 || p.ray_begin < 0 || p.ray_begin + p.ray_count > (1ll << 32))
-            return fail(PACH_ERR_INVALID_ARGUMENT,
-                        "ray_count must be >= 1 and ray_begin + ray_count <= 2^32 (convergence mode is not supported)");
+        const bool conv = p.ray_count < 1;  // convergence mode (SplitRayTracer rayCount < 1)
+        const long long conv_cap = p.max_rays > 0 ? p.max_rays : (1ll << 24);
+        if (p.ray_begin < 0 || (!conv && p.ray_begin + p.ray_count > (1ll << 32)))
+            return fail(PACH_ERR_INVALID_ARGUMENT, "ray_begin must be >= 0 and ray_begin + ray_count <= 2^32");
+        if (conv) {
+            if (p.prim_dirs || p.prim_weights || p.proposal || p.capture || p.map)
+                return fail(PACH_ERR_INVALID_ARGUMENT,
+                            "convergence mode (ray_count < 1) takes no emission overrides, proposal, capture or map");
+            if (p.max_rays < 0 || p.ray_begin + conv_cap + 80ll * kConvChunk * n_sources > (1ll << 32))
+                return fail(PACH_ERR_INVALID_ARGUMENT, "max_rays must be >= 0 and ray_begin + max_rays < 2^32");
+        }
         if (pach_status st = check_common(p)) return st;
         if (!(p.cutoff_length_m > 0)) return fail(PACH_ERR_INVALID_ARGUMENT, "cutoff_length_m must be positive");
         if (p.proposal) {
@@ -1053,10 +1178,27 @@ pach_status pach_trace_begin(pach_scene *scene, const pach_source_desc *sources,
         rm.cutoff_len = p.cutoff_length_m;  // TaskAll:83 -- the ctor's cutoff argument is a length
         std::string err;
         if (!room_setup(rm, p, err)) return fail(PACH_ERR_INVALID_ARGUMENT, err);
-        run->rooms.push_back(std::move(rm));
         run->R = n_receivers;
         run->nsrc = n_sources;
         run->T = (int)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
+        if (conv) {
+            // Revolution_Period: 80 primaries per point source, the members' sum for a cluster
+            // (Classes_Sources.cs:197-200, 687); the checks' receivers as the ctor picks them, seen from
+            // the source's Origin (a cluster's: the mean of its members' origins, Classes_Sources.cs:684-689)
+            run->conv_mode = p.ray_count == 0 ? 0 : 1;
+            run->conv_period = 80ll * n_sources;
+            rm.rays = (long long)kConvChunk * run->conv_period;  // ring sizing: one chunk of revolutions
+            double ctr[3] = {0, 0, 0}, dist[2];
+            for (int s = 0; s < n_sources; ++s)
+                for (int a = 0; a < 3; ++a) ctr[a] += sources[s].origin[a] / n_sources;
+            pick_conv_receivers(scene->hs, ctr, receivers, n_receivers, run->conv_rows, dist);
+            run->conv_checks.resize(2);
+            for (int k = 0; k < 2; ++k)
+                if (run->conv_rows[k] >= 0)
+                    conv_setup(run->conv_checks[(size_t)k], run->conv_mode == 0 ? 0 : 1, run->conv_rows[k], dist[k],
+                               scene->hs.c, p.sample_rate, run->T);
+        }
+        run->rooms.push_back(std::move(rm));
         run->worker = std::thread(run_worker, run.get());
         *out = run.release();
         return PACH_OK;

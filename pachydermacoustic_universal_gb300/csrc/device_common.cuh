@@ -359,6 +359,20 @@ __device__ __forceinline__ void hist_add(const DevRun &r, float rho_c, int k, in
 __device__ __forceinline__ void capture_add(const DevRun &r, const RoomParams &P, float4 rc, int k, uint32_t prim,
                                             double time, float e);
 
+// Convergence mode: the detection also goes to its revolution's copy of the check receiver's energy
+// and analysis histograms (the checks replay the revolutions on the host).
+__device__ __forceinline__ void conv_add(const DevRun &r, int row, int oct, long long bin, float e, int kind,
+                                         uint32_t prim) {
+    if (oct != r.conv_oct) return;
+    const int k = row == r.conv_row[0] ? 0 : (row == r.conv_row[1] ? 1 : -1);
+    if (k < 0) return;
+    const long long rev = ((long long)prim - r.ctl->prim_first) / r.conv_period;
+    if (rev < 0 || rev >= kConvChunk) return;
+    double *h = r.conv + ((size_t)rev * 2 + k) * kConvKinds * r.T;
+    atomicAdd(h + bin, (double)e);
+    atomicAdd(h + (size_t)(1 + kind) * r.T + bin, (double)e);
+}
+
 // Spherical_Receiver.CheckRay (Classes_Receivers.cs:837-877): energy I 10^(-0.1 m c time) / pi * half,
 // over the receivers of the ray's room (rec: the run's receiver table in shared memory).
 __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomParams &P, const float4 *rec,
@@ -375,8 +389,10 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomPar
         const long long bin = (long long)(time * r.fs);
         if (!(time >= 0.0) || bin < 0 || bin >= r.T) continue;
         const float e = Iabs * exp2f(P.atten_k[oct] * (float)time) * kInvPi * half;
-        hist_add(r, P.rho_c, row, oct, bin, e, d, (mask & 1) ? 1 : ((mask & 2) ? 2 : 0));
+        const int kind = (mask & 1) ? 1 : ((mask & 2) ? 2 : 0);
+        hist_add(r, P.rho_c, row, oct, bin, e, d, kind);
         if (r.capture) capture_add(r, P, c, row, prim, time, e);
+        if (r.conv) conv_add(r, row, oct, bin, e, kind, prim);
     }
     return n;
 }
@@ -402,6 +418,7 @@ __device__ __forceinline__ uint32_t detect_broad(const DevRun &r, const RoomPara
             if (oct < P.oct_lo || oct > P.oct_hi) continue;
             const float e = E[oct] * sc[oct] * exp2f(P.atten_k[oct] * (float)time) * kInvPi * half;
             hist_add(r, P.rho_c, k, oct, bin, e, d, 0);
+            if (r.conv) conv_add(r, k, oct, bin, e, 0, prim);
             esum += e;
         }
         if (r.capture) capture_add(r, P, c, k, prim, time, esum);

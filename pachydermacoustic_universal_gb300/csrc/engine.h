@@ -151,6 +151,10 @@ struct WaveCtl {
     unsigned long long iters;       // loop iterations run (graph mode)
     unsigned long long idle;        // consecutive iterations that neither traced nor fed
     int done, gave_up;
+    long long pilot_count;          // primaries of the pilot in flight (0: none)
+    unsigned long long pilot_peak;  // peak live count while the pilot runs
+    int pilot_room;                 // first room whose ring footprint has not been measured by a pilot
+    int pressure;                   // the ring passed three quarters full since the last batch was fed
 };
 
 // Progress mirror in mapped host memory, written by the device every iteration in graph mode.
@@ -251,7 +255,9 @@ struct DevRun {
     ORayItem *ring;
     unsigned long long ring_cap;   // power of two
     WaveCtl *ctl;
-    int2 *hits;                    // per wave slot: (triangle, t bits); triangle -1 = miss
+    int4 *hits;                    // per wave slot: (triangle, t bits, polygon, coplanar group); triangle -1 =
+                                   // miss.  The walk writes the hit's polygon and group so that the shading
+                                   // pass loads normal and material directly, one dependent load fewer
     unsigned long long max_wave;   // items per wave at most
     long long feed_batch;          // primaries per phase-A launch at most
     unsigned long long feed_bound; // ring slots one primary can fill in phase A
@@ -273,6 +279,12 @@ struct DevRun {
     float cap_edge[3];             // window edges, ms after the direct arrival
     // mapping receivers (used by the map variants of the broadband and shading kernels)
     MapDev map;
+    // convergence mode (null: off): each revolution's contribution to the check receivers' band-conv_oct
+    // histograms, [kConvChunk][2][kConvKinds][T]; revolution = (primary - ctl->prim_first) / conv_period
+    double *conv;
+    int conv_row[2];               // histogram rows of the check receivers (-1: none)
+    int conv_oct;
+    long long conv_period;         // primaries per revolution
 };
 
 constexpr int kLobes = PACH_MLP_LOBES;
@@ -364,11 +376,38 @@ cudaError_t launch_prop_sample(const DevRun &r, long long p0, int n, float *dirs
 cudaError_t launch_direct(const DevScene &S, const double *src, int nsrc, const double *rec, int nrec, int max_cross,
                           int *valid, double *transmod, cudaStream_t s);
 
+// Convergence mode (rayCount < 1, convergence.cpp): one of the reference's convergence checks on one
+// receiver's cumulative raw histograms of band h_oct (energy, and the three Reflection_Analysis_Data
+// kinds); check() is its Check() after each revolution.
+struct ConvCheck {
+    int mode = -1;            // 0 SpecMin_Convergence_Check (rayCount == 0), 1 Minimum_Convergence_Check (< 0)
+    int row = -1;             // histogram row of the receiver
+    int T = 0, fs = 1000;
+    int s_start = 0, s50 = 0, s80 = 0, s_inf = 0;   // Minimum: sample windows
+    double snap50 = 0, snap80 = 0, snapinf = 0;
+    int step = 0, binct = 0;  // SpecMin: 50 ms blocks
+    long long rayct = 0, nmin = 0;
+    std::vector<double> snapshot;
+    int count = 0;
+    std::vector<double> E, A0, A1, A2;  // [T] energy; specular, diffuse, specular-after-scatter
+    bool check();
+};
+void conv_setup(ConvCheck &c, int mode, int row, double dist_m, double c_mps, int fs, int T);
+void pick_conv_receivers(const HostScene &hs, const double src[3], const pach_receiver_desc *rec, int R, int rows[2],
+                         double dist[2]);
+// Per-revolution capture of the two check receivers, [kConvChunk revolutions][2][4][T] doubles.
+constexpr int kConvChunk = 64;       // revolutions traced per device loop at most
+constexpr int kConvKinds = 4;        // energy, analysis 0..2
+
 // capi.cpp: read access to a scene handle (for entry points in other translation units)
 const HostScene *scene_host(const pach_scene *s);
 const DevScene *scene_dev(const pach_scene *s);
 int scene_device(const pach_scene *s);
 void set_last_error(const char *msg);
+// argument checks of the tracing entry points (who prefixes the message, e.g. "room 3: ")
+pach_status check_common(const pach_trace_params &p);
+pach_status check_room(const pach_source_desc *sources, int32_t n_sources, const pach_receiver_desc *receivers,
+                       int32_t n_receivers, const std::string &who);
 
 // scene.cpp
 bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err);

@@ -22,11 +22,12 @@ constexpr unsigned long long kNaRing = 1ull << 16;  // octave rays in flight
 constexpr unsigned long long kNaWave = 1ull << 15;  // octave rays per wave
 constexpr int kNaMaxReceivers = 256;
 constexpr int kNaMaxSources = 16;
+constexpr int kNaStall = 64;  // synchronisations without progress before the call gives up
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kOffRing = 0;
 constexpr size_t kOffHits = align256(kOffRing + kNaRing * sizeof(ORayItem));
-constexpr size_t kOffCtl = align256(kOffHits + kNaWave * sizeof(int2));
+constexpr size_t kOffCtl = align256(kOffHits + kNaWave * sizeof(int4));
 constexpr size_t kOffCnt = align256(kOffCtl + sizeof(WaveCtl));
 constexpr size_t kOffRec = align256(kOffCnt + sizeof(DevCounters));
 constexpr size_t kOffSrc = align256(kOffRec + kNaMaxReceivers * sizeof(float4));
@@ -34,7 +35,7 @@ constexpr size_t kOffE0 = align256(kOffSrc + kNaMaxSources * sizeof(float4));
 constexpr size_t kOffGeo = align256(kOffE0 + kNaMaxSources * kBands * sizeof(float));
 constexpr size_t kOffRoom = align256(kOffGeo + kGeoFaces * 3 * sizeof(float4));
 constexpr size_t kOffRoomPrim = align256(kOffRoom + sizeof(RoomParams));
-constexpr size_t kScratchBytes = align256(kOffRoomPrim + 2 * sizeof(long long));  // ~4.6 MB
+constexpr size_t kScratchBytes = align256(kOffRoomPrim + 2 * sizeof(long long));  // ~4.7 MB
 
 // The working memory of every pach_trace_run_noalloc call on this device.  It is resident on each
 // GPU that loads the library until the process exits.  In host code the name stands for a
@@ -61,30 +62,28 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
     if (!scene || !params || !sources) return na_fail(PACH_ERR_INVALID_ARGUMENT, "null scene, sources or params");
     if (!d_energy || !d_pressure || !d_dir_pos || !d_dir_neg || !d_analysis)
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "all five device histogram buffers are required");
-    if (n_sources < 1 || n_sources > kNaMaxSources)
-        return na_fail(PACH_ERR_INVALID_ARGUMENT, "pach_trace_run_noalloc takes 1..16 sources");
-    if (n_receivers < 0 || n_receivers > kNaMaxReceivers || (n_receivers > 0 && !receivers))
-        return na_fail(PACH_ERR_INVALID_ARGUMENT, "pach_trace_run_noalloc takes 0..256 receivers");
+    // the checks of the allocating entry points (same inputs rejected with the same messages), then
+    // the limits of the fixed working memory
+    if (pach_status st = check_room(sources, n_sources, receivers, n_receivers, "")) return st;
     const pach_trace_params &p = *params;
+    if (pach_status st = check_common(p)) return st;
+    if (n_sources > kNaMaxSources) return na_fail(PACH_ERR_INVALID_ARGUMENT, "pach_trace_run_noalloc takes 1..16 sources");
+    if (n_receivers > kNaMaxReceivers)
+        return na_fail(PACH_ERR_INVALID_ARGUMENT, "pach_trace_run_noalloc takes 0..256 receivers");
     if (p.prim_dirs || p.prim_weights || p.proposal || p.capture || p.map)
         return na_fail(PACH_ERR_INVALID_ARGUMENT,
                        "pach_trace_run_noalloc does not take emission overrides, a proposal, capture or a map");
     if (p.ray_count < 1 || p.ray_begin < 0 || p.ray_begin + p.ray_count > (1ll << 32))
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "ray_count must be >= 1 and ray_begin + ray_count <= 2^32");
-    if (p.oct_lo < 0 || p.oct_hi > 7 || p.oct_lo > p.oct_hi || p.sample_rate < 1 || !(p.cutoff_length_m > 0))
-        return na_fail(PACH_ERR_INVALID_ARGUMENT, "bad octave range, sample rate or cutoff");
+    if (!(p.cutoff_length_m > 0)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "cutoff_length_m must be positive");
     const long long T = (long long)((double)p.sample_rate * (p.hist_cotime_ms / 1000.0));
-    if (T < 1 || T > (1ll << 24)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "histogram length must be 1..2^24 bins");
-    if (p.traversal < 0 || p.traversal > 3) return na_fail(PACH_ERR_INVALID_ARGUMENT, "traversal must be 0..3");
-    for (int i = 0; i < n_receivers; ++i)
-        if (!(receivers[i].radius > 0)) return na_fail(PACH_ERR_INVALID_ARGUMENT, "receiver radius must be positive");
-    for (int s = 0; s < n_sources; ++s)
-        if (sources[s].kind < 0 || sources[s].kind > 2) return na_fail(PACH_ERR_INVALID_ARGUMENT, "unknown source kind");
 
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev != scene_device(scene) || dev < 0 || dev >= kMaxDevices)
         return na_fail(PACH_ERR_INVALID_ARGUMENT, "make the scene's device current before pach_trace_run_noalloc");
-    // Set-up, once per device, with that device current: the device address of the scratch array.
+    // Set-up, once per device, with that device current: the device address of the scratch array.  It
+    // is cached for the life of the process: a cudaDeviceReset (which also invalidates every scene
+    // handle of that device) leaves it stale, so no call may follow a reset of its device.
     unsigned char *base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_setup_mu);
@@ -213,7 +212,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         r.ring = reinterpret_cast<ORayItem *>(base + kOffRing);
         r.ring_cap = kNaRing;
         r.ctl = reinterpret_cast<WaveCtl *>(base + kOffCtl);
-        r.hits = reinterpret_cast<int2 *>(base + kOffHits);
+        r.hits = reinterpret_cast<int4 *>(base + kOffHits);
         r.max_wave = kNaWave;
         r.feed_bound = bound;
         // Feed only into an empty ring, 8 primaries at a time: their split trees then grow alone,
@@ -230,8 +229,14 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
                                      fused_walk(p.traversal, (int)hs.tri_poly.size())));
         const int tr_blocks = sms * (bps_tr > 0 ? bps_tr : 1), sh_blocks = sms * (bps_sh > 0 ? bps_sh : 1);
         long long launches = 0;
-        for (long long it = 0;;) {
-            for (int k = 0; k < 32; ++k, ++it) {
+        // Every iteration of the loop either traces a wave or feeds primaries, so the schedule moves on
+        // each time; if it stops moving for kNaStall synchronisations in a row (kNaStall x 32
+        // iterations) the call gives up instead of waiting on a loop that no longer progresses.
+        unsigned long long seen_waves = 0;
+        long long seen_prim = -1;
+        int stalls = 0;
+        for (;;) {
+            for (int k = 0; k < 32; ++k) {
                 NA_TRY(launch_feed(r, stream));
                 NA_TRY(launch_broadband(r, sms * 2, 128, stream, false, hs.ntri <= kFuseMaxTris));
                 NA_TRY(launch_wave(r, stream));
@@ -243,7 +248,13 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
             NA_TRY(cudaMemcpyAsync(&h_ctl, base + kOffCtl, sizeof(WaveCtl), cudaMemcpyDeviceToHost, stream));
             NA_TRY(cudaStreamSynchronize(stream));
             if (h_ctl.done) break;
-            if (it > (1ll << 26)) return na_fail(PACH_ERR_GAVE_UP, "wavefront loop did not finish");
+            if (h_ctl.waves == seen_waves && h_ctl.next_prim == seen_prim) {
+                if (++stalls >= kNaStall) return na_fail(PACH_ERR_GAVE_UP, "wavefront loop stopped making progress");
+            } else {
+                stalls = 0;
+            }
+            seen_waves = h_ctl.waves;
+            seen_prim = h_ctl.next_prim;
         }
         if (h_ctl.overflow)
             return na_fail(PACH_ERR_BOUNDS, "the split trees outgrew the no-alloc ring (65536 octave rays); "

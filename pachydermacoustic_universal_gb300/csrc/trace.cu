@@ -67,34 +67,67 @@ __global__ void k_feed(DevRun r) {
     // cancellation (graph mode): stop feeding; the primaries already fed run to completion
     if (r.cancel && *r.cancel && c->prim_end > c->next_prim) c->prim_end = c->next_prim;
     const unsigned long long live = c->tail - c->head;
-    const long long fed = c->next_prim - c->prim_first;
-    if (c->per_prim == 0 && fed >= kPilotPrimaries) {
-        // the pilot batch ran alone: once its split trees are done, its peak live count per primary
-        // (x 1.5) is the ring footprint a batch of primaries fed together reaches
+    // Pilots: the first kPilotPrimaries primaries of every room (of a plain run: of the run) are fed
+    // alone; once their split trees are done, their peak live count per primary (x 3) is the ring
+    // footprint the feed plans batches with -- the largest over the rooms measured so far, so a room
+    // whose split trees outgrow an earlier room's cannot overfill the ring.  The margin: a pilot fits
+    // in one wave, so each wave advances its trees by a whole level, while a batch larger than a wave
+    // is traced first-in-first-out across two levels at once and peaks higher per primary (measured
+    // up to 2.7x on 12-receiver shoeboxes at 20k primaries); k_wave doubles the figure again when the
+    // ring passes three quarters full.
+    if (c->pilot_count > 0) {
         if (live != 0) return;
-        c->per_prim = c->peak_live * 3 / 2 / (unsigned long long)fed + 1;
-        if (c->per_prim < r.feed_bound) c->per_prim = r.feed_bound;
+        unsigned long long pp = c->pilot_peak * 3 / (unsigned long long)c->pilot_count + 1;
+        if (pp < r.feed_bound) pp = r.feed_bound;
+        if (pp > c->per_prim) c->per_prim = pp;
+        c->pilot_count = 0;
+    }
+    if (c->next_prim >= c->prim_end) return;
+    const int room = room_of(r, c->next_prim);
+    if (room >= c->pilot_room) {
+        if (live != 0) return;  // the pilot runs alone: the ring drains first
+        const long long room_end = room + 1 < r.n_rooms ? __ldg(r.room_prim + room + 1) : c->prim_end;
+        long long n = room_end - c->next_prim;
+        if (n > kPilotPrimaries) n = kPilotPrimaries;
+        if (n > r.feed_batch) n = r.feed_batch;
+        if (n > c->prim_end - c->next_prim) n = c->prim_end - c->next_prim;
+        const long long fit = (long long)(r.ring_cap / r.feed_bound);  // >= 4: checked at set-up
+        if (n > fit) n = fit;
+        if (n < 1) n = 1;
+        c->pa_begin = c->next_prim;
+        c->pa_count = n;
+        c->next_prim += n;
+        c->pilot_count = n;
+        c->pilot_peak = 0;
+        c->pilot_room = room + 1;
+        c->last_live = 0;
+        return;
     }
     // Split trees grow for many waves after phase A, so a batch is fed only once the previous one
     // has peaked: the live count is low and no longer rising (generations of primaries).
     const bool decaying = live <= c->last_live;
     c->last_live = live;
-    if (c->next_prim < c->prim_end && live <= r.low_water && (decaying || live == 0)) {
+    if (live <= r.low_water && (decaying || live == 0)) {
         // Hard limit: the phase-A output of every fed primary must fit.  Soft limit: the new batch's
         // peak keeps the ring at most half full.
-        unsigned long long room = (r.ring_cap - live) / r.feed_bound;
+        unsigned long long room_n = (r.ring_cap - live) / r.feed_bound;
         const unsigned long long per_prim = c->per_prim ? c->per_prim : r.feed_bound;
         const unsigned long long half = r.ring_cap / 2;
         const unsigned long long soft = live < half ? (half - live) / per_prim : 0;
-        if (soft < room) room = soft > 0 ? soft : (live == 0 ? 1 : 0);
+        if (soft < room_n) room_n = soft > 0 ? soft : (live == 0 ? 1 : 0);
         long long n = c->prim_end - c->next_prim;
         if (n > r.feed_batch) n = r.feed_batch;
-        if (c->per_prim == 0 && n > kPilotPrimaries - fed) n = kPilotPrimaries - fed;
-        if ((unsigned long long)n > room) n = (long long)room;
+        // a batch never reaches into a room whose pilot has not run
+        if (c->pilot_room < r.n_rooms) {
+            const long long lim = __ldg(r.room_prim + c->pilot_room) - c->next_prim;
+            if (n > lim) n = lim;
+        }
+        if ((unsigned long long)n > room_n) n = (long long)room_n;
         if (n > 0) {
             c->pa_begin = c->next_prim;
             c->pa_count = n;
             c->next_prim += n;
+            c->pressure = 0;
         }
     }
 }
@@ -105,6 +138,12 @@ __global__ void k_wave(DevRun r) {
     if (c->done) { c->m = 0; return; }
     const unsigned long long live = c->tail - c->head;
     if (live > c->peak_live) c->peak_live = live;
+    if (c->pilot_count > 0 && live > c->pilot_peak) c->pilot_peak = live;
+    // the batches outgrew their plan: plan the next ones with twice the footprint per primary
+    if (live > r.ring_cap / 4 * 3 && !c->pressure && c->per_prim) {
+        c->pressure = 1;
+        c->per_prim *= 2;
+    }
     unsigned long long m = (r.ring_cap - live) / 2;  // each item leaves at most two
     if (m > live) m = live;
     if (m > r.max_wave) m = r.max_wave;
@@ -367,6 +406,17 @@ __global__ void __launch_bounds__(256) k_sort_scatter(DevRun r) {
 // ------------------------------------------------------------------------------------------
 // phases B and C, split into the BVH walk and the surface interaction
 // ------------------------------------------------------------------------------------------
+// The walk's result for wave slot j: the nearest triangle (-1: none), its distance, and the polygon and
+// coplanar group the shading pass needs (read from the triangle record, which the walk has just tested).
+__device__ __forceinline__ void write_hit(const DevRun &r, const DevScene &S, unsigned j, int tri, float t) {
+    int poly = -1, plane = -1;
+    if (tri >= 0) {
+        plane = __ldg(reinterpret_cast<const int *>(S.tri + 3 * tri) + 3);
+        poly = __ldg(reinterpret_cast<const int *>(S.tri + 3 * tri + 1) + 3);
+    }
+    r.hits[j] = make_int4(tri, __float_as_int(t), poly, plane);
+}
+
 // Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
 // its next leaf and tests it; a lane whose walk has ended writes its hit and takes the next wave
 // item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
@@ -447,7 +497,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 leaf = 0;
             }
             if (have && node == kEmptyChild) {
-                r.hits[j] = make_int2(bi, __float_as_int(best));
+                write_hit(r, S, j, bi, best);
                 have = false;
             }
         } else {
@@ -469,7 +519,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 node = stack_pop(stack, sp, best);
             }
             if (node == kEmptyChild) {
-                r.hits[j] = make_int2(bi, __float_as_int(best));
+                write_hit(r, S, j, bi, best);
                 have = false;
             }
         }
@@ -513,15 +563,18 @@ __global__ void __launch_bounds__(256, FUSED ? 2 : kShadeMinBlocks) k_shade(DevR
         Ray R, C;
         if (j < m) {
             R = to_ray(load_item(wave_item(r, head, j), 0));
-            int2 h;
+            int4 h;  // (triangle, t bits, polygon, coplanar group)
             if constexpr (FUSED) {
                 float tt;
                 int tri;
                 TraceWork tw;
                 const int root = r.n_rooms > 1 ? __ldg(&r.rooms[R.room].bvh_root) : 0;
                 const float teps = r.n_rooms > 1 ? __ldg(&r.rooms[R.room].t_eps) : S.t_eps;
-                h = trace_ray<int>(S, root, teps, R.p, R.d, R.plane, tt, tri, tw) ? make_int2(tri, __float_as_int(tt))
-                                                                              : make_int2(-1, 0);
+                h = make_int4(-1, 0, -1, -1);
+                if (trace_ray<int>(S, root, teps, R.p, R.d, R.plane, tt, tri, tw)) {
+                    const float4 A = __ldg(S.tri + 3 * tri), B = __ldg(S.tri + 3 * tri + 1);
+                    h = make_int4(tri, __float_as_int(tt), __float_as_int(B.w), __float_as_int(A.w));
+                }
                 L.v[C_RET] += tw.retests;
             } else {
                 h = r.hits[j];
@@ -540,9 +593,8 @@ __global__ void __launch_bounds__(256, FUSED ? 2 : kShadeMinBlocks) k_shade(DevR
             } else {
                 R.t_sum += (double)t * P.inv_c_d;
                 R.p = R.p + R.d * t;
-                const float4 A = __ldg(S.tri + 3 * h.x), B = __ldg(S.tri + 3 * h.x + 1);
-                R.plane = __float_as_int(A.w);
-                const int poly = __float_as_int(B.w);
+                R.plane = h.w;
+                const int poly = h.z;
                 const float3 n = f3(__ldg(S.pnormal + poly));
                 const float cos_t = dot3(n, R.d);
                 const float4 mt = __ldg(S.mat + poly * kBands + R.oct);  // (1-alpha, s_lo, s_mid, s_hi)

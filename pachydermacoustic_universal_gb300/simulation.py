@@ -244,8 +244,9 @@ class SplitRayTracer:
 
     def __init__(self, sourceIn, receiverIn, roomIn, cutoffTime, octaveRange=(0, 7), isOrderIn=-1, rayCountIn=10000,
                  Vis_Feedback=None, seed=None, **kw):
-        if rayCountIn < 1:
-            raise NotImplementedError("convergence mode (rayCount < 1) is not supported by the GPU engine")
+        # rayCountIn < 1: convergence mode (TaskAll:111-176, 300-330) -- revolutions of Revolution_Period()
+        # primaries until the convergence checks agree (0: SpecMin_Convergence_Check, < 0:
+        # Minimum_Convergence_Check); the engine picks the checks' receivers as the ctor does
         self.Source = sourceIn
         self.RecMain = receiverIn
         self.Room = roomIn
@@ -302,6 +303,8 @@ class SplitRayTracer:
         if p["rays_done"] == 0:
             return "Preparing Threads"
         el = time.time() - self._st
+        if self.Raycount < 1:  # convergence mode: no total known in advance
+            return f"Calculating Ray {p['rays_done']} (sub-ray {p['end_traces']}), until convergence. Press 'Esc' to Cancel..."
         rem = el * (p["rays_total"] - p["rays_done"]) / (p["rays_done"] + 1)
         h, m, s = int(rem // 3600), int(rem % 3600 // 60), int(rem % 60)
         return (f"Calculating Ray {p['rays_done']} of {p['rays_total']} (sub-ray {p['end_traces']}). "

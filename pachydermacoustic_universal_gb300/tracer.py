@@ -126,7 +126,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
                 pure_specular=False, max_broadband_bounces=0, max_segments_per_ray=0, feed_batch=0,
                 block_threads=0, blocks_per_sm=0, prim_dirs=None, prim_weights=None, ray_begin=0, wave_kilo_items=0,
                 ring_log2=0, kernel_timing=False, ray_sort=0, traversal=0, capture=False, capture_edges_ms=None,
-                proposal=None, proposal_mix=0.0, bvh_format=0, map_receivers=None):
+                proposal=None, proposal_mix=0.0, bvh_format=0, map_receivers=None, max_rays=0):
     p = _capi.TraceParams()
     p.seed = seed
     p.ray_count = int(rays)
@@ -148,6 +148,7 @@ def make_params(*, rays, cutoff_length_m, hist_cotime_ms, seed=1, oct_range=(0, 
     p.ray_sort = int(ray_sort)
     p.traversal = int(traversal)
     p.bvh_format = int(bvh_format)
+    p.max_rays = int(max_rays)
     p.prim_dirs = dptr(prim_dirs)
     p.prim_weights = dptr(prim_weights)
     p.capture = int(capture)
@@ -405,6 +406,18 @@ def shoot_host(scene, origins, dirs):
     t = np.zeros(n)
     check(_capi.lib().pach_scene_shoot_host(C.byref(desc), n, dptr(o), dptr(d), iptr(poly), dptr(t)))
     return poly, t
+
+
+def convergence_replay(per_rev, mode, distance_m, sound_speed, sample_rate=1000):
+    """The engine's convergence checks (pach_convergence_replay) over per-revolution contributions
+    per_rev [revs][4][T] (energy, analysis 0..2 of one receiver, band h_oct).  mode 0 SpecMin, 1 Minimum.
+    Returns (first revolution after which the check agreed, 1-based, 0 if none; SpecMin's Nmin)."""
+    h = np.ascontiguousarray(per_rev, dtype=np.float64)
+    stop = C.c_int32()
+    nmin = C.c_int64()
+    check(_capi.lib().pach_convergence_replay(dptr(h), h.shape[0], h.shape[2], int(sample_rate), int(mode),
+                                              float(distance_m), float(sound_speed), C.byref(stop), C.byref(nmin)))
+    return stop.value, nmin.value
 
 
 def emit_directions(seed, ray_begin, n, n_sources, kind):

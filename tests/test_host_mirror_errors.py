@@ -42,8 +42,6 @@ def test_modes_the_engine_does_not_implement_are_refused():
     with pytest.raises(NotImplementedError):
         sim.Source([120.0] * 8, (1.0, 1.0, 1.0), Third_Octave=True)
     with pytest.raises(NotImplementedError):
-        sim.SplitRayTracer(None, None, None, 100.0, rayCountIn=0)  # convergence mode
-    with pytest.raises(NotImplementedError):
         sim.Direct_Sound(None, None, None, [0, 7], ScreenCalc=True)
     with pytest.raises(NotImplementedError):
         sim.IR_Construction.ETCurve(None, object(), None, 1000.0, 1000, 0, 0, False)
