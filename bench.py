@@ -1,17 +1,22 @@
 """Benchmark: segment-bounces/s of the split ray tracer.
 
-Default workload (one GPU): the 40 x 25 x 15 m jittered hall with 200 diffusers (~20k triangles),
-2 sources, 16 receivers of radius 0.5 m, 3 s cutoff, 1 ms bins, 1M primary rays.  A step traces
-one batch of primaries (default 131072); the timed steps together cover the 1M-ray job, each step
-tracing its own primaries (ray_begin = step * batch), the warm-up steps trace primaries after them.
---workload shoebox: the 12-triangle 10 x 8 x 4 m shoebox; --workload arena: the 500k-triangle
-120 x 90 x 35 m arena; --workload hall_map: the hall with a 608-receiver audience map (1 m squares at
-1.5 m, the reference's grid walks); --workload batched: the 64-room batch (each room's ray count x
---ray-scale per step) as one batch run with autotuned knobs.
+Default workload (one GPU): the 120 x 90 x 35 m arena (~500k triangles: jittered shell, tiered
+seating facets, 2000 diffuser panels), 4 sources, 64 receivers of radius 0.5 m, 3.5 s cutoff, 1 ms
+bins, 10M primary rays -- the largest single-GPU configuration.  The timed steps together trace the
+10M-ray job: each step traces its own 10M / steps primaries (ray_begin = step * batch); the warm-up
+and kernel-timing steps trace primaries after them.
+--workload hall: the 40 x 25 x 15 m jittered hall (~20k triangles, 2 sources, 16 receivers, 1M rays);
+shoebox: the 12-triangle 10 x 8 x 4 m shoebox (100k rays); hall_map: the hall with a 608-receiver
+audience map (1 m squares at 1.5 m, the reference's grid walks); batched: the 64-room batch (each
+room's ray count x --ray-scale per step) as one batch run with autotuned knobs.
 
 Metric: segment-bounces/s = shoot calls (broadband + octave rays, hit or miss) per second.
-  value  -- device time of the engine's kernels (CUDA events on the engine's stream), scene resident.
-  e2e    -- through the public C ABI from host buffers: scene upload, trace, histogram download.
+  value  -- device time of the engine's device loop (one CUDA-graph launch per step, the product
+            default; CUDA events on the engine's stream), scene resident, summed over the steps.
+  e2e    -- the same job through the public C ABI from host buffers: the scene built from host arrays
+            and uploaded once per job, then every step's trace and its histograms downloaded into
+            pinned host buffers.
+  roofline -- per-kernel CUDA-event times from a separate kernel-timing pass over the same workload.
 The reference arm (--impl reference) times the CPU FP64 restatement of the reference algorithm
 (voxel grid of 7 cells per axis as Pach_Properties defaults) on all host cores: the reference's own
 C# engine cannot run on this machine (no .NET runtime, unvendored geometry library).
@@ -176,8 +181,9 @@ def cpu_baseline(ws, sample_rays, seed):
 
 
 def workload(name, ray_scale):
-    """The rooms of a bench workload: the irregular hall (default), the 12-triangle shoebox, the
-    500k-triangle arena, or the 64-room batch (ray counts scaled by ray_scale)."""
+    """The rooms of a bench workload: the 500k-triangle arena (default), the irregular hall, the
+    12-triangle shoebox, the hall with an audience map, or the 64-room batch (ray counts scaled by
+    ray_scale)."""
     from pachydermacoustic_universal_gb300 import rooms
     if name == "hall":
         return [rooms.irregular_hall_c2()]
@@ -235,6 +241,178 @@ def run_reference_arm(args):
     return 0
 
 
+# ------------------------------------------------------------------------------------------
+# --metric jnd: wall time until T30 and C80 reach one JND, learned emission proposal vs uniform
+# ------------------------------------------------------------------------------------------
+JND = {"T30": 0.05, "EDT": 0.05, "C80": 1.0, "D50": 5.0}   # ISO 3382-1 Annex A; T30/EDT relative
+JND_RELATIVE = {"T30": True, "EDT": True, "C80": False, "D50": False}
+
+
+def _uniform_sources(w):
+    from pachydermacoustic_universal_gb300 import rooms
+    w.sources = [rooms.SourceSpec(s.origin, s.power_db, 2) for s in w.sources]
+    return w
+
+
+def _direct_times(w):
+    c = 331.0 + 0.6 * w.scene.temp_c
+    return [min(np.linalg.norm(np.subtract(r.origin, s.origin)) for s in w.sources) / c for r in w.receivers]
+
+
+def jnd_parameters(E, w, fs=1000):
+    """T30/EDT/C80/D50 [R][8] of raw energy histograms E [R][8][T] (AcousticalMath)."""
+    from pachydermacoustic_universal_gb300.simulation import room_parameters
+    direct = _direct_times(w)
+    out = {k: np.full(E.shape[:2], np.nan) for k in JND}
+    for r in range(E.shape[0]):
+        for o in range(E.shape[1]):
+            p = room_parameters(E[r, o], fs, direct[r])
+            for k in JND:
+                out[k][r, o] = p[k]
+    return out
+
+
+def jnd_runs(w, ds, n_rays, seeds, seed0, raw=None, mix=0.3):
+    """Parameters of independent runs, [seeds][R][8] per name, and device ms per primary."""
+    from pachydermacoustic_universal_gb300 import proposal, tracer
+    acc = {k: [] for k in JND}
+    dev_ms = 0.0
+    for s in range(seeds):
+        if raw is None:
+            h, st = tracer.trace(w, dscene=ds, rays=n_rays, seed=seed0 + s)
+        else:
+            h, st = proposal.trace_learned(w, raw, mix=mix, dscene=ds, rays=n_rays, seed=seed0 + s)
+        dev_ms += st["device_ms"]
+        p = jnd_parameters(h["energy"], w)
+        for k in JND:
+            acc[k].append(p[k])
+    return {k: np.asarray(v) for k, v in acc.items()}, dev_ms / (seeds * n_rays)
+
+
+def rays_to_jnd(P, n_rays):
+    """Per parameter: primaries until its standard error is one JND, for every receiver and band (the
+    largest over them).  Both estimators are unbiased, so the expected squared error at N rays is the
+    variance sigma^2 / N, estimated from the seed spread of runs of n_rays."""
+    out = {}
+    for k, v in P.items():
+        ok = np.all(np.isfinite(v), axis=0)
+        if not ok.any():
+            out[k] = float("nan")
+            continue
+        sd = v.std(axis=0, ddof=1)
+        if JND_RELATIVE[k]:
+            sd = sd / np.abs(v.mean(axis=0))
+        n = n_rays * (sd / JND[k]) ** 2
+        out[k] = float(np.max(n[ok]))
+    return out
+
+
+def bias_z(Pu, Pl):
+    """Largest |mean difference| / combined standard error over receivers and bands, per parameter."""
+    z = {}
+    for k in JND:
+        a, b = Pu[k], Pl[k]
+        ok = np.all(np.isfinite(a), axis=0) & np.all(np.isfinite(b), axis=0)
+        if not ok.any():
+            z[k] = float("nan")
+            continue
+        se = np.sqrt(a.var(axis=0, ddof=1) / a.shape[0] + b.var(axis=0, ddof=1) / b.shape[0])
+        d = np.abs(a.mean(axis=0) - b.mean(axis=0)) / np.maximum(se, 1e-30)
+        z[k] = float(np.max(d[ok]))
+    return z
+
+
+def _gmean(x):
+    x = np.asarray([v for v in x if np.isfinite(v) and v > 0])
+    return float(np.exp(np.mean(np.log(x)))) if x.size else float("nan")
+
+
+def jnd_study(train_rooms, train_rays, eval_rooms, eval_rays, seeds, steps, lr=1e-3, mix=0.3, seed=7,
+              train_receivers=12, target="linear"):
+    """Learned vs uniform emission on seeded rooms drawn like the 10 x 8 x 4 m shoebox
+    (rooms.proposal_room_c4).
+
+    1. Training data: train_rooms rooms traced with uniform emission and capture on (train_rays
+       primaries, train_receivers receivers each), one target distribution per receiver; a tenth of
+       the rooms is held back for the validation loss.
+    2. Training: full-batch Adam on the GPU (pach_mlp_train, the library's tcgen05 kernels).
+    3. Evaluation on eval_rooms further rooms: `seeds` runs of eval_rays primaries each with uniform
+       emission and with the learned proposal (defensive mixture, uniform weight `mix`); rays to one
+       JND from the seed spread (rays_to_jnd), times the measured device ms per primary of each method.
+       A room's time for "T30 and C80 within 1 JND" is the largest over both parameters, every
+       receiver and band.
+    4. Bias check: learned mean against uniform mean per parameter, in combined standard errors."""
+    from pachydermacoustic_universal_gb300 import proposal, rooms, tracer
+    t0 = time.perf_counter()
+    rooms_train = [rooms.proposal_room_c4(1000 + i, n_receivers=train_receivers) for i in range(train_rooms)]
+    cond, tgt, t_collect = proposal.collect(rooms_train, train_rays, seed=seed, target=target)
+    n_val = max(1, train_rooms // 10) * train_receivers
+    net = proposal.ProposalNet(seed=seed, max_rows=max(cond.shape[0], 128))
+    net.set_data(cond[n_val:], tgt[n_val:])
+    t1 = time.perf_counter()
+    curve = np.concatenate([net.train(steps // 2, lr=lr), net.train(steps - steps // 2, lr=lr * 0.3)])
+    t_train = time.perf_counter() - t1
+    net.set_data(cond[:n_val], tgt[:n_val])
+    val_loss, _ = net.loss_grad(with_grad=False)
+    per_room = []
+    for i in range(eval_rooms):
+        w = _uniform_sources(rooms.proposal_room_c4(5000 + i))
+        ds = tracer.DeviceScene(w.scene)
+        raw = net.forward(proposal.conditions(w))
+        Pu, ms_u = jnd_runs(w, ds, eval_rays, seeds, 10_000 * (i + 1))
+        Pl, ms_l = jnd_runs(w, ds, eval_rays, seeds, 10_000 * (i + 1) + 5000, raw=raw, mix=mix)
+        nu, nl = rays_to_jnd(Pu, eval_rays), rays_to_jnd(Pl, eval_rays)
+        rec = {"rays_to_jnd": {"uniform": nu, "learned": nl}, "bias_z": bias_z(Pu, Pl), "ms_to_jnd": {}}
+        for name, keys in (("T30_C80", ("T30", "C80")), ("all", tuple(JND))):
+            rec["ms_to_jnd"][name] = {"uniform": max(nu[k] for k in keys) * ms_u,
+                                      "learned": max(nl[k] for k in keys) * ms_l}
+        ds.close()
+        per_room.append(rec)
+    net.close()
+    extra = 1000.0 * (t_collect + t_train) / max(1, eval_rooms)  # one-off cost spread over the evaluated rooms
+    res = {"train_loss": float(curve[-1]), "val_loss": float(val_loss), "collect_s": t_collect, "train_s": t_train}
+    for k in JND:
+        res[f"speedup_rays_{k}"] = _gmean([r["rays_to_jnd"]["uniform"][k] / r["rays_to_jnd"]["learned"][k]
+                                           for r in per_room])
+    for name in ("T30_C80", "all"):
+        tu = [r["ms_to_jnd"][name]["uniform"] for r in per_room]
+        tl = [r["ms_to_jnd"][name]["learned"] for r in per_room]
+        res[f"wall_ms_to_jnd_{name}"] = {"uniform": _gmean(tu), "learned": _gmean(tl),
+                                         "speedup": _gmean([a / b for a, b in zip(tu, tl)]),
+                                         "learned_incl_training": _gmean(tl) + extra,
+                                         "speedup_incl_training": _gmean(tu) / (_gmean(tl) + extra)}
+    res["max_bias_z"] = {k: float(np.nanmax([r["bias_z"][k] for r in per_room])) for k in JND}
+    res["bias_comparisons"] = int(eval_rooms * 3 * 8)
+    res["wall_s"] = time.perf_counter() - t0
+    return res
+
+
+def run_jnd_arm(args):
+    """One JSON line: wall time to T30 and C80 within 1 JND, learned proposal against uniform emission."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    from pachydermacoustic_universal_gb300 import _capi
+    _capi.lib()
+    res = jnd_study(args.train_rooms, args.train_rays, args.eval_rooms, args.eval_rays, args.seeds, args.train_steps,
+                    mix=args.mix, seed=args.seed, target=args.target)
+    t = res["wall_ms_to_jnd_T30_C80"]
+    line = {"metric": "wall time to T30/C80 <= 1 JND, learned vs uniform (1 GB300)", "value": t["speedup"],
+            "unit": "x (uniform time / learned time, geometric mean over held-out rooms)", "n_gpus": 1,
+            "higher_is_better": True, "vs_baseline": None, "dtype": "f32 geometry, f64 histograms, bf16 network",
+            "data": "synthetic (seeded rooms drawn like the 10 x 8 x 4 m shoebox)",
+            "config": {"workload": "learned_proposal_rooms", "train_rooms": args.train_rooms,
+                       "train_rays_per_room": args.train_rays, "train_receivers": 12, "eval_rooms": args.eval_rooms,
+                       "eval_rays_per_run": args.eval_rays, "seeds_per_method": args.seeds,
+                       "train_steps": args.train_steps, "uniform_mix": args.mix, "target": args.target,
+                       "network": "12 -> 3 x 256 GELU -> 32 vMF lobes (160), BF16 tcgen05, FP32 accumulate"},
+            "jnd": res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def scene_bytes(scene):
     return int(scene.vertices.nbytes + scene.poly_offsets.nbytes + scene.poly_indices.nbytes +
                scene.absorption.nbytes + scene.scattering.nbytes + scene.transmission.nbytes)
@@ -246,8 +424,24 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hall", choices=["hall", "shoebox", "batched", "arena", "hall_map"])
-    ap.add_argument("--batch", type=int, default=131072, help="primaries per step (single-room workloads)")
+    ap.add_argument("--metric", default="bounces", choices=["bounces", "jnd"],
+                    help="bounces: segment-bounces/s (default); jnd: wall time to 1 JND, learned vs uniform")
+    ap.add_argument("--train-rooms", type=int, default=100, help="jnd: training rooms")
+    ap.add_argument("--train-rays", type=int, default=20000, help="jnd: uniform primaries per training room")
+    ap.add_argument("--eval-rooms", type=int, default=12, help="jnd: held-out rooms")
+    ap.add_argument("--eval-rays", type=int, default=4000, help="jnd: primaries per evaluation run")
+    ap.add_argument("--seeds", type=int, default=8, help="jnd: runs per method and room")
+    ap.add_argument("--train-steps", type=int, default=3000, help="jnd: Adam steps")
+    ap.add_argument("--mix", type=float, default=0.3, help="jnd: weight of uniform emission in the proposal")
+    ap.add_argument("--target", default="linear", choices=["linear", "l2"], help="jnd: training target")
+    ap.add_argument("--workload", default="arena", choices=["hall", "shoebox", "batched", "arena", "hall_map"])
+    ap.add_argument("--rays-total", type=int, default=None,
+                    help="primaries the timed steps trace together (default: the workload's job, arena 10M)")
+    ap.add_argument("--batch", type=int, default=None, help="primaries per step (default: rays_total / steps)")
+    ap.add_argument("--timing-steps", type=int, default=3, help="steps of the per-kernel timing pass (roofline)")
+    ap.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: all timed steps)")
+    ap.add_argument("--ring-log2", type=int, default=0,
+                    help="ring queue of 2^n octave rays (0: the engine's default; small cases for profiling)")
     ap.add_argument("--ray-scale", type=float, default=0.004, help="batched: fraction of each room's rays per step")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-sample", type=int, default=None,
@@ -258,12 +452,14 @@ def main():
     args = ap.parse_args()
     # bounded CPU samples: the FP64 restatement's grid makes a 500k-triangle arena ~100x slower per segment
     if args.cpu_sample is None:
-        args.cpu_sample = {"hall": 3000, "shoebox": 3000, "batched": 400, "arena": 40, "hall_map": 3000}[args.workload]
+        args.cpu_sample = {"hall": 3000, "shoebox": 3000, "batched": 400, "arena": 400, "hall_map": 3000}[args.workload]
     if args.ref_sample is None:
-        args.ref_sample = {"hall": 200, "shoebox": 200, "batched": 200, "arena": 8, "hall_map": 200}[args.workload]
+        args.ref_sample = {"hall": 200, "shoebox": 200, "batched": 200, "arena": 48, "hall_map": 200}[args.workload]
 
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.metric == "jnd":
+        return run_jnd_arm(args)
 
     ws, rank, local = dist_env()
     import torch
@@ -275,9 +471,14 @@ def main():
     batched = len(rooms_) > 1
     scenes = tracer.DeviceScene.many([w.scene for w in rooms_])
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
-    B = sum(w.rays for w in rooms_) if batched else args.batch
+    if batched:
+        B = sum(w.rays for w in rooms_)
+    else:
+        total = args.rays_total or rooms_[0].rays
+        B = args.batch or -(-total // args.steps)
+    n_steps_all = args.warmup + args.steps + args.timing_steps
     # this rank's primaries: steps are consecutive batches; ranks own disjoint ranges
-    base = rank * (args.warmup + args.steps) * B
+    base = rank * n_steps_all * B
     tune = None
     if batched:  # packet size and block shape from the autotuner (timed before the warm-up, cached)
         tune = tracer.autotune(rooms_, dscenes=scenes, sample_rays=min(B, 20000), seed=args.seed)
@@ -294,12 +495,12 @@ def main():
                   "dir_pos": _pin((R_all, 3, 8, T_all)), "dir_neg": _pin((R_all, 3, 8, T_all)),
                   "analysis": _pin((R_all, 3, 8, T_all))}
 
-    def step_trace(idx, e2e=False):
-        kw = dict(seed=args.seed, ray_begin=base + idx * B, kernel_timing=not e2e)
+    def step_trace(idx, ds, timing=False, out=None):
+        """One step: primaries [base + idx B, base + (idx + 1) B) through the public API.  timing: the
+        host-driven loop with CUDA events around every kernel (per-kernel times), else the product
+        default, one CUDA-graph launch of the whole device loop."""
+        kw = dict(seed=args.seed, ray_begin=base + idx * B, kernel_timing=timing, ring_log2=args.ring_log2)
         t0 = time.perf_counter()
-        # e2e: the public API from host buffers -- upload the scenes, trace, download the histograms
-        ds = tracer.DeviceScene.many([w.scene for w in rooms_]) if e2e else scenes
-        out = pinned if e2e else None
         if batched:
             h, s = tracer.trace_batch(rooms_, dscenes=ds, tune=tune, out=out, **kw)
         else:
@@ -309,14 +510,12 @@ def main():
             h, s = tracer.trace(rooms_[0], dscene=ds[0], rays=B, out=out, **kw)
             h.pop("map", None)
             h = [h]
-        if e2e:
-            for d in ds:
-                d.close()
         return h, s, time.perf_counter() - t0
 
+    # step indices: [0, steps) timed, then the warm-up steps, then the kernel-timing steps
     for i in range(args.warmup):
         flush.zero_()
-        step_trace(args.steps + i)
+        step_trace(args.steps + i, scenes)
     torch.cuda.synchronize()
     barrier(dist)
     sampler = ClockSampler()
@@ -327,7 +526,7 @@ def main():
     for i in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        _, s, _ = step_trace(i)
+        _, s, _ = step_trace(i, scenes)
         dev_ms += s["device_ms"]
         segs += s["segments"]
         launches += s["kernel_launches"]
@@ -340,29 +539,48 @@ def main():
     segs_all = sum_over_ranks(dist, segs, device=f"cuda:{local}")
     value = segs_all / (dev_ms_max * 1e-3)
 
-    # e2e through the C ABI with host buffers (scene upload + histogram download each step)
+    # per-kernel times (roofline): the host-driven loop with CUDA events around every kernel
+    tstats = []
+    for i in range(args.timing_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        tstats.append(step_trace(args.steps + args.warmup + i, scenes, timing=True)[1])
+    if not tstats:
+        tstats = stats
+
+    # e2e through the C ABI with host buffers: the scene built from the host arrays and uploaded once
+    # per job, then every step's trace with its histograms downloaded into pinned host buffers
     e2e = None
     if not args.no_e2e:
-        e_steps = max(1, min(args.steps, 3))
-        tt, es = 0.0, 0
-        h2d = d2h = 0
+        e_steps = max(1, min(args.steps, args.e2e_steps or args.steps))
+        torch.cuda.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        ds = tracer.DeviceScene.many([w.scene for w in rooms_])
+        t_scene = time.perf_counter() - t0
+        es = 0
         for i in range(e_steps):
-            h, s, dt = step_trace(i, e2e=True)
-            tt += dt
+            h, s, _ = step_trace(i, ds, out=pinned)
             es += s["segments"]
-            h2d = sum(scene_bytes(w.scene) + 88 * len(w.sources) + 32 * len(w.receivers) for w in rooms_)
-            d2h = int(sum(v.nbytes for hh in h for v in hh.values()))
+        for d in ds:
+            d.close()
+        torch.cuda.synchronize()
+        tt = time.perf_counter() - t0
         tt = max_over_ranks(dist, tt, device=f"cuda:{local}")
         es = sum_over_ranks(dist, es, device=f"cuda:{local}")
+        h2d_scene = sum(scene_bytes(w.scene) for w in rooms_)
+        h2d = int(h2d_scene / e_steps) + sum(88 * len(w.sources) + 32 * len(w.receivers) for w in rooms_)
+        d2h = int(sum(v.nbytes for hh in h for v in hh.values()))
         e2e = {"value": es / tt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "steps": e_steps, "includes": "scene build and upload, trace, histogram download into pinned host "
-                                             "buffers"}
+               "steps": e_steps, "scene_build_upload_s": t_scene, "wall_s": tt,
+               "includes": "one scene build (host BVH) and upload per job, then per step: run set-up, trace, "
+                           "histogram download into pinned host buffers; scene bytes amortised over the steps"}
 
     peaks, peak_kind = _peaks()
-    agg = {k: sum(s[k] for s in stats) for k in ("segments", "detections", "fp64_retests", "octave_rays",
-                                                   "segments_broadband", "segments_phase_b", "segments_phase_c",
-                                                   "trace_ms", "shade_ms", "broadband_ms", "waves",
-                                                   "bvh_nodes_visited", "tri_tests")}
+    agg = {k: sum(s[k] for s in tstats) for k in ("segments", "detections", "fp64_retests", "octave_rays",
+                                                    "segments_broadband", "segments_phase_b", "segments_phase_c",
+                                                    "trace_ms", "shade_ms", "broadband_ms", "waves",
+                                                    "bvh_nodes_visited", "tri_tests", "device_ms")}
     # HBM roofline of the dominant wavefront kernel, algorithmic bytes per octave-ray segment:
     #   k_trace  reads the ray's position, direction and plane (48 B) and writes (triangle, t) (8 B);
     #   k_shade  reads the 64 B ray and its 8 B hit, writes the surviving ray and split children
@@ -383,6 +601,8 @@ def main():
     tris = sum(w.scene.n_triangles for w in rooms_)
     cfg = {"workload": rooms_[0].name if not batched else f"batched_{len(rooms_)}_rooms",
            "rays_per_step": B, "rays_total": B * args.steps * ws, "triangles": tris,
+           "timing": "graph-mode device loop per step (CUDA events); per-kernel times from "
+                     f"{len(tstats)} further kernel-timing steps",
            "sources": sum(len(w.sources) for w in rooms_), "receivers": sum(len(w.receivers) for w in rooms_),
            "cutoff_s": max(w.cutoff_s for w in rooms_), "bins_ms": 1, "l2": "256 MiB buffer written between steps",
            "bvh_nodes_leaves_depth": stats[0]["accel"], "walk": stats[0]["walk"]}
@@ -419,16 +639,38 @@ def main():
                    "octave_rays": agg["octave_rays"], "peak_live_rays": max(s["peak_live_rays"] for s in stats),
                    "bvh_nodes_per_segment": agg["bvh_nodes_visited"] / max(1, seg_oct),
                    "tri_tests_per_segment": agg["tri_tests"] / max(1, seg_oct),
-                   "segments_phase_c_frac": agg["segments_phase_c"] / max(1, agg["segments"])},
+                   "segments_phase_c_frac": agg["segments_phase_c"] / max(1, agg["segments"]),
+                   "kernel_timing_pass_segments_per_s": agg["segments"] / max(agg["device_ms"] * 1e-3, 1e-30)},
     }
-    traffic_file = os.path.join(ROOT, "profiles", f"{kern}_traffic.json")
-    if os.path.exists(traffic_file) and not batched:
-        try:
-            tr = json.load(open(traffic_file))
-            line["roofline"]["traffic"] = tr.get("dram_bytes_per_segment", 0) * seg_oct / max(1, oct_launch)
-            line["roofline"]["traffic_source"] = tr.get("source")
-        except Exception:
-            pass
+    # ncu figures per octave segment of the dominant kernel on this workload (profiles/roofline_inputs.json):
+    # DRAM bytes (-> traffic per launch) and executed lane-instructions (-> the issue roofline)
+    prof = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_inputs.json")) as f:
+            prof = json.load(f).get(args.workload, {}).get(kern, {})
+    except (OSError, ValueError):
+        prof = {}
+    if prof.get("dram_bytes_per_segment") and not batched:
+        line["roofline"]["traffic"] = prof["dram_bytes_per_segment"] * seg_oct / max(1, oct_launch)
+        line["roofline"]["traffic_source"] = prof.get("source")
+    if prof.get("thread_inst_per_segment") and k_ms > 0:
+        # The walk is bound by instruction issue, not HBM: useful lane-instructions per second against
+        # the SM issue peak, SMs x 4 schedulers x 32 lanes x the sampled SM clock.
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        lane_peak = sms * 4 * 32 * mhz * 1e6
+        lane_rate = prof["thread_inst_per_segment"] * seg_oct / (k_ms * 1e-3)
+        warp_rate = prof.get("warp_inst_per_segment", 0.0) * seg_oct / (k_ms * 1e-3)
+        line["roofline"]["binding"] = {
+            "resource": "issue", "kernel": kern, "achieved": lane_rate / 1e12, "peak": lane_peak / 1e12,
+            "unit": "T lane-instructions/s", "frac": lane_rate / lane_peak,
+            "warp_issue_frac": warp_rate / (lane_peak / 32),
+            "lanes_active_per_warp_instruction": (prof["thread_inst_per_segment"] /
+                                                  max(prof.get("warp_inst_per_segment", 0.0), 1e-30)),
+            "per_unit": f"{prof['thread_inst_per_segment']:.0f} lane-instructions and "
+                        f"{prof.get('warp_inst_per_segment', 0.0):.0f} warp-instructions per octave segment (ncu)",
+            "peak_source": f"{sms} SMs x 4 schedulers x 32 lanes x {mhz:.0f} MHz (sampled)",
+            "source": prof.get("source")}
     if rank == 0 and ws >= 1 and not args.no_cpu_baseline:
         sample_rooms = rooms_[:4]
         cb, st = cpu_baseline(sample_rooms, args.cpu_sample, args.seed)
