@@ -235,8 +235,10 @@ int pach_device_count(void);
 
 pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out);
 /* n scenes at once (a batch's rooms): the host builds (BVH, materials) run on `threads` host threads
- * (0 = all cores), the device copies go to the calling thread's device.  On failure no scene is
- * returned. */
+ * (0 = all cores); the scenes belong to the calling thread's device.  Each scene's own device copy is
+ * made on its first single-room use (pach_trace_begin, pach_trace_specular_paths, pach_direct_sound),
+ * since a batch run uploads the concatenation of its rooms instead; pach_trace_run_noalloc, which
+ * allocates nothing, needs a scene from pach_scene_create.  On failure no scene is returned. */
 pach_status pach_scenes_create(const pach_scene_desc *descs, int32_t n, pach_scene **out, int32_t threads);
 void pach_scene_destroy(pach_scene *scene);
 /* Scene facts the SplitRayTracer ctor derives (Scene.SurfaceArea, Sound_speed, Rho_C, Attenuation). */

@@ -58,7 +58,10 @@ struct pach_scene {
     HostScene hs;
     DevScene dev{};
     DevMem tri, tri64, norm, mat, trans, bvh, bvhq;
-    std::mutex mu;
+    // the device copy above exists (pach_scene_create makes it at once; pach_scenes_create leaves it to the
+    // first single-room use, since a batch run uploads the concatenation of its rooms instead)
+    bool on_device = false;
+    std::mutex mu;  // guards the first upload
     ~pach_scene() {
         cudaSetDevice(device);
         for (DevMem *m : {&tri, &tri64, &norm, &mat, &trans, &bvh, &bvhq}) m->release();
@@ -256,6 +259,18 @@ cudaError_t upload_scene(const SceneArrays &A, DevMem &tri, DevMem &tri64, DevMe
     return cudaSuccess;
 }
 
+// The scene's own device arrays, uploaded on first use (single-room runs, the specular-path and
+// direct-sound probes); the caller has made the scene's device current.
+cudaError_t scene_upload(pach_scene *sc) {
+    std::lock_guard<std::mutex> lk(sc->mu);
+    if (sc->on_device) return cudaSuccess;
+    SceneArrays A;
+    append_scene(sc->hs, A);
+    const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->bvhq, sc->dev);
+    if (e == cudaSuccess) sc->on_device = true;
+    return e;
+}
+
 // SplitRayTracer ctor values of one room (TaskAll:83-109): COTime from the cutoff length, h_oct (the
 // band of least total absorption among bands carrying >= 1e-6 of the peak power; a SourceCluster's
 // power is the per-band maximum over members, Classes_Sources.cs:680-688) and the phase-A bound.
@@ -362,6 +377,7 @@ void run_worker_body(pach_run *run) {
         if (e) break;
 
         // scene: the first room's own device arrays, or the concatenation of every room's
+        if (n_rooms == 1) TRY(scene_upload(sc));
         DevScene S = sc->dev;
         std::vector<int> roots(n_rooms, 0);
         if (n_rooms > 1) {
@@ -1023,9 +1039,7 @@ pach_status pach_scene_create(const pach_scene_desc *desc, pach_scene **out) {
         if (pach_device_count() <= 0)
             return fail(PACH_ERR_NO_DEVICE, "no CUDA device visible: the GB300 engine has no CPU fallback");
         cudaGetDevice(&sc->device);
-        SceneArrays A;
-        append_scene(sc->hs, A);
-        const cudaError_t e = upload_scene(A, sc->tri, sc->tri64, sc->norm, sc->mat, sc->trans, sc->bvh, sc->bvhq, sc->dev);
+        const cudaError_t e = scene_upload(sc.get());
         if (e != cudaSuccess)
             return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
         *out = sc.release();
@@ -1081,16 +1095,10 @@ pach_status pach_scenes_create(const pach_scene_desc *descs, int32_t n, pach_sce
             if (!sc[(size_t)i])
                 return fail(oom[(size_t)i] ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_INVALID_ARGUMENT,
                             "scene " + std::to_string(i) + ": " + errs[(size_t)i]);
-        // device copies on the caller's device
-        for (int i = 0; i < n; ++i) {
-            pach_scene *s = sc[(size_t)i].get();
-            s->device = device;
-            SceneArrays A;
-            append_scene(s->hs, A);
-            const cudaError_t e = upload_scene(A, s->tri, s->tri64, s->norm, s->mat, s->trans, s->bvh, s->bvhq, s->dev);
-            if (e != cudaSuccess)
-                return fail(e == cudaErrorMemoryAllocation ? PACH_ERR_OUT_OF_MEMORY : PACH_ERR_CUDA, cuda_msg(e, "scene upload"));
-        }
+        // the scenes belong to the caller's device; each one's device copy is made on its first
+        // single-room use (a batch run uploads the concatenation of its rooms, so a batch's scenes are
+        // uploaded once, not twice)
+        for (int i = 0; i < n; ++i) sc[(size_t)i]->device = device;
         for (int i = 0; i < n; ++i) out[i] = sc[(size_t)i].release();
         return PACH_OK;
     }, fail);
@@ -1528,7 +1536,7 @@ pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double
         DevMem o, d, pl, t, pt;
         const size_t k = (size_t)n * max_bounces;
         cudaError_t e;
-        if ((e = upload(o, origins, sizeof(double) * 3 * n)) || (e = upload(d, dirs, sizeof(double) * 3 * n)) ||
+        if ((e = scene_upload(scene)) || (e = upload(o, origins, sizeof(double) * 3 * n)) || (e = upload(d, dirs, sizeof(double) * 3 * n)) ||
             (e = pl.alloc(sizeof(int32_t) * k)) || (e = t.alloc(sizeof(double) * k)) || (e = pt.alloc(sizeof(double) * 3 * k)) ||
             (e = launch_paths(scene->dev, n, o.as<double>(), d.as<double>(), max_bounces, pl.as<int>(), t.as<double>(),
                               pt.as<double>(), 0)) ||
@@ -1620,7 +1628,8 @@ pach_status pach_direct_sound(pach_scene *scene, const pach_source_desc *sources
         std::vector<int> v(npair);
         std::vector<double> tm(npair * kBands);
         cudaError_t e;
-        if ((e = upload(ds, s3.data(), s3.size() * sizeof(double))) || (e = upload(dr, r3.data(), r3.size() * sizeof(double))) ||
+        if ((e = scene_upload(scene)) || (e = upload(ds, s3.data(), s3.size() * sizeof(double))) ||
+            (e = upload(dr, r3.data(), r3.size() * sizeof(double))) ||
             (e = dv.alloc(npair * sizeof(int))) || (e = dt.alloc(npair * kBands * sizeof(double))) ||
             (e = launch_direct(scene->dev, ds.as<double>(), n_sources, dr.as<double>(), n_receivers, 64, dv.as<int>(),
                                dt.as<double>(), 0)) ||
@@ -1677,7 +1686,7 @@ pach_status pach_proposal_sample(const float *proposal, int32_t n_prop, double m
 // Read access to scene handles for entry points defined in other translation units.
 namespace pach {
 const HostScene *scene_host(const pach_scene *s) { return s ? &s->hs : nullptr; }
-const DevScene *scene_dev(const pach_scene *s) { return s ? &s->dev : nullptr; }
+const DevScene *scene_dev(const pach_scene *s) { return s && s->on_device ? &s->dev : nullptr; }
 int scene_device(const pach_scene *s) { return s ? s->device : -1; }
 void set_last_error(const char *msg) { g_err = msg; }
 }  // namespace pach

@@ -505,8 +505,11 @@ __device__ __forceinline__ void map_walk(const MapDev &M, float3 o, float3 d, fl
         if (!quirk) s = o + d * t0;
     }
     const float sp[3] = {s.x, s.y, s.z}, ep[3] = {end.x, end.y, end.z};
-    // the quantity whose sign and size steer the walk: the direction, or the reference broadband walk's position
-    const float g[3] = {quirk ? o.x : d.x, quirk ? o.y : d.y, quirk ? o.z : d.z};
+    // the quantity whose sign and size steer the walk: the direction, or the reference broadband walk's
+    // position; a direction component of -0 walks as +0 (its crossing time is +inf, never -inf)
+    float g[3] = {quirk ? o.x : d.x, quirk ? o.y : d.y, quirk ? o.z : d.z};
+    if (!quirk)
+        for (int a = 0; a < 3; ++a) g[a] = g[a] == 0.f ? 0.f : g[a];
     int c[3], ce[3], step[3];
     float tmax[3], tdel[3];
 #pragma unroll

@@ -96,6 +96,11 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
         base = g_scratch_addr[dev];
     }
 
+    // The scene's device arrays must exist already: this call does not upload (it would allocate).
+    if (!scene_dev(scene))
+        return na_fail(PACH_ERR_INVALID_ARGUMENT, "the scene has no device copy yet (a scene of pach_scenes_create is "
+                                                  "uploaded by its first single-room run); use pach_scene_create");
+
     // The ctor's derived quantities (TaskAll:83-109): COTime, h_oct, and the phase-A bound.
     const HostScene &hs = *scene_host(scene);
     double total_abs[kBands] = {0}, power[kBands] = {0};
