@@ -17,6 +17,8 @@ Metric: segment-bounces/s = shoot calls (broadband + octave rays, hit or miss) p
             and uploaded once per job, then every step's trace and its histograms downloaded into
             pinned host buffers.
   roofline -- per-kernel CUDA-event times from a separate kernel-timing pass over the same workload.
+  jnd    -- (arena line) the metric's second half at a compact size: wall time to T30/C80 within 1 JND,
+            learned emission proposal against uniform emission (--metric jnd runs the larger study).
 The reference arm (--impl reference) times the CPU FP64 restatement of the reference algorithm
 (voxel grid of 7 cells per axis as Pach_Properties defaults) on all host cores: the reference's own
 C# engine cannot run on this machine (no .NET runtime, unvendored geometry library).
@@ -434,12 +436,16 @@ def main():
     ap.add_argument("--train-steps", type=int, default=3000, help="jnd: Adam steps")
     ap.add_argument("--mix", type=float, default=0.3, help="jnd: weight of uniform emission in the proposal")
     ap.add_argument("--target", default="linear", choices=["linear", "l2"], help="jnd: training target")
+    ap.add_argument("--no-jnd", action="store_true",
+                    help="skip the compact learned-vs-uniform JND study the default arena line carries")
     ap.add_argument("--workload", default="arena", choices=["hall", "shoebox", "batched", "arena", "hall_map"])
     ap.add_argument("--rays-total", type=int, default=None,
                     help="primaries the timed steps trace together (default: the workload's job, arena 10M)")
     ap.add_argument("--batch", type=int, default=None, help="primaries per step (default: rays_total / steps)")
     ap.add_argument("--timing-steps", type=int, default=3, help="steps of the per-kernel timing pass (roofline)")
     ap.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: all timed steps)")
+    ap.add_argument("--ray-sort", type=int, default=0,
+                    help="1: order each wave by direction octant and origin cell before the walk (opt-in)")
     ap.add_argument("--ring-log2", type=int, default=0,
                     help="ring queue of 2^n octave rays (0: the engine's default; small cases for profiling)")
     ap.add_argument("--ray-scale", type=float, default=0.004, help="batched: fraction of each room's rays per step")
@@ -499,7 +505,8 @@ def main():
         """One step: primaries [base + idx B, base + (idx + 1) B) through the public API.  timing: the
         host-driven loop with CUDA events around every kernel (per-kernel times), else the product
         default, one CUDA-graph launch of the whole device loop."""
-        kw = dict(seed=args.seed, ray_begin=base + idx * B, kernel_timing=timing, ring_log2=args.ring_log2)
+        kw = dict(seed=args.seed, ray_begin=base + idx * B, kernel_timing=timing, ring_log2=args.ring_log2,
+                  ray_sort=args.ray_sort)
         t0 = time.perf_counter()
         if batched:
             h, s = tracer.trace_batch(rooms_, dscenes=ds, tune=tune, out=out, **kw)
@@ -687,6 +694,19 @@ def main():
                                   "reference_work_gbs": bytes_seg * value / 1e9,
                                   "note": "work the reference traversal (grid domain 7) does for the same "
                                           "segments, at this run's segment rate"}
+    if rank == 0 and not args.no_jnd and args.workload == "arena":
+        # the metric's second half, measured in the same run at a compact size (bench.py --metric jnd
+        # runs the larger study): wall time to T30 and C80 within 1 JND, learned proposal vs uniform
+        res = jnd_study(40, 20000, 8, 4000, 8, 2000, mix=0.3, seed=args.seed)
+        t = res["wall_ms_to_jnd_T30_C80"]
+        line["jnd"] = {"metric": "wall time to T30/C80 <= 1 JND, learned vs uniform",
+                       "speedup": t["speedup"], "uniform_ms": t["uniform"], "learned_ms": t["learned"],
+                       "learned_incl_training_ms": t["learned_incl_training"],
+                       "speedup_rays": {k: res[f"speedup_rays_{k}"] for k in JND},
+                       "max_bias_z": res["max_bias_z"], "collect_s": res["collect_s"], "train_s": res["train_s"],
+                       "config": "40 training rooms x 12 receivers x 20k uniform primaries, 2000 Adam steps; "
+                                 "8 held-out rooms x 8 seeds x 4000 primaries per method; uniform weight 0.3",
+                       "wall_s": res["wall_s"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
