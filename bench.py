@@ -17,6 +17,9 @@ Metric: segment-bounces/s = shoot calls (broadband + octave rays, hit or miss) p
             and uploaded once per job, then every step's trace and its histograms downloaded into
             pinned host buffers.
   roofline -- per-kernel CUDA-event times from a separate kernel-timing pass over the same workload.
+  filters -- the receivers' filters (7 per receiver, FP64 FFT convolution on the GPU) of the last
+            end-to-end step's histograms: device time, end to end through the host-array call, and the
+            FP64 oracle per filter on one host core (--metric filters prints this as its own line).
   jnd    -- (arena line) the metric's second half at a compact size: wall time to T30/C80 within 1 JND,
             learned emission proposal against uniform emission (--metric jnd runs the larger study).
 The reference arm (--impl reference) times the CPU FP64 restatement of the reference algorithm
@@ -415,6 +418,105 @@ def run_jnd_arm(args):
     return 0
 
 
+def filters_measure(h0, fs, reps, flush, device):
+    """Receiver filters (Directional_Histogram.Create_Filter, 7 per receiver) of one step's histograms:
+    device time of the filter kernels (CUDA events on the launching stream, L2 flushed between calls),
+    the host-array call end to end, and the FP64 oracle on the host cores for one receiver."""
+    import torch
+    import ctypes as C
+    from pachydermacoustic_universal_gb300 import _capi, tracer
+    L = _capi.lib()
+    E, P, Dp, Dn = (np.ascontiguousarray(h0[k]) for k in ("energy", "pressure", "dir_pos", "dir_neg"))
+    R, _, T = P.shape
+    n = R * 7
+    d = {k: torch.from_numpy(v).to(device) for k, v in dict(E=E, P=P, Dp=Dp, Dn=Dn).items()}
+    wsb = L.pach_filters_workspace_bytes(n, T)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=device)
+    out = torch.empty((R, 7, T + 12287), dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream(device)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def call():
+        _capi.check(L.pach_filters_device(d["E"].data_ptr(), d["P"].data_ptr(), d["Dp"].data_ptr(), d["Dn"].data_ptr(),
+                                          None, R, T, 7, fs, None, 4096, out.data_ptr(), ws.data_ptr(), wsb, sp))
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    ms = 0.0
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    ms /= reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        tracer.receiver_filters(P, E, Dp, Dn, sample_rate=fs)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+    from oracle import filters as OF
+    t0 = time.perf_counter()
+    OF.receiver_filters(E[0], P[0], Dp[0], Dn[0], [120.0] * 8, fs)
+    cpu_ms = (time.perf_counter() - t0) * 1e3 / 7
+    geo = 1 << (T + 16383 - 1).bit_length()
+    roof = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_inputs.json")) as f:
+            fp = json.load(f).get("filters", {})
+    except (OSError, ValueError):
+        fp = {}
+    if fp.get("dp_inst_per_filter") and geo == 32768:
+        # FP64 issue: DP lane-instructions per second against SMs x 2 FP64 lanes x the SM clock
+        props = torch.cuda.get_device_properties(device)
+        mhz = (_peaks()[0] or {}).get("sm_max_mhz", 2070.0)
+        peak = props.multi_processor_count * fp["fp64_lanes_per_sm_cycle"] * mhz * 1e6
+        ach = fp["dp_inst_per_filter"] * n / (ms * 1e-3)
+        roof = {"bound": "fp64 issue", "achieved": ach / 1e9, "peak": peak / 1e9, "unit": "G DP lane-instructions/s",
+                "frac": ach / peak, "per_unit": f"{fp['dp_inst_per_filter'] / 1e6:.2f} M DP instructions per filter "
+                                                "of a 32768-point transform (ncu)",
+                "peak_source": f"{props.multi_processor_count} SMs x {fp['fp64_lanes_per_sm_cycle']} FP64 lanes x "
+                               f"{mhz:.0f} MHz", "source": fp.get("source")}
+    return {"filters": n, "receivers": R, "bins": T, "transform_length": geo, "filter_samples": T + 12287,
+            "device_ms": ms, "device_us_per_filter": ms * 1e3 / n, "e2e_ms": e2e_ms,
+            "e2e_h2d_bytes": int(E.nbytes + P.nbytes + Dp.nbytes + Dn.nbytes), "e2e_d2h_bytes": int(n * (T + 12287) * 8),
+            "launches": 4 + 3 * -(-n // max(1, min(n, (512 << 20) // (5 * geo * 16)))),
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms per filter", "cores": 1, "kind": "port",
+                             "sample": "the 7 filters of receiver 0 (numpy FP64 FFT convolution)"},
+            "roofline": roof,
+            "timing": "CUDA events around pach_filters_device on its stream, 256 MiB written between calls"}
+
+
+def run_filters_arm(args):
+    """One JSON line: receiver filters of the arena's 64 receivers (7 each) from one traced step."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    from pachydermacoustic_universal_gb300 import tracer, _capi
+    _capi.lib()
+    w = workload("arena", 1.0)[0]
+    ds = tracer.DeviceScene(w.scene)
+    h, _ = tracer.trace(w, dscene=ds, rays=args.batch or 200_000, seed=args.seed, scaled=True)
+    ds.close()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    f = filters_measure(h, w.sample_rate, max(1, args.steps), flush, f"cuda:{local}")
+    line = {"metric": "receiver filters per second (Directional_Histogram.Create_Filter, 1 GB300)",
+            "value": f["filters"] / (f["device_ms"] * 1e-3), "unit": "filters/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": 3, "higher_is_better": True, "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (histograms of one traced step of the arena)",
+            "config": {"workload": "arena_filters", "receivers": f["receivers"], "bins": f["bins"],
+                       "filters_per_receiver": 7},
+            "e2e": {"value": f["filters"] / (f["e2e_ms"] * 1e-3), "unit": "filters/s",
+                    "h2d_bytes_per_step": f["e2e_h2d_bytes"], "d2h_bytes_per_step": f["e2e_d2h_bytes"]},
+            "detail": f}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def scene_bytes(scene):
     return int(scene.vertices.nbytes + scene.poly_offsets.nbytes + scene.poly_indices.nbytes +
                scene.absorption.nbytes + scene.scattering.nbytes + scene.transmission.nbytes)
@@ -426,7 +528,7 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--metric", default="bounces", choices=["bounces", "jnd"],
+    ap.add_argument("--metric", default="bounces", choices=["bounces", "jnd", "filters"],
                     help="bounces: segment-bounces/s (default); jnd: wall time to 1 JND, learned vs uniform")
     ap.add_argument("--train-rooms", type=int, default=100, help="jnd: training rooms")
     ap.add_argument("--train-rays", type=int, default=20000, help="jnd: uniform primaries per training room")
@@ -466,6 +568,8 @@ def main():
         return run_reference_arm(args)
     if args.metric == "jnd":
         return run_jnd_arm(args)
+    if args.metric == "filters":
+        return run_filters_arm(args)
 
     ws, rank, local = dist_env()
     import torch
@@ -694,6 +798,9 @@ def main():
                                   "reference_work_gbs": bytes_seg * value / 1e9,
                                   "note": "work the reference traversal (grid domain 7) does for the same "
                                           "segments, at this run's segment rate"}
+    if rank == 0 and e2e is not None and not batched and rooms_[0].receivers:
+        # the receivers' filters (auralisation impulse responses) of the last end-to-end step
+        line["filters"] = filters_measure(h[0], rooms_[0].sample_rate, 5, flush, f"cuda:{local}")
     if rank == 0 and not args.no_jnd and args.workload == "arena":
         # the metric's second half, measured in the same run at a compact size (bench.py --metric jnd
         # runs the larger study): wall time to T30 and C80 within 1 JND, learned proposal vs uniform

@@ -378,6 +378,37 @@ pach_status pach_trace_specular_paths(pach_scene *scene, int32_t n, const double
 pach_status pach_scene_shoot_host(const pach_scene_desc *desc, int32_t n, const double *origins, const double *dirs,
                                   int32_t *poly_out, double *t_out);
 
+/* Receiver filters (auralisation impulse responses), computed on the GPU in FP64.
+ * pach_etc_to_filter: Pach_SP.ETCToFilter (Pach_SP.cs:1584-1680) of n band-pressure envelope sets
+ *   prms [n][8][T] at sample_rate Hz: out [n][T + 16383].  Each band's |P| 10^((120 - swl[b]) / 20) is
+ *   convolved with a 16384-sample band-limited sinc carrier, plus a 16 kHz band from the 8 kHz
+ *   envelope; swl NULL = 120 dB in every band.
+ * pach_receiver_filters: Directional_Histogram.Create_Filter(SWL, Rho_C) (Classes_Receivers.cs:1910-1937)
+ *   of R receivers' scaled histograms (the pach_trace_get_histograms layouts): out [R][7][T + 12287],
+ *   filter 0 from the pressures, 2d+1 / 2d+2 (d = x, y, z) from P Dir_Rec_Neg[d] / E and
+ *   P Dir_Rec_Pos[d] / E (0 where E = 0), each cut by 4096 samples as the reference cuts them.  With
+ *   dir_pos or dir_neg NULL: Histogram.Create_Filter (1186-1197), out [R][1][T + 12287] (energy unused).
+ *   Host arrays; the calling thread's current device computes.
+ * pach_trace_get_filters: the same from a finished run's device histograms, scaled as
+ *   pach_trace_get_histograms(scaled = 1) scales them, without copying them to the host; directional
+ *   = 0 gives filter 0 only.
+ * pach_filters_device: device-pointer form, asynchronous on stream (a cudaStream_t; NULL = the legacy
+ *   default stream): kinds 1 or 7, cut 0 (ETCToFilter) or 4096 (Create_Filter), d_scale [R] multiplies
+ *   each receiver's envelopes (NULL: 1), d_out [R][kinds][T + 16383 - cut]; d_workspace 256-byte
+ *   aligned, of at least pach_filters_workspace_bytes(R * kinds, T) bytes (smaller workspaces of at
+ *   least one filter's share work in more passes).  T + 16383 <= 2^20. */
+pach_status pach_etc_to_filter(const double *prms, int32_t n, int32_t T, const double *swl, int32_t sample_rate,
+                               double *out, size_t cap);
+pach_status pach_receiver_filters(const double *energy, const double *pressure, const double *dir_pos,
+                                  const double *dir_neg, int32_t R, int32_t T, int32_t sample_rate, const double *swl,
+                                  double *out, size_t cap);
+pach_status pach_trace_get_filters(pach_run *run, int32_t directional, const double *swl, double *out, size_t cap);
+size_t pach_filters_workspace_bytes(int32_t n_filters, int32_t T);
+pach_status pach_filters_device(const double *d_energy, const double *d_pressure, const double *d_dir_pos,
+                                const double *d_dir_neg, const double *d_scale, int32_t R, int32_t T, int32_t kinds,
+                                int32_t sample_rate, const double *swl, int32_t cut, double *d_out,
+                                void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Emission directions of primaries [ray_begin, ray_begin+n) as the tracer draws them. */
 pach_status pach_emit_directions(uint64_t seed, int64_t ray_begin, int32_t n, int32_t n_sources,
                                  int32_t kind, double *dirs_out);

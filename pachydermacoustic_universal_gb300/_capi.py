@@ -109,7 +109,8 @@ class Stats(C.Structure):
 EXPORTS = ["pach_version", "pach_last_error", "pach_device_count", "pach_scene_create", "pach_scenes_create",
            "pach_scene_destroy",
            "pach_scene_info", "pach_trace_begin", "pach_batch_begin", "pach_autotune", "pach_direct_sound", "pach_trace_poll", "pach_trace_cancel", "pach_trace_wait",
-           "pach_trace_get_histograms", "pach_trace_get_stats", "pach_trace_get_map", "pach_trace_get_map_directions", "pach_map_parameters",
+           "pach_trace_get_histograms", "pach_trace_get_filters", "pach_etc_to_filter", "pach_receiver_filters",
+           "pach_filters_workspace_bytes", "pach_filters_device", "pach_trace_get_stats", "pach_trace_get_map", "pach_trace_get_map_directions", "pach_map_parameters",
            "pach_etc_parameters",
            "pach_run_destroy", "pach_trace_run",
            "pach_trace_run_noalloc", "pach_convergence_replay", "pach_trace_specular_paths", "pach_scene_shoot_host", "pach_emit_directions", "pach_medium_properties", "pach_medium_attenuation_third_octave", "pach_math_schroeder",
@@ -148,6 +149,12 @@ def _declare(L):
         "pach_trace_cancel": (C.c_int, [vp]),
         "pach_trace_wait": (C.c_int, [vp, C.c_int64]),
         "pach_trace_get_histograms": (C.c_int, [vp, C.c_int32, _dp, _dp, _dp, _dp, _dp, C.c_size_t]),
+        "pach_trace_get_filters": (C.c_int, [vp, C.c_int32, _dp, _dp, C.c_size_t]),
+        "pach_etc_to_filter": (C.c_int, [_dp, C.c_int32, C.c_int32, _dp, C.c_int32, _dp, C.c_size_t]),
+        "pach_receiver_filters": (C.c_int, [_dp, _dp, _dp, _dp, C.c_int32, C.c_int32, C.c_int32, _dp, _dp, C.c_size_t]),
+        "pach_filters_workspace_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
+        "pach_filters_device": (C.c_int, [vp, vp, vp, vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _dp,
+                                          C.c_int32, vp, vp, C.c_size_t, vp]),
         "pach_trace_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
         "pach_trace_get_map": (C.c_int, [vp, C.c_int32, _dp, _dp, _dp, _ip, C.c_size_t]),
         "pach_trace_get_map_directions": (C.c_int, [vp, C.c_int32, _dp, _dp, C.c_size_t]),

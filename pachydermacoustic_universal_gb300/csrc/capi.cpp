@@ -1349,6 +1349,45 @@ pach_status pach_trace_get_histograms(pach_run *run, int32_t scaled, double *ene
     }, fail);
 }
 
+pach_status pach_trace_get_filters(pach_run *run, int32_t directional, const double *swl, double *out, size_t cap) {
+    return guarded([&]() -> pach_status {
+        if (pach_status s = check_run(run)) return s;
+        {
+            std::lock_guard<std::mutex> lk(run->mu);
+            if (!run->finished) return fail(PACH_ERR_NOT_READY, "run still in progress");
+            if (run->status != PACH_OK && run->status != PACH_ERR_CANCELLED) return fail(run->status, run->err);
+        }
+        if (run->R == 0) return fail(PACH_ERR_INVALID_ARGUMENT, "the run has no receivers");
+        const int kinds = directional ? 7 : 1;
+        const size_t n_out = (size_t)run->R * kinds * ((size_t)run->T + 16383 - 4096);
+        if (!out || cap < n_out) return fail(PACH_ERR_INVALID_ARGUMENT, "cap < receivers x filters x (T + 12287)");
+        cudaSetDevice(run->scene->device);
+        // each receiver's pressure factor of the scaled histograms, sqrt(n_sources / N) (P Dir / E keeps it)
+        std::vector<double> scale;
+        const long long done = run->rays_done.load();
+        for (const RoomSpec &rm : run->rooms) {
+            const long long off = rm.prim_begin - run->rooms[0].prim_begin;
+            const double N = (double)std::max(1ll, std::min(rm.rays, done - off));
+            scale.insert(scale.end(), rm.rec.size(), std::sqrt((double)rm.src.size()) / std::sqrt(N));
+        }
+        const size_t wsb = filters_workspace_bytes(run->R * kinds, run->T);
+        DevMem dscale, dout, ws;
+        cudaError_t e;
+        if ((e = dscale.alloc(scale.size() * sizeof(double))) != cudaSuccess ||
+            (e = dout.alloc(n_out * sizeof(double))) != cudaSuccess || (e = ws.alloc(wsb)) != cudaSuccess)
+            return fail(PACH_ERR_OUT_OF_MEMORY, cuda_msg(e, "filter buffers"));
+        if ((e = cudaMemcpy(dscale.p, scale.data(), scale.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "filter scale copy"));
+        pach_status s = filters_device(run->hE.as<double>(), run->hP.as<double>(), run->hDp.as<double>(),
+                                       run->hDn.as<double>(), dscale.as<double>(), run->R, run->T, kinds,
+                                       run->p.sample_rate, swl, 4096, dout.as<double>(), ws.p, wsb, nullptr);
+        if (s != PACH_OK) return s;
+        if ((e = cudaMemcpy(out, dout.p, n_out * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return fail(PACH_ERR_CUDA, cuda_msg(e, "filters"));
+        return PACH_OK;
+    }, fail);
+}
+
 pach_status pach_trace_get_capture(pach_run *run, float *out, size_t cap) {
     return guarded([&]() -> pach_status {
         if (pach_status s = check_run(run)) return s;

@@ -409,6 +409,14 @@ pach_status check_common(const pach_trace_params &p);
 pach_status check_room(const pach_source_desc *sources, int32_t n_sources, const pach_receiver_desc *receivers,
                        int32_t n_receivers, const std::string &who);
 
+// filters.cu: receiver filters (ETCToFilter of the band pressures and of P Dir / E) on the device.
+// kinds 1 (pressure) or 7 (pressure, then -x +x -y +y -z +z from Dir_Rec_Neg / Dir_Rec_Pos); cut 0 or
+// 4096 samples; scale [R] multiplies each receiver's envelopes (NULL: 1); asynchronous on st.
+size_t filters_workspace_bytes(int n_filters, int T);
+pach_status filters_device(const double *E, const double *P, const double *Dp, const double *Dn, const double *scale,
+                           int R, int T, int kinds, int fs, const double *swl, int cut, double *out, void *ws,
+                           size_t ws_bytes, cudaStream_t st);
+
 // scene.cpp
 bool build_host_scene(const pach_scene_desc *d, HostScene &hs, std::string &err);
 void medium_properties(double temp_c, double hr, double pa_hpa, int air_choice, int edge, double atten[kBands],

@@ -14,6 +14,9 @@ written against SplitRayTracer drives this engine unchanged:
   ``PercentLost``, ``Conclude_Simulation``, ``Sim_Type`` -- "Classes_Complete_Trace - TaskAll.cs".
   ``cutoffTime`` is a LENGTH in metres (COTime = cutoffTime / c, TaskAll:83).
 * ``AcousticalMath`` -- Classes_Math.cs parameter functions.
+* ``Receiver_Bank.Create_Filter`` / ``Spherical_Receiver.Create_Filter`` / ``Pach_SP.ETCToFilter`` --
+  the receivers' filters (Classes_Receivers.cs:626-663, 1059-1080, 1910-1995; Pach_SP.cs:1584-1680),
+  computed on the GPU.
 """
 from __future__ import annotations
 
@@ -224,6 +227,36 @@ class Spherical_Receiver:
     def Energy(self, t, oct):
         return float(self._E[:, t].sum()) if oct == 8 else float(self._E[oct, t])
 
+    def Create_Filter(self, SWL=None, dim=None):
+        """Directional_Histogram.Create_Filter on the GPU (Classes_Receivers.cs:1059-1071, 1910-1995):
+        no argument -- F (pressure) and Fdir[6] (-x +x -y +y -z +z) at 120 dB, kept on the receiver;
+        SWL -- the 7 filters returned; SWL and dim -- dim outside 1..6 returns the pressure filter, and
+        dim in 1..6 fails as the reference's does (it fills an unallocated array, 1942-1958)."""
+        if dim is not None:
+            if 1 <= int(dim) <= 6:
+                raise RuntimeError("Create_Filter(SWL, Rho_C, dim) for dim 1..6 writes into unallocated "
+                                   "arrays in the reference (NullReferenceException)")
+            return self._filters(SWL, directional=False)[0]
+        if SWL is None:
+            f = self._filters(None)
+            self.F, self.Fdir = f[0], list(f[1:])
+            return None
+        return list(self._filters(SWL))
+
+    def _filters(self, SWL, directional=True):
+        from .tracer import receiver_filters
+        out = receiver_filters(self._P[None], self._E[None], self._Dp[None] if directional else None,
+                               self._Dn[None] if directional else None, swl=SWL, sample_rate=self.SampleRate)
+        return out[0]
+
+    def Filter3Axis(self):
+        """The six directional filters made by Create_Filter() (Classes_Receivers.cs:1073-1080)."""
+        return getattr(self, "Fdir", None)
+
+    def HasFilter(self):
+        f = getattr(self, "Fdir", None)
+        return f is not None and len(f) == 6 and len(f[5]) > 0
+
 
 class Receiver_Bank:
     def __init__(self, Pt, SrcPT, Sc, SampleRate_in=1000, COTime_in=2000.0, Type=0, third_Oct=False):
@@ -237,6 +270,41 @@ class Receiver_Bank:
 
     def Origins(self):
         return [r.Origin for r in self.Rec_List]
+
+    def Create_Filter(self, SWL=None, Rec_ID=None, dim=None, VB=None):
+        """Receiver_Bank.Create_Filter (Classes_Receivers.cs:626-663).  No SWL / Rec_ID: every
+        receiver's F and Fdir (120 dB), all receivers in one GPU call; with them: that receiver's 7
+        filters, or with dim its Create_Filter(SWL, dim)."""
+        if Rec_ID is None:
+            from .tracer import receiver_filters
+            recs = self.Rec_List
+            f = receiver_filters(np.stack([r._P for r in recs]), np.stack([r._E for r in recs]),
+                                 np.stack([r._Dp for r in recs]), np.stack([r._Dn for r in recs]),
+                                 swl=None, sample_rate=self.SampleRate)
+            for r, fr in zip(recs, f):
+                r.F, r.Fdir = fr[0], list(fr[1:])
+            return None
+        return self.Rec_List[Rec_ID].Create_Filter(SWL, dim)
+
+    def Filter_3Axis(self, rec_id):
+        return self.Rec_List[rec_id].Filter3Axis()
+
+
+class Pach_SP:
+    """Audio.Pach_SP's filter construction (Pach_SP.cs)."""
+
+    @staticmethod
+    def ETCToFilter(Octave_PRMS, SWL, sample_frequency=44100, sample_frequency_out=44100, reuseEdgeForOutside=True):
+        """Pach_SP.ETCToFilter (Pach_SP.cs:1584-1680) on the GPU: [8][T] band pressure envelopes at
+        sample_frequency -> T + 16383 samples (sample_frequency_out and reuseEdgeForOutside are unused
+        there too)."""
+        if Octave_PRMS is None or len(Octave_PRMS) != 8:
+            raise ValueError("Octave_PRMS must be 8 bands.")
+        T = len(Octave_PRMS[0])
+        if any(len(b) != T for b in Octave_PRMS[1:]):
+            raise ValueError("Inconsistent band lengths.")
+        from .tracer import etc_to_filter
+        return etc_to_filter(np.asarray(Octave_PRMS, dtype=np.float64), SWL, int(sample_frequency))
 
 
 class SplitRayTracer:

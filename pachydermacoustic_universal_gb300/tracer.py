@@ -209,6 +209,17 @@ class Run:
                                                     dptr(Dn), dptr(An), E.size))
         return {"energy": E, "pressure": P, "dir_pos": Dp, "dir_neg": Dn, "analysis": An}
 
+    def filters(self, directional=True, swl=None):
+        """Receiver filters from the run's device histograms (Directional_Histogram.Create_Filter,
+        Classes_Receivers.cs:1910-1937): [R][7][T + 12287] (omni, then -x +x -y +y -z +z arrivals
+        weighted by P Dir_Rec_Neg / E and P Dir_Rec_Pos / E), or [R][1][...] with directional=False;
+        swl: the source's 8 band powers (dB), None for 120 dB."""
+        kinds = 7 if directional else 1
+        out = np.zeros((self.R, kinds, self.T + FILTER_LEN_ADD - FILTER_CUT))
+        sw = None if swl is None else np.ascontiguousarray(swl, dtype=np.float64)
+        check(_capi.lib().pach_trace_get_filters(self.handle, int(bool(directional)), dptr(sw), dptr(out), out.size))
+        return out
+
     def capture(self):
         """Captured energy (W, unscaled): capture 1 -> [R][4][1536] per emission-direction bin,
         capture 2 -> [primaries][R][4] per primary."""
@@ -418,6 +429,44 @@ def convergence_replay(per_rev, mode, distance_m, sound_speed, sample_rate=1000)
     check(_capi.lib().pach_convergence_replay(dptr(h), h.shape[0], h.shape[2], int(sample_rate), int(mode),
                                               float(distance_m), float(sound_speed), C.byref(stop), C.byref(nmin)))
     return stop.value, nmin.value
+
+
+FILTER_LEN_ADD = 16383   # ETCToFilter output: T + carrier length - 1
+FILTER_CUT = 4096        # Create_Filter's Array.Resize(F.Length - 4096)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def etc_to_filter(prms, swl=None, sample_rate=1000):
+    """Pach_SP.ETCToFilter on the GPU: prms [8][T] or [n][8][T] band pressure envelopes at sample_rate
+    Hz -> [T + 16383] (or [n][T + 16383])."""
+    a = _f64(prms)
+    one = a.ndim == 2
+    a = a[None] if one else a
+    if a.ndim != 3 or a.shape[1] != 8:
+        raise ValueError("prms must be [8][T] or [n][8][T]")
+    n, _, T = a.shape
+    out = np.zeros((n, T + FILTER_LEN_ADD))
+    check(_capi.lib().pach_etc_to_filter(dptr(a), n, T, dptr(_f64(swl)), int(sample_rate), dptr(out), out.size))
+    return out[0] if one else out
+
+
+def receiver_filters(pressure, energy=None, dir_pos=None, dir_neg=None, swl=None, sample_rate=1000):
+    """Create_Filter of R receivers' scaled histograms (pressure/energy [R][8][T], dir_pos/dir_neg
+    [R][3][8][T]) on the GPU: [R][7][T + 12287] with the directions, [R][1][T + 12287] without."""
+    P = _f64(pressure)
+    R, _, T = P.shape
+    directional = dir_pos is not None and dir_neg is not None
+    E, Dp, Dn = (_f64(energy), _f64(dir_pos), _f64(dir_neg)) if directional else (None, None, None)
+    for a, shp in ((E, (R, 8, T)), (Dp, (R, 3, 8, T)), (Dn, (R, 3, 8, T))):
+        if a is not None and a.shape != shp:
+            raise ValueError(f"histogram shape {a.shape}, expected {shp}")
+    out = np.zeros((R, 7 if directional else 1, T + FILTER_LEN_ADD - FILTER_CUT))
+    check(_capi.lib().pach_receiver_filters(dptr(E), dptr(P), dptr(Dp), dptr(Dn), R, T, int(sample_rate),
+                                            dptr(_f64(swl)), dptr(out), out.size))
+    return out
 
 
 def emit_directions(seed, ray_begin, n, n_sources, kind):
