@@ -213,8 +213,11 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
 }
 
 // The same step on a 64-byte quantised node: child bounds are 8-bit steps from the node's origin,
-// a power-of-two step per axis, so the slab distance q (s / d) + (origin - o) / d is one FMA per
-// bound as with float nodes (s / d is exact: s is a power of two).
+// a power-of-two step s per axis, so the slab distance q (s / d) + (origin - o) / d is one FMA per
+// bound as with float nodes (s / d is exact: s is a power of two).  One byte permute makes the float
+// 2^23 + 256 q; with the node's scale s / 256 the 2^15 steps it carries are taken off the slab offset
+// once per node and axis (one rounding, at most 2^-9 of a step, inside the builder's s / 256 margin)
+// instead of a subtraction per bound.
 template <typename E>
 __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int node, float ix, float iy, float iz,
                                            float ox, float oy, float oz, float best, E *stack, int &sp, int &next) {
@@ -226,12 +229,13 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
     const uint32_t e = __float_as_uint(H.w);
     const float sx = __uint_as_float((e & 255u) << 23) * ix, sy = __uint_as_float(((e >> 8) & 255u) << 23) * iy,
                 sz = __uint_as_float(((e >> 16) & 255u) << 23) * iz;
-    const float bx = fmaf(H.x, ix, -ox), by = fmaf(H.y, iy, -oy), bz = fmaf(H.z, iz, -oz);
+    const float bx = fmaf(-8388608.0f, sx, fmaf(H.x, ix, -ox)), by = fmaf(-8388608.0f, sy, fmaf(H.y, iy, -oy)),
+                bz = fmaf(-8388608.0f, sz, fmaf(H.z, iz, -oz));
     int id[4] = {ch.x, ch.y, ch.z, ch.w};
     float tk[4];
-    // byte k of w as a float: one byte permute builds 2^23 + byte (bits 0x4B0000bb), one add removes 2^23
+    // byte k of w as the float 2^23 + 256 byte (bits 0x4B00bb00): one byte permute
     auto q = [](uint32_t w, int k) {
-        return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)) - 8388608.0f;
+        return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7504u + 16u * (uint32_t)k));
     };
     // near / far bound words of each axis, chosen by the direction's sign (as for float nodes)
     const uint32_t nwx = ix < 0.f ? A.y : A.x, fwx = ix < 0.f ? A.x : A.y;
@@ -241,7 +245,7 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
     for (int k = 0; k < 4; ++k) {
         const float tn = fmaxf(fmaxf(fmaf(q(nwx, k), sx, bx), fmaf(q(nwy, k), sy, by)), fmaxf(fmaf(q(nwz, k), sz, bz), 0.f));
         const float tf = fminf(fminf(fmaf(q(fwx, k), sx, bx), fmaf(q(fwy, k), sy, by)), fminf(fmaf(q(fwz, k), sz, bz), best));
-        tk[k] = (tn <= tf && id[k] != kEmptyChild) ? tn : FLT_MAX;
+        tk[k] = tn <= tf ? tn : FLT_MAX;  // an empty slot's box is inverted on every axis: never hit
     }
     cswap(tk[0], id[0], tk[1], id[1]);
     cswap(tk[2], id[2], tk[3], id[3]);

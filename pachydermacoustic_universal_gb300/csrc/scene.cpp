@@ -456,8 +456,11 @@ void build_bvh(HostScene &hs, int leaf_max) {
 }
 
 // 64-byte copy of the 4-wide BVH: per node a frame (origin of the children's union box and a
-// power-of-two step per axis, 255 steps spanning it) and each child's box as 8-bit steps, the lower
-// bound rounded down and the upper rounded up, so a decoded box always contains the float box.
+// power-of-two step s = 2^e per axis, 255 steps spanning it) and each child's box as 8-bit steps, the
+// lower bound rounded down and the upper rounded up, at least s / 256 outside the float box: the walk
+// folds the byte decode's bias into the slab offset, one rounding of at most 2^-9 s, so a decoded box
+// still contains the float box.  The stored exponent is that of 2^(e - 8) = s / 256, the scale of a
+// byte decoded as 2^23 + 256 q.
 //   float4 (origin x, y, z, biased exponents ex | ey << 8 | ez << 16 as bits)
 //   uint4  (lo.x of children 0-3 as bytes, hi.x, lo.y, hi.y)
 //   uint4  (lo.z, hi.z, 0, 0)
@@ -493,32 +496,36 @@ static void quantize_nodes(HostScene &hs, size_t q0, size_t q1) {
         uint32_t qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0};  // 4 children x 8 bits each
         for (int a = 0; a < 3; ++a) {
             if (lo[a] > hi[a]) continue;  // no valid child: the node is never entered
-            origin[a] = (float)lo[a];
-            if ((double)origin[a] > lo[a]) origin[a] = std::nextafter(origin[a], -INFINITY);
-            const double ext = hi[a] - (double)origin[a];
-            int e = ext > 0 ? (int)std::ceil(std::log2(ext / 255.0)) : -126;
-            e = std::max(-126, std::min(127, e));
-            for (;;) {  // the decoded float boxes must contain every child box
+            const double ext = hi[a] - lo[a];
+            int e = ext > 0 ? (int)std::ceil(std::log2(ext / 254.0)) : -100;
+            e = std::max(-100, std::min(127, e));  // e - 8 stays a normal exponent
+            float org = 0.f;
+            for (;;) {  // the decoded boxes must contain every child box with s / 256 to spare
                 const float s = std::ldexp(1.0f, e);
-                bool ok = true;
+                org = (float)(lo[a] - s / 256.0);
+                if ((double)org > lo[a] - s / 256.0) org = std::nextafter(org, -INFINITY);
+                bool ok = std::isfinite(org);
                 uint32_t L = 0, H = 0;
                 for (int k = 0; k < 4 && ok; ++k) {
                     int ql = 255, qh = 0;  // invalid children: an inverted box (never tested: code check)
                     if (valid[k]) {
-                        ql = (int)std::floor(((double)f[8 * a + k] - origin[a]) / s);
-                        qh = (int)std::ceil(((double)f[8 * a + 4 + k] - origin[a]) / s);
+                        // decoded bounds org + q s are exact in double
+                        const double wl = (double)f[8 * a + k] - s / 256.0, wh = (double)f[8 * a + 4 + k] + s / 256.0;
+                        ql = (int)std::floor((wl - org) / s);
+                        qh = (int)std::ceil((wh - org) / s);
                         ql = std::max(0, ql);
-                        while (ql > 0 && origin[a] + (float)ql * s > f[8 * a + k]) --ql;
-                        while (qh <= 255 && origin[a] + (float)qh * s < f[8 * a + 4 + k]) ++qh;
-                        if (qh > 255 || origin[a] + (float)ql * s > f[8 * a + k]) ok = false;
+                        while (ql > 0 && (double)org + (double)ql * s > wl) --ql;
+                        while (qh <= 255 && (double)org + (double)qh * s < wh) ++qh;
+                        if (qh > 255 || (double)org + (double)ql * s > wl) ok = false;
                     }
                     L |= (uint32_t)ql << (8 * k);
                     H |= (uint32_t)std::min(qh, 255) << (8 * k);
                 }
                 if (ok || e >= 127) {
+                    origin[a] = org;
                     qlo[a] = L;
                     qhi[a] = H;
-                    ebias[a] = e + 127;
+                    ebias[a] = e - 8 + 127;
                     break;
                 }
                 ++e;
