@@ -509,7 +509,10 @@ void run_worker_body(pach_run *run) {
         if (!quant) S.bvhq = nullptr;  // trace_ray walks whichever node array is set
         const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max, quant);
         const bool fused = fused_walk(run->p.traversal, ntri_max) && run->p.ray_sort <= 0;
-        TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh, fused));
+        size_t rec_max = 0;
+        for (const RoomSpec &rm : run->rooms) rec_max = std::max(rec_max, rm.rec.size());
+        const bool wide = rec_max >= (size_t)kShadeWideReceivers;
+        TRY(wave_kernel_occupancy(tr_variant, threads, receiver_smem_bytes(R), &bps_tr, &bps_sh, fused, wide));
         const int tr_blocks = dev_sms * std::max(bps_tr, 1), sh_blocks = dev_sms * std::max(bps_sh, 1);
 
         // ring and wave sizing
@@ -663,7 +666,7 @@ void run_worker_body(pach_run *run) {
             if (timing && (x = cudaEventRecord(kev[6 * k + 3], stream))) return x;
             if (!fused && (x = launch_trace(r, tr_variant, tr_blocks, threads, stream))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 4], stream))) return x;
-            if ((x = launch_shade(r, sh_blocks, threads, stream, fused, map))) return x;
+            if ((x = launch_shade(r, sh_blocks, threads, stream, fused, map, wide))) return x;
             if (timing && (x = cudaEventRecord(kev[6 * k + 5], stream))) return x;
             return cudaSuccess;
         };

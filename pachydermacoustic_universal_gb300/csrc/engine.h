@@ -360,7 +360,10 @@ cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, 
 // fused: k_shade walks the rays itself (no k_trace launch) -- the default for scenes of at most
 // kFuseMaxTris triangles, or traversal = 3
 // map: also detect the run's mapping receivers (kernel variants compiled with the grid walk)
-cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused = false, bool map = false);
+// wide: the shading variant with 4 blocks per SM, for rooms of at least kShadeWideReceivers receivers
+constexpr int kShadeWideReceivers = 48;
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused = false, bool map = false,
+                         bool wide = false);
 // Room-acoustic parameters of n energy-time curves etc [n][T] x scale at fs Hz on the device (map_params.cu).
 cudaError_t launch_map_params(const double *etc, int n, int T, double fs, double scale, int decay_depth,
                               double clarity_s, double *t_x, double *edt, double *clarity, double *definition,
@@ -368,7 +371,7 @@ cudaError_t launch_map_params(const double *etc, int n, int T, double fs, double
 constexpr int kFuseMaxTris = 64;
 inline bool fused_walk(int traversal, int ntri) { return traversal == 3 || (traversal == 0 && ntri <= kFuseMaxTris); }
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade,
-                                  bool fused = false);
+                                  bool fused = false, bool wide = false);
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
                          double *t, double *pts, cudaStream_t s);
 cudaError_t launch_emit(const DevRun &r, long long p0, int n, double *out, cudaStream_t s);

@@ -553,10 +553,13 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
 // FUSED: walk the ray here instead of reading k_trace's hit (small scenes, whose walk is a few
 // cached nodes: the separate trace pass would only re-read the ray and round-trip its hit via HBM).
 // the shading pass alone fits three 256-thread blocks per SM (80 registers; +1.6 % on a 500k-triangle
-// arena, equal on a 20k-triangle hall); the fused walk, two (128 registers)
+// arena, equal on a 20k-triangle hall); the fused walk, two (128 registers).  WIDE, for rooms of many
+// receivers: the grouped detection and four blocks per SM (64 registers, more spilled: the long
+// detection loop waits on its loads) -- -6 % shading time on the 64-receiver arena from the fourth
+// block alone, but +17 % on the 16-receiver hall, which keeps three.
 constexpr int kShadeMinBlocks = 3;
-template <bool FUSED, bool MAP>
-__global__ void __launch_bounds__(256, FUSED ? 2 : kShadeMinBlocks) k_shade(DevRun r) {
+template <bool FUSED, bool MAP, bool WIDE = false>
+__global__ void __launch_bounds__(256, FUSED ? 2 : (WIDE ? 4 : kShadeMinBlocks)) k_shade(DevRun r) {
     extern __shared__ float4 s_rec_buf[];
     const int *s_rid;
     const float4 *s_rec = stage_receivers(r, s_rec_buf, s_rid);
@@ -594,7 +597,7 @@ __global__ void __launch_bounds__(256, FUSED ? 2 : kShadeMinBlocks) k_shade(DevR
             const float t = __int_as_float(h.y);
             ++L.v[R.phase == 0 ? C_SEGB : C_SEGC];
             const RoomParams &P = r.rooms[R.room];
-            L.v[C_DET] += detect_octave(r, P, s_rec, s_rid, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct,
+            L.v[C_DET] += detect_octave<WIDE>(r, P, s_rec, s_rid, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct,
                                         R.mask, R.prim);
             if constexpr (MAP)
                 L.v[C_DET] += map_detect_octave(r.map, P, R.p, R.d, hit ? t : 1e6f, R.t_sum, R.I * R.scale, R.oct);
@@ -811,19 +814,20 @@ cudaError_t launch_trace(const DevRun &r, int variant, int blocks, int threads, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused, bool map) {
+cudaError_t launch_shade(const DevRun &r, int blocks, int threads, cudaStream_t s, bool fused, bool map, bool wide) {
     if (map) {
         if (fused) k_shade<true, true><<<blocks, threads, rec_smem(r), s>>>(r);
         else k_shade<false, true><<<blocks, threads, rec_smem(r), s>>>(r);
     } else {
         if (fused) k_shade<true, false><<<blocks, threads, rec_smem(r), s>>>(r);
+        else if (wide) k_shade<false, false, true><<<blocks, threads, rec_smem(r), s>>>(r);
         else k_shade<false, false><<<blocks, threads, rec_smem(r), s>>>(r);
     }
     return cudaGetLastError();
 }
 
 cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int *bpsm_trace, int *bpsm_shade,
-                                  bool fused) {
+                                  bool fused, bool wide) {
     cudaError_t e;
     switch (variant) {
 #define PACH_OCC(M, SP, Q)                                                                           \
@@ -835,8 +839,9 @@ cudaError_t wave_kernel_occupancy(int variant, int threads, int smem_shade, int 
         default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_trace, k_trace<4, false, false>, threads, 0); break;
     }
     if (e != cudaSuccess) return e;
-    return fused ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<true, false>, threads, smem_shade)
-                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false, false>, threads, smem_shade);
+    if (fused) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<true, false>, threads, smem_shade);
+    if (wide) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false, false, true>, threads, smem_shade);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm_shade, k_shade<false, false>, threads, smem_shade);
 }
 
 cudaError_t launch_paths(const DevScene &S, int n, const double *o, const double *d, int max_bounces, int *poly,
