@@ -377,15 +377,16 @@ __device__ __forceinline__ void conv_add(const DevRun &r, int row, int oct, long
     atomicAdd(h + (size_t)(1 + kind) * r.T + bin, (double)e);
 }
 
-// A cheap superset of sphere_hit: the chord midpoint -b inside the segment and |m|^2 - b^2 within the
-// squared radius, each with a margin far above their FP32 rounding (|m|^2 - b^2 is the squared
-// distance of the centre from the line, a few ulps of |m|^2 away from sphere_hit's |m - b d|^2).
-__device__ __forceinline__ bool sphere_near(float4 c, float3 o, float3 d, float tseg) {
+// A cheap superset of sphere_hit: the centre's squared distance from the ray's line, |m|^2 - b^2,
+// within the squared radius plus a margin far above its FP32 rounding (a few ulps of |m|^2 away from
+// sphere_hit's |m - b d|^2; a float32 emulation over 10M centres placed about one radius from random
+// rays found no sphere the exact test accepts and this one rejects).  The chord's position along the
+// segment is left to the exact test: a receiver near the line but beyond the segment is rare.
+__device__ __forceinline__ bool sphere_near(float4 c, float3 o, float3 d) {
     const float mx = o.x - c.x, my = o.y - c.y, mz = o.z - c.z;
     const float b = fmaf(mx, d.x, fmaf(my, d.y, mz * d.z));
     const float mm = fmaf(mx, mx, fmaf(my, my, mz * mz));
-    const float tb = 1e-5f * (fabsf(b) + 1.f);
-    return fmaf(-b, b, mm) <= fmaf(1e-5f, mm, c.w + 1e-6f) && -b > -tb && -b < tseg + tb;
+    return fmaf(-b, b, mm) <= fmaf(1e-5f, mm, c.w + 1e-6f);
 }
 
 // One octave detection (Spherical_Receiver.CheckRay, Classes_Receivers.cs:837-877) of the receiver in
@@ -406,10 +407,9 @@ __device__ __forceinline__ void detect_octave_one(const DevRun &r, const RoomPar
 }
 
 // Spherical_Receiver.CheckRay over the receivers of the ray's room (rec: the run's receiver table in
-// shared memory).  Returns the spheres hit.  GROUPED (rooms of many receivers): receivers go four at a
-// time through sphere_near (four independent chains, no branch while none is near) and the exact
-// sphere_hit decides for the near ones -- -11 % shading time on the 64-receiver arena, +10 % on the
-// 16-receiver hall, which keeps the plain loop.
+// shared memory).  Returns the spheres hit.  GROUPED: receivers go four at a time through sphere_near
+// (four independent chains, no branch while none is near; the remainder of the room's receivers one
+// at a time) and the exact sphere_hit decides for the near ones.
 template <bool GROUPED>
 __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomParams &P, const float4 *rec,
                                                   const int *rid, float3 o, float3 d, float tseg, double t_sum,
@@ -426,10 +426,11 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomPar
         }
         return n;
     }
-    for (int s0 = P.rec_begin; s0 < s1; s0 += 4) {
+    int s0 = P.rec_begin;
+    for (; s0 + 4 <= s1; s0 += 4) {
         bool near[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) near[k] = s0 + k < s1 && sphere_near(rec[min(s0 + k, s1 - 1)], o, d, tseg);
+        for (int k = 0; k < 4; ++k) near[k] = sphere_near(rec[s0 + k], o, d);
         if (!(near[0] | near[1] | near[2] | near[3])) continue;
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
@@ -440,6 +441,13 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomPar
             ++n;
             detect_octave_one(r, P, rid, s0 + k, c, d, t, half, t_sum, Iabs, oct, mask, prim);
         }
+    }
+    for (; s0 < s1; ++s0) {
+        const float4 c = rec[s0];
+        float t, half;
+        if (!sphere_hit(c, o, d, tseg, t, half)) continue;
+        ++n;
+        detect_octave_one(r, P, rid, s0, c, d, t, half, t_sum, Iabs, oct, mask, prim);
     }
     return n;
 }

@@ -555,8 +555,9 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
 // the shading pass alone fits three 256-thread blocks per SM (80 registers; +1.6 % on a 500k-triangle
 // arena, equal on a 20k-triangle hall); the fused walk, two (128 registers).  WIDE, for rooms of many
 // receivers: the grouped detection and four blocks per SM (64 registers, more spilled: the long
-// detection loop waits on its loads) -- -6 % shading time on the 64-receiver arena from the fourth
-// block alone, but +17 % on the 16-receiver hall, which keeps three.
+// detection loop waits on its loads) -- on the 64-receiver arena -6 % shading time from the fourth
+// block, -28 % more from the grouped detection; on the 16-receiver hall +17 % and +12 %, so it keeps
+// three blocks and the plain loop.
 constexpr int kShadeMinBlocks = 3;
 template <bool FUSED, bool MAP, bool WIDE = false>
 __global__ void __launch_bounds__(256, FUSED ? 2 : (WIDE ? 4 : kShadeMinBlocks)) k_shade(DevRun r) {
