@@ -214,13 +214,14 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
 
 // The same step on a 64-byte quantised node: child bounds are 8-bit steps from the node's origin,
 // a power-of-two step s per axis, so the slab distance q (s / d) + (origin - o) / d is one FMA per
-// bound as with float nodes (s / d is exact: s is a power of two).  One byte permute makes the float
+// bound as with float nodes (s / d is exact: s is a power of two); (origin - o) / d is formed per node
+// from the ray origin (px, py, pz), which keeps three fewer values live through the walk.  One byte permute makes the float
 // 2^23 + 256 q; with the node's scale s / 256 the 2^15 steps it carries are taken off the slab offset
 // once per node and axis (one rounding, at most 2^-9 of a step, inside the builder's s / 256 margin)
 // instead of a subtraction per bound.
 template <typename E>
 __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int node, float ix, float iy, float iz,
-                                           float ox, float oy, float oz, float best, E *stack, int &sp, int &next) {
+                                           float px, float py, float pz, float best, E *stack, int &sp, int &next) {
     const float4 *N = bvhq + (kBvhQNodeFloats / 4) * node;
     const float4 H = __ldg(N);
     const uint4 A = __ldg(reinterpret_cast<const uint4 *>(N + 1));
@@ -229,8 +230,8 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
     const uint32_t e = __float_as_uint(H.w);
     const float sx = __uint_as_float((e & 255u) << 23) * ix, sy = __uint_as_float(((e >> 8) & 255u) << 23) * iy,
                 sz = __uint_as_float(((e >> 16) & 255u) << 23) * iz;
-    const float bx = fmaf(-8388608.0f, sx, fmaf(H.x, ix, -ox)), by = fmaf(-8388608.0f, sy, fmaf(H.y, iy, -oy)),
-                bz = fmaf(-8388608.0f, sz, fmaf(H.z, iz, -oz));
+    const float bx = fmaf(-8388608.0f, sx, (H.x - px) * ix), by = fmaf(-8388608.0f, sy, (H.y - py) * iy),
+                bz = fmaf(-8388608.0f, sz, (H.z - pz) * iz);
     int id[4] = {ch.x, ch.y, ch.z, ch.w};
     float tk[4];
     // byte k of w as the float 2^23 + 256 byte (bits 0x4B00bb00): one byte permute
@@ -282,7 +283,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, int root, float t_e
             if (node >= 0) {
                 ++w.nodes;
                 int next;
-                node = (S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                node = (S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, o.x, o.y, o.z, best, stack, sp, next)
                                : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
                            ? next
                            : stack_pop(stack, sp, best);
@@ -303,7 +304,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, int root, float t_e
             while (node >= 0) {
                 ++w.nodes;
                 int next;
-                if (!(S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                if (!(S.bvhq ? bvh4q_step(S.bvhq, node, ix, iy, iz, o.x, o.y, o.z, best, stack, sp, next)
                              : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))) {
                     if (sp == 0) { done = true; break; }
                     node = stack[--sp];

@@ -427,12 +427,19 @@ constexpr int kSpecSlack = 10;
 // Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
 // its next leaf and tests it; a lane whose walk has ended writes its hit and takes the next wave
 // item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
+// Values the walk needs only when a ray starts or ends, or once per warp iteration, live in shared
+// memory (each lane's wave index; each warp's node and triangle counts), not in registers: the walk's
+// 40 registers already spill.
 template <int MINB, bool SPEC, bool QUANT>
 __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
+    __shared__ unsigned s_item[256];
+    __shared__ unsigned long long s_cnt[8][2];
     WaveCtl *c = r.ctl;
     const unsigned long long m = c->m, head = c->head;
     const DevScene &S = r.S;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_cnt[wid][0] = s_cnt[wid][1] = 0;
+    __syncwarp();
     TraceWork w;
     bool have = false, exhausted = false;
     unsigned j = 0;  // index in the wave (a wave holds at most half the ring: < 2^31 items)
@@ -462,7 +469,8 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                     const float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
                     const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
                     ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
-                    ox = o.x * ix; oy = o.y * iy; oz = o.z * iz;
+                    if constexpr (!QUANT) { ox = o.x * ix; oy = o.y * iy; oz = o.z * iz; }
+                    if constexpr (SPEC) s_item[threadIdx.x] = j;
                     node = r.n_rooms > 1 ? __ldg(&r.rooms[room].bvh_root) : 0;
                     teps = r.n_rooms > 1 ? __ldg(&r.rooms[room].t_eps) : S.t_eps;
                     sp = 0; best = FLT_MAX; bi = -1;
@@ -487,10 +495,11 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 // looking, so it ends)
                 const int looking = __popc(__ballot_sync(FULL, have && node >= 0 && leaf == 0));
                 if (looking == 0 || (looking <= kSpecSlack && __any_sync(FULL, have && leaf != 0))) break;
+                const unsigned stepping = __ballot_sync(FULL, have && node >= 0);
+                if (lane == 0) s_cnt[wid][0] += (unsigned)__popc(stepping);
                 if (have && node >= 0) {
-                    ++w.nodes;
                     int next;
-                    if (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                    if (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, o.x, o.y, o.z, best, stack, sp, next)
                               : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
                         node = next;
                     else node = stack_pop(stack, sp, best);
@@ -500,15 +509,17 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                     }
                 }
             }
-            if (have && leaf != 0) {
+            const bool testing = have && leaf != 0;
+            const unsigned ntri = __reduce_add_sync(FULL, testing ? (unsigned)(((~leaf) & 15) + 1) : 0u);
+            if (lane == 0) s_cnt[wid][1] += ntri;
+            if (testing) {
                 const int code = ~leaf;
                 const int f0 = code >> 4, cnt = (code & 15) + 1;
-                w.tris += (unsigned)cnt;
                 for (int k = 0; k < cnt; ++k) test_tri(S, teps, f0 + k, o, d, skip, best, bi, w);
                 leaf = 0;
             }
             if (have && node == kEmptyChild) {
-                write_hit(r, S, j, bi, best);
+                write_hit(r, S, s_item[threadIdx.x], bi, best);
                 have = false;
             }
         } else {
@@ -516,7 +527,7 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             while (node >= 0) {
                 ++w.nodes;
                 int next;
-                node = (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next)
+                node = (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, o.x, o.y, o.z, best, stack, sp, next)
                               : bvh4_step(S.bvh, node, ix, iy, iz, ox, oy, oz, best, stack, sp, next))
                            ? next
                            : stack_pop(stack, sp, best);
@@ -537,6 +548,11 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     }
     // one atomic per warp for each counter
     unsigned long long a = w.retests, b = w.nodes, c2 = w.tris;
+    if constexpr (SPEC) {
+        __syncwarp();
+        b = lane == 0 ? s_cnt[wid][0] : 0;
+        c2 = lane == 0 ? s_cnt[wid][1] : 0;
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(FULL, a, o);
