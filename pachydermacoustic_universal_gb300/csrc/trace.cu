@@ -427,12 +427,14 @@ constexpr int kSpecSlack = 10;
 // Persistent BVH walk with dynamic ray fetch: every loop iteration a lane descends inner nodes to
 // its next leaf and tests it; a lane whose walk has ended writes its hit and takes the next wave
 // item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
-// Values the walk needs only when a ray starts or ends, or once per warp iteration, live in shared
-// memory (each lane's wave index; each warp's node and triangle counts), not in registers: the walk's
-// 40 registers already spill.
+// Values the walk needs only when a ray starts or ends, once per leaf or once per warp iteration live
+// in shared memory (each lane's wave index, the plane it leaves and its hit tolerance; each warp's node
+// and triangle counts), not in registers: the walk's 40 registers already spill.
 template <int MINB, bool SPEC, bool QUANT>
 __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     __shared__ unsigned s_item[256];
+    __shared__ int s_skip[256];
+    __shared__ float s_teps[256];
     __shared__ unsigned long long s_cnt[8][2];
     WaveCtl *c = r.ctl;
     const unsigned long long m = c->m, head = c->head;
@@ -470,9 +472,13 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                     const float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
                     ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
                     if constexpr (!QUANT) { ox = o.x * ix; oy = o.y * iy; oz = o.z * iz; }
-                    if constexpr (SPEC) s_item[threadIdx.x] = j;
                     node = r.n_rooms > 1 ? __ldg(&r.rooms[room].bvh_root) : 0;
                     teps = r.n_rooms > 1 ? __ldg(&r.rooms[room].t_eps) : S.t_eps;
+                    if constexpr (SPEC) {
+                        s_item[threadIdx.x] = j;
+                        s_skip[threadIdx.x] = skip;
+                        s_teps[threadIdx.x] = teps;
+                    }
                     sp = 0; best = FLT_MAX; bi = -1;
                     have = true;
                 } else {
@@ -515,7 +521,9 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
             if (testing) {
                 const int code = ~leaf;
                 const int f0 = code >> 4, cnt = (code & 15) + 1;
-                for (int k = 0; k < cnt; ++k) test_tri(S, teps, f0 + k, o, d, skip, best, bi, w);
+                const int sk = s_skip[threadIdx.x];
+                const float te = s_teps[threadIdx.x];
+                for (int k = 0; k < cnt; ++k) test_tri(S, te, f0 + k, o, d, sk, best, bi, w);
                 leaf = 0;
             }
             if (have && node == kEmptyChild) {
