@@ -380,8 +380,8 @@ __device__ __forceinline__ void conv_add(const DevRun &r, int row, int oct, long
 
 // A cheap superset of sphere_hit: the centre's squared distance from the ray's line, |m|^2 - b^2,
 // within the squared radius plus a margin far above its FP32 rounding (a few ulps of |m|^2 away from
-// sphere_hit's |m - b d|^2; a float32 emulation over 10M centres placed about one radius from random
-// rays found no sphere the exact test accepts and this one rejects).  The chord's position along the
+// sphere_hit's |m - b d|^2; tests/test_receiver_prefilter.py checks in float32 that no sphere the
+// exact test accepts is rejected here).  The chord's position along the
 // segment is left to the exact test: a receiver near the line but beyond the segment is rare.
 __device__ __forceinline__ bool sphere_near(float4 c, float3 o, float3 d) {
     const float mx = o.x - c.x, my = o.y - c.y, mz = o.z - c.z;
