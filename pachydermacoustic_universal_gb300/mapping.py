@@ -239,6 +239,30 @@ class PachMapReceiver:
                     if s < self.SampleCT:
                         rec.Combine_Sample(s, Io[s], np.sqrt(Io[s]), oct, u, u)
 
+    def Create_Filter(self, VB=None):
+        """Receiver_Bank.Create_Filter (Classes_Receivers.cs:626-651) for the map's receivers, on the GPU:
+        each Map_Receiver's Histogram.Create_Filter (1175-1184: the pressure filter at 120 dB; none for
+        one-point histograms) or, for a directional map, Directional_Histogram.Create_Filter
+        (1968-1995: also the six directional filters)."""
+        if self._E.shape[2] == 1:
+            return None
+        from .tracer import receiver_filters
+        d = self.Directional
+        f = receiver_filters(self._P, self._E, self._Dp if d else None, self._Dn if d else None, swl=None,
+                             sample_rate=self.SampleRate)
+        self._F = f[:, 0]
+        self._Fdir = f[:, 1:] if d else None
+        return None
+
+    def GetFilter(self, Rec_Index):
+        """Receiver_Bank.GetFilter (Classes_Receivers.cs:454-461): the receiver's filter, or SampleCT
+        zeros before Create_Filter."""
+        F = getattr(self, "_F", None)
+        return np.zeros(self.SampleCT) if F is None else F[Rec_Index].copy()
+
+    def HasFilter(self):
+        return getattr(self, "_F", None) is not None
+
     def Combine_Clones(self, other):
         self._E += other._E
         self._P += other._P

@@ -26,7 +26,8 @@ def _close(got, ref):
     assert err <= RTOL_MAX, err
 
 
-@pytest.mark.parametrize("T,fs", [(1, 1000), (37, 1000), (3500, 1000), (16386, 1000), (2000, 44100), (40000, 44100)])
+@pytest.mark.parametrize("T,fs", [(1, 1000), (37, 1000), (3500, 1000), (16385, 1000), (16386, 1000), (2000, 44100),
+                                  (40000, 44100)])
 def test_etc_to_filter_matches_oracle(T, fs):
     rng = np.random.default_rng(T)
     P = rng.random((8, T)) * (rng.random((8, T)) > 0.2)

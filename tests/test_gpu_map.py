@@ -195,6 +195,15 @@ def test_split_ray_tracer_fills_a_pach_map_receiver_and_parameter_maps():
                    "definition": AcousticalMath.Definition(etc, 1000, 0.05, 0.0, False)}
             for k in maps:
                 np.testing.assert_allclose(maps[k][i], ref[k], rtol=1e-9, equal_nan=True, err_msg=k)
+    # each map receiver's filter (Receiver_Bank.Create_Filter / GetFilter) against the FP64 oracle
+    from oracle import filters as OF
+    assert not pm.HasFilter() and not pm.GetFilter(0).any()
+    pm.Create_Filter()
+    for i in (0, pm.Count // 2, pm.Count - 1):
+        ref = OF.receiver_filters(pm._E[i], pm._P[i], None, None, [120.0] * 8, 1000, directional=False)[0]
+        got = pm.GetFilter(i)
+        assert got.shape == ref.shape
+        assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
 
 
 def test_directional_map_matches_oracle():
