@@ -133,7 +133,8 @@ typedef struct {
     const float *proposal;         /* optional [n_proposal][160] learned-proposal lobes (pach_proposal.h) */
     int32_t n_proposal;
     int32_t bvh_format;            /* BVH nodes the trace kernel walks: 0 = default, 1 = 128-byte float
-                                      boxes, 2 = 64-byte nodes with 8-bit child boxes */
+                                      boxes, 2 = 48-byte nodes with 8-bit child boxes (scenes whose
+                                      triangle ids fit 24 bits; others walk the float boxes) */
     double proposal_mix;           /* weight of uniform emission in the proposal, (0, 1]; 0 = 0.3 */
     double capture_edges_ms[3];    /* capture windows, ms after the direct arrival; zeros = 80, 400, 1200 */
     const struct pach_map_desc *map; /* optional mapping receivers (single-room runs), else NULL */

@@ -175,6 +175,23 @@ static void rebase_codes(float *nodes, size_t count, int stride, int code_at, in
     });
 }
 
+// Rebases 48-byte quantised nodes (see quantize_bvh): the first inner child's node id and the first
+// leaf triangle, which keeps its 24 bits (append_scene drops the quantised copy of a batch beyond that).
+static void rebase_qnodes(float *nodes, size_t count, int node_off, int tri_off) {
+    parallel_chunks(count, 16384, [=](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q) {
+            float *g = nodes + q * kBvhQNodeFloats;
+            uint32_t nb, tw;
+            std::memcpy(&nb, &g[10], 4);
+            std::memcpy(&tw, &g[11], 4);
+            nb += (uint32_t)node_off;
+            tw = (((tw & 0xFFFFFFu) + (uint32_t)tri_off) & 0xFFFFFFu) | (tw & 0xFF000000u);
+            std::memcpy(&g[10], &nb, 4);
+            std::memcpy(&g[11], &tw, 4);
+        }
+    });
+}
+
 int append_scene(const HostScene &hs, SceneArrays &A) {
     const int tri_off = (int)(A.tri.size() / 3), poly_off = (int)A.norm.size(), plane_off = A.planes;
     const int node_off = (int)(A.bvh.size() / kBvhNodeFloats);
@@ -224,11 +241,15 @@ int append_scene(const HostScene &hs, SceneArrays &A) {
     });
     const size_t b0 = A.bvh.size();
     A.bvh.insert(A.bvh.end(), hs.bvh.begin(), hs.bvh.end());
+    // a quantised copy only when every scene of the array has one and the triangle ids fit 24 bits
+    const bool quant = (node_off == 0 || !A.bvhq.empty()) && !hs.bvhq.empty() &&
+                       (long long)tri_off + hs.ntri <= (1ll << 24);
+    if (!quant) A.bvhq.clear();
     const size_t q0 = A.bvhq.size();
-    A.bvhq.insert(A.bvhq.end(), hs.bvhq.begin(), hs.bvhq.end());
+    if (quant) A.bvhq.insert(A.bvhq.end(), hs.bvhq.begin(), hs.bvhq.end());
     if (tri_off || node_off) {
         rebase_codes(&A.bvh[b0], hs.bvh.size() / kBvhNodeFloats, kBvhNodeFloats, 24, node_off, tri_off);
-        rebase_codes(&A.bvhq[q0], hs.bvhq.size() / kBvhQNodeFloats, kBvhQNodeFloats, 12, node_off, tri_off);
+        if (quant) rebase_qnodes(&A.bvhq[q0], hs.bvhq.size() / kBvhQNodeFloats, node_off, tri_off);
     }
     A.t_eps = std::max(A.t_eps, (float)(2e-7 * hs.scale));
     A.has_trans = A.has_trans || hs.has_trans;
@@ -505,7 +526,7 @@ void run_worker_body(pach_run *run) {
         const int threads = run->p.block_threads > 0 ? std::max(32, std::min(256, run->p.block_threads / 32 * 32)) : 256;
         int bps_tr = 0, bps_sh = 0;
         // blocks_per_sm picks the trace kernel's register variant (3..6 blocks of 256 per SM)
-        const bool quant = use_quantised_nodes(run->p.bvh_format, ntri_max);
+        const bool quant = use_quantised_nodes(run->p.bvh_format, ntri_max) && S.bvhq != nullptr;
         if (!quant) S.bvhq = nullptr;  // trace_ray walks whichever node array is set
         const int tr_variant = trace_variant(run->p.blocks_per_sm, run->p.traversal, ntri_max, quant);
         const bool fused = fused_walk(run->p.traversal, ntri_max) && run->p.ray_sort <= 0;

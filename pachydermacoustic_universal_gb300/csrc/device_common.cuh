@@ -212,7 +212,7 @@ __device__ __forceinline__ bool bvh4_step(const float4 *__restrict__ bvh, int no
     return true;
 }
 
-// The same step on a 64-byte quantised node: child bounds are 8-bit steps from the node's origin,
+// The same step on a 48-byte quantised node: child bounds are 8-bit steps from the node's origin,
 // a power-of-two step s per axis, so the slab distance q (s / d) + (origin - o) / d is one FMA per
 // bound as with float nodes (s / d is exact: s is a power of two); (origin - o) / d is formed per node
 // from the ray origin (px, py, pz), which keeps three fewer values live through the walk.  One byte permute makes the float
@@ -226,13 +226,25 @@ __device__ __forceinline__ bool bvh4q_step(const float4 *__restrict__ bvhq, int 
     const float4 H = __ldg(N);
     const uint4 A = __ldg(reinterpret_cast<const uint4 *>(N + 1));
     const uint4 B = __ldg(reinterpret_cast<const uint4 *>(N + 2));
-    const int4 ch = __ldg(reinterpret_cast<const int4 *>(N + 3));
     const uint32_t e = __float_as_uint(H.w);
+    // children from the slot codes (0 inner, 1-8 leaf of that many triangles, 15 empty): inner ids
+    // count up from B.z, leaf triangles from the low 24 bits of B.w
+    const uint32_t slots = (e >> 24) | ((B.w >> 24) << 8);
+    int id[4];
+    {
+        int inner = (int)B.z, tri = (int)(B.w & 0xFFFFFFu);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int v = (int)((slots >> (4 * k)) & 15u);
+            id[k] = v == 0 ? inner : (v <= 8 ? ~(tri * 16 + v - 1) : kEmptyChild);
+            inner += v == 0;
+            tri += v <= 8 ? v : 0;
+        }
+    }
     const float sx = __uint_as_float((e & 255u) << 23) * ix, sy = __uint_as_float(((e >> 8) & 255u) << 23) * iy,
                 sz = __uint_as_float(((e >> 16) & 255u) << 23) * iz;
     const float bx = fmaf(-8388608.0f, sx, (H.x - px) * ix), by = fmaf(-8388608.0f, sy, (H.y - py) * iy),
                 bz = fmaf(-8388608.0f, sz, (H.z - pz) * iz);
-    int id[4] = {ch.x, ch.y, ch.z, ch.w};
     float tk[4];
     // byte k of w as the float 2^23 + 256 byte (bits 0x4B00bb00): one byte permute
     auto q = [](uint32_t w, int k) {

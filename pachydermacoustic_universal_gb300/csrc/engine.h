@@ -92,7 +92,8 @@ struct HostScene {
     // bits), unused; a child >= 0 is an inner node, < 0 the leaf ~(first * 16 + count - 1); an
     // empty slot has an inverted box.
     hvec<float> bvh;                 // [nodes*32]
-    hvec<float> bvhq;                // [nodes*16]: the same tree with 8-bit child boxes (64-byte nodes)
+    hvec<float> bvhq;                // [nodes*12]: the same tree with 8-bit child boxes (48-byte nodes; empty
+                                     // when the triangle ids need more than 24 bits)
     int bvh_nodes = 0, bvh_leaves = 0, bvh_depth = 0;
     double c = 343, rho = 1.2, rho_c = 411.6, atten[kBands] = {0};
     double scale = 1;                // largest box extent
@@ -100,7 +101,7 @@ struct HostScene {
 
 constexpr int kBvhStack = 64;
 constexpr int kBvhNodeFloats = 32;
-constexpr int kBvhQNodeFloats = 16;
+constexpr int kBvhQNodeFloats = 12;  // 48-byte quantised nodes
 constexpr int kLeafMax = 8;      // largest leaf the node encoding holds
 constexpr int kLeafDefault = 3;  // leaf size used when the scene does not ask for one (measured best of 2..8)
 
@@ -112,7 +113,7 @@ struct DevScene {
     const float4 *mat;          // [npoly*8]: (1-alpha, s_lo, s_mid, s_hi)
     const float *trans;         // [npoly*8]
     const float4 *bvh;          // [nodes*8] 128-byte nodes
-    const float4 *bvhq;         // [nodes*4] 64-byte quantised nodes (null: walk the 128-byte ones)
+    const float4 *bvhq;         // [nodes*3] 48-byte quantised nodes (null: walk the 128-byte ones)
     int ntri;
     float t_eps;
     int has_trans;
@@ -338,7 +339,7 @@ cudaError_t launch_sort(const DevRun &r, int blocks, cudaStream_t s);  // count 
 // scenes of more than kSpecMinTris triangles: measured on a 20k-triangle hall it walks 1.5x faster than
 // one leaf at a time, while on a 12-triangle shoebox (a two-level tree) it is 10 % slower.
 constexpr int kSpecMinTris = 64;
-// quantised: walk the 64-byte nodes (variants for 4 and 6 blocks per SM), + 32.
+// quantised: walk the 48-byte nodes (variants for 4 and 6 blocks per SM), + 32.
 inline int trace_variant(int blocks_per_sm, int traversal, int ntri, bool quantised = false) {
     // default: 6 blocks of 256 (40 registers) on the smaller quantised nodes (+2.5 % on a 20k-triangle
     // hall), 4 (64 registers) on 128-byte nodes (+23 %)
@@ -348,7 +349,7 @@ inline int trace_variant(int blocks_per_sm, int traversal, int ntri, bool quanti
     if (spec) return 16 + (minb >= 6 ? 6 : 4);
     return minb;
 }
-// bvh_format of pach_trace_params: 0 default, 1 128-byte float nodes, 2 64-byte quantised nodes.
+// bvh_format of pach_trace_params: 0 default, 1 128-byte float nodes, 2 48-byte quantised nodes.
 // The default walks quantised nodes above kQuantMinTris triangles: measured +6 % walk rate on a
 // 20k-triangle hall and +8 % on a 500k-triangle arena (L1-bound walks), -37 % on a 12-triangle
 // shoebox (a two-node tree: the decode costs, the smaller nodes save nothing).

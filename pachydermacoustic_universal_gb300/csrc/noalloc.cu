@@ -227,7 +227,7 @@ extern "C" pach_status pach_trace_run_noalloc(const pach_scene *scene, const pac
 
         int sms = 0, bps_tr = 0, bps_sh = 0;
         NA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        const bool quant = use_quantised_nodes(p.bvh_format, (int)hs.tri_poly.size());
+        const bool quant = use_quantised_nodes(p.bvh_format, (int)hs.tri_poly.size()) && r.S.bvhq != nullptr;
         if (!quant) r.S.bvhq = nullptr;
         const int variant = trace_variant(p.blocks_per_sm, p.traversal, (int)hs.tri_poly.size(), quant);
         NA_TRY(wave_kernel_occupancy(variant, 256, receiver_smem_bytes(n_receivers), &bps_tr, &bps_sh,

@@ -7,6 +7,7 @@
 // Voxel_Grid as the nearest-hit structure (any structure that returns the nearest hit with t > eps
 // gives the same answer).  Air properties follow Uniform_Medium (Classes_Medium_Props.cs:286-299).
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <cmath>
 #include <cstring>
@@ -409,6 +410,24 @@ void build_bvh(HostScene &hs, int leaf_max) {
         else
             for (int n = first_new; n < (int)order4.size(); ++n) todo.push_back(n);
     }
+    // Leaf triangles in node order: the leaves that are children of one 4-wide node sit together, in
+    // slot order, so a quantised node names them by one base index and per-slot counts.  (The empty
+    // leaf of a wrapped leaf root holds no triangle.)
+    std::vector<int> leaf_first(B.nodes.size(), 0);
+    {
+        std::vector<int> norder;
+        norder.reserve((size_t)hs.ntri);
+        for (size_t q = 0; q < order4.size(); ++q)
+            for (int k = 0; k < nkids4[q]; ++k) {
+                const int kid = kids4[q][k];
+                const BNode &x = B.nodes[kid];
+                if (x.left >= 0) continue;
+                leaf_first[kid] = (int)norder.size();
+                if (x.lo[0] > x.hi[0]) continue;
+                for (int t = 0; t < x.count; ++t) norder.push_back(B.order[x.first + t]);
+            }
+        B.order.swap(norder);
+    }
     const int max_depth4 = *std::max_element(depth4.begin(), depth4.end());
     const double pad = 2e-6 * hs.scale;
     auto lo_f = [&](double v) { return v > 1e299 ? INFINITY : (float)(v - pad); };
@@ -425,7 +444,7 @@ void build_bvh(HostScene &hs, int leaf_max) {
                     f[0 + k] = lo_f(x.lo[0]); f[4 + k] = hi_f(x.hi[0]);
                     f[8 + k] = lo_f(x.lo[1]); f[12 + k] = hi_f(x.hi[1]);
                     f[16 + k] = lo_f(x.lo[2]); f[20 + k] = hi_f(x.hi[2]);
-                    code = x.left >= 0 ? id4[kq[k]] : ~(x.first * 16 + (x.count - 1));
+                    code = x.left >= 0 ? id4[kq[k]] : ~(leaf_first[kq[k]] * 16 + (x.count - 1));
                 } else {  // empty slot: flagged by its code (a slab test cannot reject an inverted box)
                     f[0 + k] = f[4 + k] = f[8 + k] = f[12 + k] = f[16 + k] = f[20 + k] = 0.f;
                     code = (int)0x80000000;
@@ -455,27 +474,36 @@ void build_bvh(HostScene &hs, int leaf_max) {
     hs.tri_plane.swap(tl);
 }
 
-// 64-byte copy of the 4-wide BVH: per node a frame (origin of the children's union box and a
-// power-of-two step s = 2^e per axis, 255 steps spanning it) and each child's box as 8-bit steps, the
-// lower bound rounded down and the upper rounded up, at least s / 256 outside the float box: the walk
+// 48-byte copy of the 4-wide BVH: per node a frame (origin of the children's union box and a
+// power-of-two step s = 2^e per axis, 255 steps spanning it), each child's box as 8-bit steps, the
+// lower bound rounded down and the upper rounded up, at least s / 256 outside the float box (the walk
 // folds the byte decode's bias into the slab offset, one rounding of at most 2^-9 s, so a decoded box
-// still contains the float box.  The stored exponent is that of 2^(e - 8) = s / 256, the scale of a
-// byte decoded as 2^23 + 256 q.
-//   float4 (origin x, y, z, biased exponents ex | ey << 8 | ez << 16 as bits)
+// still contains the float box), and the children as one base index each for inner nodes and leaf
+// triangles plus a 4-bit code per slot.  The stored exponent is that of 2^(e - 8) = s / 256, the scale
+// of a byte decoded as 2^23 + 256 q.
+//   float4 (origin x, y, z, bits: ex | ey << 8 | ez << 16 | slot codes 0-1 << 24)
 //   uint4  (lo.x of children 0-3 as bytes, hi.x, lo.y, hi.y)
-//   uint4  (lo.z, hi.z, 0, 0)
-//   int4   child codes (as the 128-byte nodes)
-static void quantize_nodes(HostScene &hs, size_t q0, size_t q1);
+//   uint4  (lo.z, hi.z, first inner child's node id, first leaf triangle | slot codes 2-3 << 24)
+// Slot code: 0 inner child (the node ids of a node's inner children are consecutive), 1-8 a leaf of
+// that many triangles (a node's leaves' triangles are consecutive), 15 empty.  A scene whose triangle
+// ids need more than 24 bits keeps no quantised copy.
+static bool quantize_nodes(HostScene &hs, size_t q0, size_t q1);
 
 void quantize_bvh(HostScene &hs) {
     const size_t nodes = hs.bvh.size() / kBvhNodeFloats;
     hs.bvhq.resize(nodes * kBvhQNodeFloats);  // every float of every node is written
+    std::atomic<bool> ok{hs.ntri < (1 << 24)};
     // nodes are independent: large trees are quantised in chunks on several threads
-    parallel_chunks(nodes, 8192, [&hs](size_t q0, size_t q1) { quantize_nodes(hs, q0, q1); });
+    parallel_chunks(nodes, 8192, [&hs, &ok](size_t q0, size_t q1) {
+        if (!quantize_nodes(hs, q0, q1)) ok = false;
+    });
+    if (!ok) hs.bvhq.clear();
 }
 
-// Quantised copy of nodes [q0, q1) (see quantize_bvh).
-static void quantize_nodes(HostScene &hs, size_t q0, size_t q1) {
+// Quantised copy of nodes [q0, q1) (see quantize_bvh); false if a node's children do not fit the
+// base-and-count form.
+static bool quantize_nodes(HostScene &hs, size_t q0, size_t q1) {
+    bool fits = true;
     for (size_t q = q0; q < q1; ++q) {
         const float *f = &hs.bvh[q * kBvhNodeFloats];
         int code[4];
@@ -491,6 +519,28 @@ static void quantize_nodes(HostScene &hs, size_t q0, size_t q1) {
                 hi[a] = std::max(hi[a], (double)f[8 * a + 4 + k]);
             }
         }
+        // children: base ids and slot codes
+        uint32_t slots = 0;
+        int nbase = -1, tbase = -1, ninner = 0, ntris = 0;
+        for (int k = 0; k < 4; ++k) {
+            uint32_t v = 15;
+            if (valid[k] && code[k] >= 0) {
+                if (nbase < 0) nbase = code[k];
+                fits = fits && code[k] == nbase + ninner;
+                ++ninner;
+                v = 0;
+            } else if (valid[k]) {
+                const int c = ~code[k], first = c >> 4, cnt = (c & 15) + 1;
+                if (tbase < 0) tbase = first;
+                fits = fits && first == tbase + ntris && cnt <= 8;
+                ntris += cnt;
+                v = (uint32_t)cnt;
+            }
+            slots |= v << (4 * k);
+        }
+        if (nbase < 0) nbase = 0;
+        if (tbase < 0) tbase = 0;
+        fits = fits && tbase + ntris <= (1 << 24);
         float origin[3] = {0.f, 0.f, 0.f};
         int ebias[3] = {127, 127, 127};
         uint32_t qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0};  // 4 children x 8 bits each
@@ -535,12 +585,14 @@ static void quantize_nodes(HostScene &hs, size_t q0, size_t q1) {
         g[0] = origin[0];
         g[1] = origin[1];
         g[2] = origin[2];
-        const uint32_t ex = (uint32_t)ebias[0] | ((uint32_t)ebias[1] << 8) | ((uint32_t)ebias[2] << 16);
+        const uint32_t ex = (uint32_t)ebias[0] | ((uint32_t)ebias[1] << 8) | ((uint32_t)ebias[2] << 16) |
+                            ((slots & 255u) << 24);
         std::memcpy(&g[3], &ex, 4);
-        const uint32_t words[8] = {qlo[0], qhi[0], qlo[1], qhi[1], qlo[2], qhi[2], 0u, 0u};
+        const uint32_t words[8] = {qlo[0], qhi[0], qlo[1], qhi[1], qlo[2], qhi[2], (uint32_t)nbase,
+                                   ((uint32_t)tbase & 0xFFFFFFu) | ((slots >> 8) << 24)};
         std::memcpy(&g[4], words, sizeof(words));
-        std::memcpy(&g[12], code, sizeof(code));
     }
+    return fits;
 }
 
 }  // namespace
