@@ -428,9 +428,8 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomPar
                                                   const int *rid, float3 o, float3 d, float tseg, double t_sum,
                                                   float Iabs, int oct, int mask, uint32_t prim) {
     uint32_t n = 0;
-    const int s1 = P.rec_begin + P.R;
     if constexpr (!GROUPED) {
-        for (int s = P.rec_begin; s < s1; ++s) {
+        for (int s = P.rec_begin; s < P.rec_begin + P.R; ++s) {
             const float4 c = rec[s];
             float t, half;
             if (!sphere_hit(c, o, d, tseg, t, half)) continue;
@@ -439,6 +438,7 @@ __device__ __forceinline__ uint32_t detect_octave(const DevRun &r, const RoomPar
         }
         return n;
     }
+    const int s1 = P.rec_begin + P.R;
     int s0 = P.rec_begin;
     for (; s0 + 4 <= s1; s0 += 4) {
         bool near[4];
