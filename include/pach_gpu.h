@@ -218,7 +218,7 @@ typedef struct {
     int64_t tri_tests;             /* octave-ray traversal work: triangles tested */
     double wall_ms;
     int32_t accel[3];              /* BVH inner nodes, leaves, depth */
-    int32_t walk;                  /* the walk used: BVH node bytes (64 or 128) + 1000 x traversal (1-3) */
+    int32_t walk;                  /* the walk used: BVH node bytes (48 or 128) + 1000 x traversal (1-3) */
     int64_t revolutions;           /* convergence mode: revolutions traced (primaries = revolutions x period) */
     int32_t converged;             /* convergence mode: 1 when the checks agreed, 0 when max_rays stopped it */
     int32_t check_receivers[2];    /* convergence mode: receivers of the two checks (-1: none) */

@@ -924,7 +924,7 @@ void run_worker_body(pach_run *run) {
         s.accel[0] = (int32_t)(n_rooms > 1 ? run->bbvh.bytes / (kBvhNodeFloats * sizeof(float)) : hs.bvh_nodes);
         s.accel[1] = hs.bvh_leaves;
         s.accel[2] = hs.bvh_depth;
-        s.walk = (quant ? 64 : 128) + 1000 * (fused ? 3 : ((tr_variant & 16) ? 2 : 1));
+        s.walk = (quant ? 4 * kBvhQNodeFloats : 4 * kBvhNodeFloats) + 1000 * (fused ? 3 : ((tr_variant & 16) ? 2 : 1));
         s.revolutions = conv_mode ? run->conv_revs : 0;
         s.converged = conv_mode && run->conv_converged ? 1 : 0;
         s.check_receivers[0] = conv_mode ? run->conv_rows[0] : -1;
