@@ -214,8 +214,9 @@ typedef struct {
     int64_t waves;                 /* wavefront iterations that traced octave rays */
     int64_t kernel_launches;
     int64_t peak_live_rays;        /* most octave rays held in the ring at once */
-    int64_t bvh_nodes_visited;     /* octave-ray traversal work: inner BVH nodes visited */
-    int64_t tri_tests;             /* octave-ray traversal work: triangles tested */
+    int64_t bvh_nodes_visited;     /* octave-ray traversal work: inner BVH nodes visited, and */
+    int64_t tri_tests;             /* triangles tested (counted when kernel_timing = 1; else 0 on
+                                      scenes walked by the speculative walk) */
     double wall_ms;
     int32_t accel[3];              /* BVH inner nodes, leaves, depth */
     int32_t walk;                  /* the walk used: BVH node bytes (48 or 128) + 1000 x traversal (1-3) */

@@ -590,6 +590,7 @@ void run_worker_body(pach_run *run) {
         r.prop_mix = (float)(run->p.proposal_mix > 0 ? run->p.proposal_mix : 0.3);
         r.capture = run->p.capture ? run->dcap.as<float>() : nullptr;
         r.capture_mode = run->p.capture;
+        r.count_work = run->p.kernel_timing != 0;
         {
             const bool given = run->p.capture_edges_ms[0] != 0 || run->p.capture_edges_ms[1] != 0 ||
                                run->p.capture_edges_ms[2] != 0;

@@ -286,6 +286,7 @@ struct DevRun {
     int conv_row[2];               // histogram rows of the check receivers (-1: none)
     int conv_oct;
     long long conv_period;         // primaries per revolution
+    int count_work;                // 1: the walk counts its node visits and triangle tests (kernel-timing runs)
 };
 
 constexpr int kLobes = PACH_MLP_LOBES;

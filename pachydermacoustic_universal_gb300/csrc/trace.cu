@@ -429,7 +429,8 @@ constexpr int kSpecSlack = 10;
 // item at once (one ticket atomic per warp), so a warp does not idle on its slowest lane.
 // Values the walk needs only when a ray starts or ends, once per leaf or once per warp iteration live
 // in shared memory (each lane's wave index, the plane it leaves and its hit tolerance; each warp's node
-// and triangle counts), not in registers: the walk's 40 registers already spill.
+// and triangle counts), not in registers: the walk's 40 registers already spill.  The counts are taken
+// in kernel-timing runs only (r.count_work): they cost a ballot and a shared-memory update per pass.
 template <int MINB, bool SPEC, bool QUANT>
 __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
     __shared__ unsigned s_item[256];
@@ -501,8 +502,10 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 // looking, so it ends)
                 const int looking = __popc(__ballot_sync(FULL, have && node >= 0 && leaf == 0));
                 if (looking == 0 || (looking <= kSpecSlack && __any_sync(FULL, have && leaf != 0))) break;
-                const unsigned stepping = __ballot_sync(FULL, have && node >= 0);
-                if (lane == 0) s_cnt[wid][0] += (unsigned)__popc(stepping);
+                if (r.count_work) {
+                    const unsigned stepping = __ballot_sync(FULL, have && node >= 0);
+                    if (lane == 0) s_cnt[wid][0] += (unsigned)__popc(stepping);
+                }
                 if (have && node >= 0) {
                     int next;
                     if (QUANT ? bvh4q_step(S.bvhq, node, ix, iy, iz, o.x, o.y, o.z, best, stack, sp, next)
@@ -516,8 +519,10 @@ __global__ void __launch_bounds__(256, MINB) k_trace(DevRun r) {
                 }
             }
             const bool testing = have && leaf != 0;
-            const unsigned ntri = __reduce_add_sync(FULL, testing ? (unsigned)(((~leaf) & 15) + 1) : 0u);
-            if (lane == 0) s_cnt[wid][1] += ntri;
+            if (r.count_work) {
+                const unsigned ntri = __reduce_add_sync(FULL, testing ? (unsigned)(((~leaf) & 15) + 1) : 0u);
+                if (lane == 0) s_cnt[wid][1] += ntri;
+            }
             if (testing) {
                 const int code = ~leaf;
                 const int f0 = code >> 4, cnt = (code & 15) + 1;
