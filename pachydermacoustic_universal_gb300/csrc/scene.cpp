@@ -426,7 +426,11 @@ void build_bvh(HostScene &hs, int leaf_max) {
                 if (x.lo[0] > x.hi[0]) continue;
                 for (int t = 0; t < x.count; ++t) norder.push_back(B.order[x.first + t]);
             }
-        B.order.swap(norder);
+        if (norder.size() == B.order.size()) {
+            B.order.swap(norder);
+        } else {  // not every triangle reached once: keep the builder's order (no quantised copy then)
+            for (size_t n = 0; n < B.nodes.size(); ++n) leaf_first[n] = B.nodes[n].first;
+        }
     }
     const int max_depth4 = *std::max_element(depth4.begin(), depth4.end());
     const double pad = 2e-6 * hs.scale;
